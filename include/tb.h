@@ -1,0 +1,201 @@
+/*
+ * tb.h -- C ABI of the GB300 tropical contraction engine.
+ *
+ * This is the drop-in boundary for the hot path of TensorBranching.jl's
+ * dynamic_ob_mis: the tropical (max,+) contraction of the independent-set
+ * tensor network of every slice / branch, plus "+ r" and the max over slices.
+ *
+ * Reference interfaces it replaces (paths inside the TensorBranching.jl tree):
+ *   solve_slice(branch, element_type, usecuda)::T      src/dynamic_ob.jl:30-34
+ *     GenericTensorNetwork(IndependentSet(g, w), uncompress(code), Dict())
+ *     solve(net, SizeMax(), T = element_type, usecuda)  src/dynamic_ob.jl:31-32
+ *   contract_slices(branches, element_type, usecuda)    src/dynamic_ob.jl:36-48
+ *   maximum(res)                                        src/dynamic_ob.jl:27
+ *   CompressedEinsum{ixs, iy, ct} / uncompress          src/types.jl:51-79
+ *   SlicedBranch{p, code, r}                            src/types.jl:85-103
+ *
+ * Conventions.  Labels are dense ids 0..n_labels-1 (a Julia caller passes
+ * vertex v as v-1).  Every label has dimension 2.  Tensors are column-major:
+ * the first label of a tensor is its fastest index.  A network is given as
+ * its leaf tensors (ixs), its open labels (iy; empty for the MIS scalar) and a
+ * binary contraction tree in post-order pairs: internal node j has children
+ * children[2j], children[2j+1]; ids < n_tensors are leaves, id n_tensors + k
+ * is internal node k < j; the last internal node is the root.
+ *
+ * Tensor contents for the MIS path (GenericTensorNetworks IndependentSet):
+ * a leaf with one label v is the vertex tensor [0, w_v]; a leaf with two
+ * labels is the edge tensor [[0,0],[0,-inf]] (a self-loop [v,v] is its
+ * diagonal [0,-inf]).
+ *
+ * Errors.  Every entry point returns tb_status; no C++ exception crosses the
+ * ABI.  tb_last_error(ctx) returns a message for the last failure on that
+ * context (thread-local to the calling thread).  A context is used by one
+ * host thread at a time, except the streaming calls tb_submit / tb_poll /
+ * tb_wait, which may be called from any thread.  Plans are immutable after
+ * tb_plan_bind_mis and may be shared between calls.
+ *
+ * Memory.  The library copies every input array; callers keep ownership of
+ * what they pass.  Output arrays are host memory written before return.
+ */
+#ifndef TB_H
+#define TB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t tb_status;
+#define TB_OK 0
+#define TB_ERR_INVALID 1     /* malformed plan or argument */
+#define TB_ERR_OOM 2         /* device memory budget exceeded */
+#define TB_ERR_TIMEOUT 3     /* a bounded device-side wait ran out */
+#define TB_ERR_CUDA 4        /* a CUDA runtime call failed */
+#define TB_ERR_UNSUPPORTED 5 /* valid request outside this build's limits */
+#define TB_ERR_BUSY 6        /* streaming queue full */
+
+#define TB_DTYPE_F32 0 /* Tropical{Float32}: -inf is the additive zero */
+#define TB_DTYPE_I32 1 /* int32 with sentinel TB_I32_NEG standing for -inf */
+#define TB_I32_NEG (-536870912)
+
+/* Execution modes of tb_solve_batch. */
+#define TB_MODE_PLAIN 0   /* drop-in: one item at a time, per-contraction launches
+                             (permute + batched tropical GEMM + permute), result
+                             copied back after each item, as the reference's loop */
+#define TB_MODE_BATCHED 1 /* every item in one persistent launch over a device
+                             work queue, replayed from a captured CUDA graph */
+#define TB_MODE_LAYERED 2 /* fused per-contraction launches over all items,
+                             captured in a CUDA graph */
+
+typedef struct tb_ctx tb_ctx;
+typedef struct tb_plan tb_plan;
+
+typedef struct tb_options {
+  int32_t dtype;            /* TB_DTYPE_* */
+  int32_t use_graphs;       /* 1: capture batched launches in CUDA graphs */
+  int64_t max_device_bytes; /* arena budget; 0 = 80% of free memory at create */
+  int32_t timeout_ms;       /* bound on every device-side wait (default 20000) */
+  int32_t autotune;         /* 1: choose tile shapes by timing (cached per shape) */
+  int32_t persistent_ctas;  /* CTAs of the persistent executor; 0 = 2 per SM */
+  int32_t reserved[9];
+} tb_options;
+
+typedef struct tb_plan_stats {
+  double tc;              /* log2 sum over nodes of 2^|labels(node)| */
+  double sc;              /* log2 of the largest tensor */
+  double rwc;             /* log2 of total elements read + written */
+  double ops;             /* algorithmic tropical ops per item: 2 per (max,+) pair */
+  double bytes;           /* algorithmic bytes per item: 4 (|A|+|B|+|C|) per node */
+  int64_t arena_bytes;    /* device bytes one item of this plan occupies */
+  int32_t n_steps;        /* compiled contraction steps */
+  int32_t n_tensors;
+  int32_t n_open;         /* labels left open in the root tensor */
+  int32_t n_sliced;       /* labels fixed per item by tb_solve_batch */
+  int32_t n_tiles;        /* CTA tiles of one item in the fused form */
+  int32_t reserved[7];
+} tb_plan_stats;
+
+/* Fill *opt with defaults (f32, graphs on, autotune on). */
+void tb_options_default(tb_options* opt);
+
+/* Create / destroy a context bound to CUDA device `device`. */
+tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out);
+void tb_ctx_destroy(tb_ctx* ctx);
+const char* tb_last_error(const tb_ctx* ctx);
+/* Library version string, e.g. "tb 0.1 sm_103a". */
+const char* tb_version(void);
+
+/*
+ * Compile a contraction plan.
+ *   ixs       : n_tensors leaf label lists, CSR (ix_off[n_tensors+1], ix_lab)
+ *   iy        : n_iy open labels of the result (empty for the MIS value)
+ *   children  : n_nodes = n_tensors - 1 post-order pairs (see above)
+ *   node_iy   : optional explicit output labels of every internal node (CSR
+ *               node_iy_off[n_nodes+1], node_iy_lab), e.g. the eins.iy of each
+ *               node of an OMEinsum DynamicNestedEinsum; NULL derives them as
+ *               the labels of (left ∪ right), in that order, still needed
+ *               outside the subtree or open in iy
+ *   sliced    : n_sliced labels fixed per item (index slicing); each item of
+ *               tb_solve_batch gives their 0/1 values
+ * Replaces: uncompress (src/types.jl:75-79) + GenericTensorNetwork(...)
+ * construction (src/dynamic_ob.jl:31).
+ */
+tb_status tb_plan_create(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const int32_t* ix_off,
+                         const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
+                         const int32_t* children, const int32_t* node_iy_off,
+                         const int32_t* node_iy_lab, int32_t n_sliced, const int32_t* sliced,
+                         tb_plan** out);
+void tb_plan_destroy(tb_plan* plan);
+tb_status tb_plan_stats_get(const tb_plan* plan, tb_plan_stats* out);
+
+/*
+ * Output labels of internal node j (after slicing), for reading dumps.
+ * Writes up to cap labels to labels_out and their count to *n_out.
+ */
+tb_status tb_plan_node_labels(const tb_plan* plan, int32_t node, int32_t cap, int32_t* labels_out,
+                              int32_t* n_out);
+
+/*
+ * Bind vertex weights (n_labels floats, indexed by label) for the MIS leaf
+ * tensors.  Replaces IndependentSet(g, weights) (src/dynamic_ob.jl:31).
+ * Weights must be finite; in TB_DTYPE_I32 they must be integers.
+ */
+tb_status tb_plan_bind_mis(tb_plan* plan, const float* weights);
+
+/*
+ * Solve a batch of n items.  Item i contracts plans[i] with its sliced labels
+ * fixed to slice_vals[sv_off_i .. sv_off_i + n_sliced_i) (items concatenated
+ * in order; NULL when no plan slices), and returns
+ *   out_item[i] = max(root tensor of item i) + r[i]
+ * and *out_max = max_i out_item[i] (either pointer may be NULL; r may be NULL
+ * for zeros).  A plan whose graph is empty (n_tensors == 0 is not allowed;
+ * callers skip such items and use r directly, as contract_slices does at
+ * src/dynamic_ob.jl:39-40).
+ * Replaces: contract_slices (src/dynamic_ob.jl:36-48) and maximum(res)
+ * (src/dynamic_ob.jl:27); with n == 1 and mode PLAIN, solve_slice.
+ */
+tb_status tb_solve_batch(tb_ctx* ctx, int32_t n, tb_plan* const* plans, const int8_t* slice_vals,
+                         const float* r, float* out_item, float* out_max, int32_t mode);
+
+/*
+ * Contract one plan with explicit leaf tensors (host arrays, leaf i holding
+ * 2^|ixs[i]| values, Tropical semantics: -inf is zero).  Writes the root
+ * tensor (2^n_iy values, labels in iy order) to out.  The test form
+ * `code(tensors...)` (test/utils.jl:34, test/decompose.jl:28).  Sliced plans
+ * are not accepted here.
+ */
+tb_status tb_contract(tb_ctx* ctx, tb_plan* plan, const float* const* leaf_data, float* out,
+                      int32_t mode);
+
+/*
+ * Run one item (MIS leaves) and copy every internal node's tensor to host:
+ * node_out[j] receives 2^|labels(j)| values in the order tb_plan_node_labels
+ * reports.  Entries of node_out may be NULL to skip a node.
+ */
+tb_status tb_dump_intermediates(tb_ctx* ctx, tb_plan* plan, const int8_t* slice_vals,
+                                float* const* node_out, int32_t mode);
+
+/*
+ * Time the last tb_solve_batch's device work: kernel-only milliseconds of
+ * the most recent call (CUDA events around the device work, excluding host
+ * copies), and the number of kernel launches it made.
+ */
+tb_status tb_last_timing(const tb_ctx* ctx, double* device_ms, int64_t* launches);
+
+/*
+ * Standalone batched tropical GEMM (the K1 kernel), device pointers:
+ *   C[m + M n + M N b] = max_k A[m + M k + M K b] + B[k + K n + K N b]
+ * for b < batch.  M, N, K >= 1.  `stream` is a cudaStream_t (NULL: default).
+ * Uses the dtype of ctx.  Exposed for benchmarking the kernel at dense
+ * square shapes.
+ */
+tb_status tb_gemm_device(tb_ctx* ctx, int64_t M, int64_t N, int64_t K, int64_t batch,
+                         const void* A, const void* B, void* C, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TB_H */

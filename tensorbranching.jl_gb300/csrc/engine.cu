@@ -1,0 +1,1033 @@
+// Engine: contexts, plans, execution modes and the C ABI of include/tb.h.
+//
+// Execution modes of tb_solve_batch (contract_slices, src/dynamic_ob.jl:36-48):
+//   PLAIN    one item at a time; per contraction node the OMEinsum lowering
+//            (permute kernels + K1 batched max-plus GEMM + permute), result
+//            copied to the host after every item -- the reference's
+//            one-contraction-at-a-time GPU loop, as a drop-in.
+//   LAYERED  fused tile kernels, one launch per tree level covering every
+//            item, captured in a CUDA graph.
+//   BATCHED  one persistent launch: CTAs take tickets in dependency order
+//            from a device work queue, wait (bounded) on per-step completion
+//            counters, run fused tiles; captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/tb.h"
+#include "kernels.cuh"
+#include "plan.h"
+
+using namespace tb;
+
+// ---------------------------------------------------------------------------
+// kernels (thin __global__ wrappers over the device routines)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_leaves(const LeafDesc* leaves, int n, const int8_t* sv, T* arena) {
+  leaves_tile<T>(leaves, n, sv, arena, blockIdx.x);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_tile(const TileDesc d, T* arena) {
+  extern __shared__ int tb_smem[];
+  stream_tile<T>(d, blockIdx.x, arena, tb_smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_final(const FinalDesc f, const T* arena, float r, float* out) {
+  final_tile<T>(f, arena, r, out);
+}
+
+// K4: max over per-item results (warp-shuffle tree).
+__global__ void __launch_bounds__(kThreads) k_reduce_max(const float* v, int n, float* out) {
+  __shared__ float wmax[kThreads / 32];
+  float m = __int_as_float(0xff800000);
+  for (int i = threadIdx.x; i < n; i += kThreads) m = fmaxf(m, v[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = wmax[0];
+    for (int w = 1; w < kThreads / 32; w++) b = fmaxf(b, wmax[w]);
+    *out = b;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, int64_t tile, int* smem,
+                                         float* out_item, int item) {
+  switch (st.kind) {
+    case STEP_LEAVES:
+      leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile);
+      break;
+    case STEP_TILE:
+      stream_tile<T>(it.tiles[st.desc], tile, it.arena, smem);
+      break;
+    case STEP_FINAL:
+      final_tile<T>(it.fin, it.arena, it.r, out_item + item);
+      break;
+    default:
+      break;
+  }
+}
+
+__device__ __forceinline__ int find_group(const Group* groups, int n_groups, int64_t tk) {
+  int lo = 0, hi = n_groups - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (groups[mid].first <= tk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One launch per tree level: block b runs ticket first_ticket + b.  No
+// waiting: the previous launch on the stream finished every dependency.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
+                                                   int64_t first_ticket, float* out_item) {
+  extern __shared__ int tb_smem[];
+  __shared__ int s_g;
+  int64_t tk = first_ticket + blockIdx.x;
+  if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
+  __syncthreads();
+  const Group g = groups[s_g];
+  const ItemDev<T>& it = items[g.item];
+  run_step<T>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, g.item);
+}
+
+// Persistent executor.  Tickets are handed out in dependency order, so a
+// ticket only waits on tickets already held by running CTAs; every wait is
+// bounded by timeout_ns and ends with err set instead of hanging.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_persistent(const ItemDev<T>* items, const Group* groups, int n_groups,
+                                                        int64_t n_tickets, int* done, unsigned long long* ticket,
+                                                        int* err, float* out_item, int64_t timeout_ns) {
+  extern __shared__ int tb_smem[];
+  __shared__ long long s_tk;
+  __shared__ int s_g, s_stop;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long tk = (long long)atomicAdd(ticket, 1ull);
+      int stop = (tk >= n_tickets) || (*(volatile int*)err != 0);
+      int gi = 0;
+      if (!stop) {
+        gi = find_group(groups, n_groups, tk);
+        const Group g = groups[gi];
+        const ItemDev<T>& it = items[g.item];
+        const Step st = it.steps[g.step];
+        const int deps[2] = {st.dep0, st.dep1};
+        uint64_t t0 = globaltimer();
+        for (int d = 0; d < 2 && !stop; d++) {
+          if (deps[d] < 0) continue;
+          const int need = it.steps[deps[d]].n_tiles;
+          const int* cnt = done + it.done_base + deps[d];
+          while (ld_acquire(cnt) < need) {
+            if (*(volatile int*)err != 0) { stop = 1; break; }
+            if (globaltimer() - t0 > (uint64_t)timeout_ns) {
+              atomicExch(err, TB_ERR_TIMEOUT);
+              stop = 1;
+              break;
+            }
+            __nanosleep(128);
+          }
+        }
+      }
+      s_tk = tk;
+      s_g = gi;
+      s_stop = stop;
+    }
+    __syncthreads();
+    if (s_stop) break;
+    const Group g = groups[s_g];
+    const ItemDev<T>& it = items[g.item];
+    run_step<T>(it, it.steps[g.step], s_tk - g.first, tb_smem, out_item, g.item);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(done + it.done_base + g.step, 1);
+  }
+}
+
+template <typename T, int BM, int BN>
+static cudaError_t launch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
+                             cudaStream_t s) {
+  using Cfg = K1Cfg<T, BM, BN>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(gemm_k1<T, BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES);
+    attr = true;
+  }
+  int64_t tiles_mn = (M / BM) * (N / BN);
+  int64_t grid = tiles_mn * batch;
+  if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  gemm_k1<T, BM, BN><<<(unsigned)grid, 256, Cfg::SMEM_BYTES, s>>>(A, B, C, (int)M, (int)N, (int)K, tiles_mn);
+  return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
+                               cudaStream_t s) {
+  int bm = M >= 128 ? 128 : M >= 64 ? 64 : M >= 32 ? 32 : 16;
+  int bn = N >= 128 ? 128 : N >= 64 ? 64 : N >= 32 ? 32 : 16;
+#define K1_CASE(X, Y) \
+  if (bm == X && bn == Y) return launch_k1<T, X, Y>(A, B, C, M, N, K, batch, s);
+  K1_CASE(128, 128) K1_CASE(128, 64) K1_CASE(128, 32) K1_CASE(128, 16)
+  K1_CASE(64, 128) K1_CASE(64, 64) K1_CASE(64, 32) K1_CASE(64, 16)
+  K1_CASE(32, 128) K1_CASE(32, 64) K1_CASE(32, 32) K1_CASE(32, 16)
+  K1_CASE(16, 128) K1_CASE(16, 64) K1_CASE(16, 32) K1_CASE(16, 16)
+#undef K1_CASE
+  return cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------
+// host objects
+// ---------------------------------------------------------------------------
+namespace {
+
+thread_local std::string g_err;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+};
+
+struct HostBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~HostBuf() { if (p) cudaFreeHost(p); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(&p, bytes);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+};
+
+}  // namespace
+
+struct tb_plan {
+  tb_ctx* ctx = nullptr;
+  PlanHost h;
+  DevBuf d_steps, d_tiles, d_gemms, d_leaves;
+  bool uploaded = false;
+  uint64_t version = 0;  // bumps on bind
+};
+
+struct GraphKey {
+  std::vector<const tb_plan*> plans;
+  std::vector<uint64_t> versions;
+  int mode = 0;
+  bool operator==(const GraphKey& o) const { return plans == o.plans && versions == o.versions && mode == o.mode; }
+};
+
+struct tb_ctx {
+  int device = 0;
+  tb_options opt{};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int sms = 0;
+  int persistent_ctas = 0;
+  size_t budget = 0;
+  DevBuf arena, items, groups, done, misc, slice_vals, out_item;
+  HostBuf h_items, h_groups, h_in, h_out;
+  // batch state of the last upload (reused when the same plans come again)
+  GraphKey key;
+  bool have_key = false;
+  int64_t n_tickets = 0;
+  int n_groups = 0;
+  std::vector<std::pair<int64_t, int64_t>> level_ranges;  // (first ticket, count)
+  size_t sv_bytes = 0;
+  int n_items = 0;
+  cudaGraphExec_t gexec = nullptr;
+  double last_ms = 0;
+  int64_t last_launches = 0;
+  int64_t launches_graph = 0;
+  uint64_t plan_counter = 0;
+  std::mutex mu;
+};
+
+static tb_status fail(tb_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+#define CU(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess)                                                                      \
+      return fail(TB_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));                \
+  } while (0)
+
+static int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+template <typename T>
+static size_t elem() { return sizeof(T); }
+
+static size_t dtype_size(const tb_ctx*) { return 4; }
+
+static int max_stream_smem_bytes() {
+  // largest dynamic shared memory a stream tile may ask for (see plan_tile)
+  return (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4;
+}
+
+template <typename T>
+static tb_status set_kernel_attrs() {
+  static bool done = false;
+  if (done) return TB_OK;
+  int sm = max_stream_smem_bytes();
+  CU(cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CU(cudaFuncSetAttribute(k_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CU(cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  done = true;
+  return TB_OK;
+}
+
+static tb_status upload_plan(tb_plan* p) {
+  if (p->uploaded) return TB_OK;
+  auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = b.ensure(bytes);
+    if (e != cudaSuccess) return e;
+    if (src) return cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice);
+    return cudaSuccess;
+  };
+  const PlanHost& h = p->h;
+  CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
+  CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
+  CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
+  CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
+  p->uploaded = true;
+  return TB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plain path (drop-in): one item, per-node launches
+// ---------------------------------------------------------------------------
+template <typename T>
+static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv, bool leaves_from_mis,
+                            int64_t& launches) {
+  const PlanHost& h = p->h;
+  cudaStream_t s = c->stream;
+  if (leaves_from_mis) {
+    k_leaves<T><<<(h.n_tensors + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+        reinterpret_cast<const LeafDesc*>(p->d_leaves.p), h.n_tensors, d_sv, arena);
+    CU(cudaGetLastError());
+    launches++;
+  }
+  if (h.n_nodes == 0) {
+    const TileDesc& d = h.tiles[0];
+    k_tile<T><<<d.n_tiles, kThreads, stream_smem_words(d) * 4, s>>>(d, arena);
+    CU(cudaGetLastError());
+    launches++;
+    return TB_OK;
+  }
+  for (int j = 0; j < h.n_nodes; j++) {
+    for (const PlainOp& op : h.plain[j]) {
+      if (op.kind == PLAIN_TILE) {
+        k_tile<T><<<op.tile.n_tiles, kThreads, stream_smem_words(op.tile) * 4, s>>>(op.tile, arena);
+        CU(cudaGetLastError());
+      } else {
+        CU(dispatch_k1<T>(arena + op.a_off, arena + op.b_off, arena + op.c_off, op.M, op.N, op.K, op.batch, s));
+      }
+      launches++;
+    }
+  }
+  return TB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched upload: items, groups (dependency order), counters
+// ---------------------------------------------------------------------------
+template <typename T>
+static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std::vector<int64_t>& arena_off,
+                              const std::vector<int64_t>& sv_off, const float* r, bool skip_leaves) {
+  // items
+  CU(c->h_items.ensure(sizeof(ItemDev<T>) * n));
+  ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(c->h_items.p);
+  int done_base = 0;
+  for (int i = 0; i < n; i++) {
+    tb_plan* p = plans[i];
+    ItemDev<T> it{};
+    it.arena = reinterpret_cast<T*>(c->arena.p) + arena_off[i];
+    it.steps = reinterpret_cast<const Step*>(p->d_steps.p);
+    it.tiles = reinterpret_cast<const TileDesc*>(p->d_tiles.p);
+    it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
+    it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
+    it.slice_vals = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
+    it.r = r ? r[i] : 0.0f;
+    it.n_leaves = p->h.n_tensors;
+    it.done_base = done_base;
+    it.n_steps = (int)p->h.steps.size();
+    it.fin = p->h.fin;
+    done_base += it.n_steps;
+    hi[i] = it;
+  }
+  // groups sorted by (level, item, step)
+  struct GK { int level, item, step; };
+  std::vector<GK> gk;
+  for (int i = 0; i < n; i++) {
+    const PlanHost& h = plans[i]->h;
+    for (int s = 0; s < (int)h.steps.size(); s++) {
+      if (skip_leaves && h.steps[s].kind == STEP_LEAVES) continue;
+      gk.push_back({h.steps[s].level, i, s});
+    }
+  }
+  std::stable_sort(gk.begin(), gk.end(), [](const GK& a, const GK& b) {
+    if (a.level != b.level) return a.level < b.level;
+    if (a.item != b.item) return a.item < b.item;
+    return a.step < b.step;
+  });
+  CU(c->h_groups.ensure(sizeof(Group) * std::max<size_t>(gk.size(), 1)));
+  Group* hg = reinterpret_cast<Group*>(c->h_groups.p);
+  int64_t tk = 0;
+  c->level_ranges.clear();
+  int cur_level = -1;
+  for (size_t g = 0; g < gk.size(); g++) {
+    hg[g].item = gk[g].item;
+    hg[g].step = gk[g].step;
+    hg[g].first = tk;
+    if (gk[g].level != cur_level) {
+      c->level_ranges.push_back({tk, 0});
+      cur_level = gk[g].level;
+    }
+    int64_t nt = plans[gk[g].item]->h.steps[gk[g].step].n_tiles;
+    tk += nt;
+    c->level_ranges.back().second += nt;
+  }
+  c->n_tickets = tk;
+  c->n_groups = (int)gk.size();
+  CU(c->items.ensure(sizeof(ItemDev<T>) * n));
+  CU(c->groups.ensure(sizeof(Group) * std::max<size_t>(gk.size(), 1)));
+  CU(c->done.ensure(sizeof(int) * std::max(done_base, 1) + 64));
+  CU(cudaMemcpyAsync(c->items.p, hi, sizeof(ItemDev<T>) * n, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaMemcpyAsync(c->groups.p, hg, sizeof(Group) * gk.size(), cudaMemcpyHostToDevice, c->stream));
+  c->misc.ensure(64);
+  // leaves of skipped-leaf runs count as done
+  if (skip_leaves) {
+    std::vector<int> init(done_base, 0);
+    for (int i = 0; i < n; i++) init[hi[i].done_base] = plans[i]->h.steps[0].n_tiles;
+    CU(cudaMemcpyAsync(c->done.p, init.data(), sizeof(int) * done_base, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+  }
+  return TB_OK;
+}
+
+template <typename T>
+static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int64_t& launches) {
+  cudaStream_t s = c->stream;
+  const ItemDev<T>* items = reinterpret_cast<const ItemDev<T>*>(c->items.p);
+  const Group* groups = reinterpret_cast<const Group*>(c->groups.p);
+  float* out_item = reinterpret_cast<float*>(c->out_item.p);
+  const int smem = max_stream_smem_bytes();
+  if (mode == TB_MODE_BATCHED) {
+    CU(cudaMemsetAsync(c->done.p, 0, sizeof(int) * done_words, s));
+    CU(cudaMemsetAsync(c->misc.p, 0, 64, s));
+    unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
+    int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
+    int64_t timeout_ns = (int64_t)c->opt.timeout_ms * 1000000LL;
+    k_persistent<T><<<c->persistent_ctas, kThreads, smem, s>>>(items, groups, c->n_groups, c->n_tickets,
+                                                               reinterpret_cast<int*>(c->done.p), ticket, err,
+                                                               out_item, timeout_ns);
+    CU(cudaGetLastError());
+    launches++;
+  } else {
+    for (auto& lr : c->level_ranges) {
+      if (lr.second > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
+      k_level<T><<<(unsigned)lr.second, kThreads, smem, s>>>(items, groups, c->n_groups, lr.first, out_item);
+      CU(cudaGetLastError());
+      launches++;
+    }
+  }
+  k_reduce_max<<<1, kThreads, 0, s>>>(out_item, n, out_item + n);
+  CU(cudaGetLastError());
+  launches++;
+  return TB_OK;
+}
+
+template <typename T>
+static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const int8_t* slice_vals, const float* r,
+                               float* out_item, float* out_max, int mode) {
+  CU(cudaSetDevice(c->device));
+  tb_status st = set_kernel_attrs<T>();
+  if (st) return st;
+  for (int i = 0; i < n; i++) {
+    if (!plans[i]) return fail(TB_ERR_INVALID, "null plan");
+    if (plans[i]->ctx != c) return fail(TB_ERR_INVALID, "plan belongs to another context");
+    if (!plans[i]->h.has_weights) return fail(TB_ERR_INVALID, "plan has no bound weights (tb_plan_bind_mis)");
+    if ((st = upload_plan(plans[i]))) return st;
+  }
+  // slice values (concatenated)
+  std::vector<int64_t> sv_off(n);
+  size_t sv = 0;
+  for (int i = 0; i < n; i++) {
+    sv_off[i] = (int64_t)sv;
+    sv += plans[i]->h.sliced.size();
+  }
+  if (sv > 0 && !slice_vals) return fail(TB_ERR_INVALID, "slice_vals required for sliced plans");
+  for (size_t k = 0; k < sv; k++)
+    if (slice_vals[k] != 0 && slice_vals[k] != 1) return fail(TB_ERR_INVALID, "slice values must be 0 or 1");
+  CU(c->slice_vals.ensure(std::max<size_t>(sv, 16)));
+  CU(c->out_item.ensure(sizeof(float) * (n + 1)));
+  CU(c->h_out.ensure(sizeof(float) * (n + 1) + 64));
+  CU(c->h_in.ensure(std::max<size_t>(sv, 16)));
+  if (sv) std::memcpy(c->h_in.p, slice_vals, sv);
+  float* hout = reinterpret_cast<float*>(c->h_out.p);
+  int64_t launches = 0;
+  CU(cudaEventRecord(c->ev0, c->stream));
+  if (mode == TB_MODE_PLAIN) {
+    // one item at a time, as the reference loop
+    int64_t need = 0;
+    for (int i = 0; i < n; i++) need = std::max(need, plans[i]->h.plain_elems);
+    size_t bytes = (size_t)need * sizeof(T) + 256;
+    if (bytes > c->budget) return fail(TB_ERR_OOM, "plan needs more device memory than the budget");
+    CU(c->arena.ensure(bytes));
+    if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, c->h_in.p, sv, cudaMemcpyHostToDevice, c->stream));
+    T* arena = reinterpret_cast<T*>(c->arena.p);
+    for (int i = 0; i < n; i++) {
+      tb_plan* p = plans[i];
+      const int8_t* d_sv = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
+      if ((st = plain_item<T>(c, p, arena, d_sv, true, launches))) return st;
+      k_final<T><<<1, kThreads, 0, c->stream>>>(p->h.fin, arena, r ? r[i] : 0.0f,
+                                                reinterpret_cast<float*>(c->out_item.p) + i);
+      CU(cudaGetLastError());
+      launches++;
+      // synchronous read-back per item (Array(...)[] in solve_slice)
+      CU(cudaMemcpyAsync(hout + i, reinterpret_cast<float*>(c->out_item.p) + i, sizeof(float),
+                         cudaMemcpyDeviceToHost, c->stream));
+      CU(cudaStreamSynchronize(c->stream));
+    }
+    float m = -INFINITY;
+    for (int i = 0; i < n; i++) m = std::max(m, hout[i]);
+    hout[n] = m;
+    CU(cudaEventRecord(c->ev1, c->stream));
+    CU(cudaEventSynchronize(c->ev1));
+  } else {
+    // arenas of all items side by side; waves when over budget
+    std::vector<int64_t> aoff(n);
+    int64_t tot = 0;
+    for (int i = 0; i < n; i++) {
+      aoff[i] = tot;
+      tot = align_up(tot + plans[i]->h.arena_elems, 64);
+    }
+    size_t bytes = (size_t)tot * sizeof(T) + 256;
+    if (bytes > c->budget) {
+      // split into waves that fit
+      int i0 = 0;
+      std::vector<float> all(n + 1, -INFINITY);
+      while (i0 < n) {
+        int i1 = i0;
+        int64_t t2 = 0;
+        while (i1 < n && ((size_t)(t2 + plans[i1]->h.arena_elems) * sizeof(T) + 256 <= c->budget || i1 == i0)) {
+          t2 = align_up(t2 + plans[i1]->h.arena_elems, 64);
+          i1++;
+        }
+        if ((size_t)t2 * sizeof(T) + 256 > c->budget) return fail(TB_ERR_OOM, "one item exceeds the device budget");
+        std::vector<float> part(i1 - i0);
+        float pm;
+        st = solve_batch_t<T>(c, i1 - i0, plans + i0, slice_vals ? slice_vals + sv_off[i0] : nullptr,
+                              r ? r + i0 : nullptr, part.data(), &pm, mode);
+        if (st) return st;
+        for (int i = i0; i < i1; i++) all[i] = part[i - i0];
+        i0 = i1;
+      }
+      float m = -INFINITY;
+      for (int i = 0; i < n; i++) m = std::max(m, all[i]);
+      if (out_item) std::memcpy(out_item, all.data(), sizeof(float) * n);
+      if (out_max) *out_max = m;
+      return TB_OK;
+    }
+    CU(c->arena.ensure(bytes));
+    GraphKey key;
+    key.mode = mode;
+    for (int i = 0; i < n; i++) {
+      key.plans.push_back(plans[i]);
+      key.versions.push_back(plans[i]->version);
+    }
+    bool reuse = c->have_key && c->key == key && c->n_items == n;
+    // r values live in the items table; changing r means re-upload
+    if (reuse && r) {
+      const ItemDev<T>* hi = reinterpret_cast<const ItemDev<T>*>(c->h_items.p);
+      for (int i = 0; i < n && reuse; i++)
+        if (hi[i].r != r[i]) reuse = false;
+    }
+    if (reuse && !r) {
+      const ItemDev<T>* hi = reinterpret_cast<const ItemDev<T>*>(c->h_items.p);
+      for (int i = 0; i < n && reuse; i++)
+        if (hi[i].r != 0.0f) reuse = false;
+    }
+    int done_words = 0;
+    for (int i = 0; i < n; i++) done_words += (int)plans[i]->h.steps.size();
+    if (!reuse) {
+      if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+      }
+      c->have_key = false;
+      if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, r, false))) return st;
+      CU(cudaStreamSynchronize(c->stream));
+      c->key = key;
+      c->have_key = true;
+      c->n_items = n;
+      c->sv_bytes = sv;
+      if (c->opt.use_graphs) {
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int64_t l2 = 0;
+        if (sv) {
+          cudaError_t e = cudaMemcpyAsync(c->slice_vals.p, c->h_in.p, sv, cudaMemcpyHostToDevice, c->stream);
+          if (e != cudaSuccess) {
+            cudaStreamEndCapture(c->stream, &g);
+            return fail(TB_ERR_CUDA, cudaGetErrorString(e));
+          }
+        }
+        st = enqueue_batched<T>(c, n, mode, done_words, l2);
+        cudaError_t e1 = cudaMemcpyAsync(hout, c->out_item.p, sizeof(float) * (n + 1), cudaMemcpyDeviceToHost,
+                                         c->stream);
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+        if (st) return st;
+        if (e1 != cudaSuccess) return fail(TB_ERR_CUDA, cudaGetErrorString(e1));
+        if (e2 != cudaSuccess) return fail(TB_ERR_CUDA, cudaGetErrorString(e2));
+        cudaError_t e3 = cudaGraphInstantiate(&c->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) return fail(TB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+        c->launches_graph = l2;
+      }
+    }
+    if (c->opt.use_graphs && c->gexec) {
+      CU(cudaGraphLaunch(c->gexec, c->stream));
+      launches += c->launches_graph;
+    } else {
+      if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, c->h_in.p, sv, cudaMemcpyHostToDevice, c->stream));
+      if ((st = enqueue_batched<T>(c, n, mode, done_words, launches))) return st;
+      CU(cudaMemcpyAsync(hout, c->out_item.p, sizeof(float) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
+    }
+    CU(cudaEventRecord(c->ev1, c->stream));
+    CU(cudaEventSynchronize(c->ev1));
+    if (mode == TB_MODE_BATCHED) {
+      int err = 0;
+      CU(cudaMemcpy(&err, reinterpret_cast<char*>(c->misc.p) + 16, sizeof(int), cudaMemcpyDeviceToHost));
+      if (err) {
+        c->have_key = false;
+        return fail(TB_ERR_TIMEOUT, "a device-side wait of the persistent executor timed out");
+      }
+    }
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_ms = ms;
+  c->last_launches = launches;
+  if (out_item) std::memcpy(out_item, hout, sizeof(float) * n);
+  if (out_max) *out_max = hout[n];
+  return TB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void tb_options_default(tb_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->dtype = TB_DTYPE_F32;
+  o->use_graphs = 1;
+  o->max_device_bytes = 0;
+  o->timeout_ms = 20000;
+  o->autotune = 0;
+  o->persistent_ctas = 0;
+}
+
+const char* tb_version(void) { return "tb 0.1 sm_103a"; }
+
+const char* tb_last_error(const tb_ctx*) { return g_err.c_str(); }
+
+tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
+  if (!out) return fail(TB_ERR_INVALID, "out is null");
+  *out = nullptr;
+  int ndev = 0;
+  CU(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(TB_ERR_INVALID, "no such CUDA device");
+  std::unique_ptr<tb_ctx> c(new tb_ctx());
+  c->device = device;
+  if (opt) c->opt = *opt; else tb_options_default(&c->opt);
+  if (c->opt.dtype != TB_DTYPE_F32 && c->opt.dtype != TB_DTYPE_I32) return fail(TB_ERR_INVALID, "unknown dtype");
+  if (c->opt.timeout_ms <= 0) c->opt.timeout_ms = 20000;
+  CU(cudaSetDevice(device));
+  CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CU(cudaEventCreate(&c->ev0));
+  CU(cudaEventCreate(&c->ev1));
+  CU(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device));
+  size_t fr = 0, tot = 0;
+  CU(cudaMemGetInfo(&fr, &tot));
+  c->budget = c->opt.max_device_bytes > 0 ? (size_t)c->opt.max_device_bytes : (size_t)(fr * 0.8);
+  tb_status st = c->opt.dtype == TB_DTYPE_F32 ? set_kernel_attrs<float>() : set_kernel_attrs<int32_t>();
+  if (st) return st;
+  int per_sm = 0;
+  if (c->opt.dtype == TB_DTYPE_F32)
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<float>, kThreads, max_stream_smem_bytes()));
+  else
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<int32_t>, kThreads, max_stream_smem_bytes()));
+  per_sm = std::max(1, per_sm);
+  c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : per_sm * c->sms;
+  *out = c.release();
+  return TB_OK;
+}
+
+void tb_ctx_destroy(tb_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+tb_status tb_plan_create(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const int32_t* ix_off,
+                         const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
+                         const int32_t* children, const int32_t* node_iy_off, const int32_t* node_iy_lab,
+                         int32_t n_sliced, const int32_t* sliced, tb_plan** out) {
+  if (!ctx || !out) return fail(TB_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (n_iy > 0 && !iy) return fail(TB_ERR_INVALID, "iy is null");
+  if (n_nodes > 0 && !children) return fail(TB_ERR_INVALID, "children is null");
+  if (n_sliced > 0 && !sliced) return fail(TB_ERR_INVALID, "sliced is null");
+  if ((node_iy_off == nullptr) != (node_iy_lab == nullptr) && n_nodes > 0)
+    return fail(TB_ERR_INVALID, "node_iy_off and node_iy_lab go together");
+  PlanInput in;
+  in.n_labels = n_labels;
+  in.n_tensors = n_tensors;
+  in.ix_off = ix_off;
+  in.ix_lab = ix_lab;
+  in.n_iy = n_iy;
+  in.iy = iy;
+  in.n_nodes = n_nodes;
+  in.children = children;
+  in.node_iy_off = node_iy_off;
+  in.node_iy_lab = node_iy_lab;
+  in.n_sliced = n_sliced;
+  in.sliced = sliced;
+  std::unique_ptr<tb_plan> p(new tb_plan());
+  p->ctx = ctx;
+  std::string e;
+  try {
+    e = compile_plan(in, p->h, 0);
+  } catch (const std::exception& ex) {
+    e = std::string("plan compiler: ") + ex.what();
+  }
+  if (!e.empty()) return fail(TB_ERR_INVALID, e);
+  for (auto& lab : p->h.labels)
+    if (lab.size() > 30) return fail(TB_ERR_UNSUPPORTED, "a tensor of rank > 30 (over 4 GiB)");
+  p->version = ++ctx->plan_counter;
+  *out = p.release();
+  return TB_OK;
+}
+
+void tb_plan_destroy(tb_plan* p) {
+  if (!p) return;
+  if (p->ctx && p->ctx->have_key) {
+    for (auto* q : p->ctx->key.plans)
+      if (q == p) {
+        p->ctx->have_key = false;
+        break;
+      }
+  }
+  delete p;
+}
+
+tb_status tb_plan_stats_get(const tb_plan* p, tb_plan_stats* o) {
+  if (!p || !o) return fail(TB_ERR_INVALID, "null argument");
+  std::memset(o, 0, sizeof(*o));
+  o->tc = p->h.tc;
+  o->sc = p->h.sc;
+  o->rwc = p->h.rwc;
+  o->ops = p->h.ops;
+  o->bytes = p->h.bytes;
+  o->arena_bytes = p->h.arena_elems * 4;
+  o->n_steps = (int32_t)p->h.steps.size();
+  o->n_tensors = p->h.n_tensors;
+  o->n_open = (int32_t)p->h.open.size();
+  o->n_sliced = (int32_t)p->h.sliced.size();
+  o->n_tiles = (int32_t)std::min<int64_t>(p->h.total_tiles, 0x7fffffff);
+  return TB_OK;
+}
+
+tb_status tb_plan_node_labels(const tb_plan* p, int32_t node, int32_t cap, int32_t* labels_out, int32_t* n_out) {
+  if (!p || !n_out) return fail(TB_ERR_INVALID, "null argument");
+  if (node < 0 || node >= p->h.n_nodes) return fail(TB_ERR_INVALID, "node out of range");
+  const auto& l = p->h.labels[p->h.n_tensors + node];
+  *n_out = (int32_t)l.size();
+  for (int i = 0; i < (int)l.size() && i < cap; i++) labels_out[i] = l[i];
+  return TB_OK;
+}
+
+tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
+  if (!p || !w) return fail(TB_ERR_INVALID, "null argument");
+  const bool is_int = p->ctx->opt.dtype == TB_DTYPE_I32;
+  for (int i = 0; i < p->h.n_tensors; i++) {
+    LeafDesc& ld = p->h.leaves[i];
+    if (ld.nraw == 1) {
+      float x = w[p->h.leaf_raw[i][0]];
+      if (!std::isfinite(x)) return fail(TB_ERR_INVALID, "weights must be finite");
+      if (is_int && (x != std::floor(x) || std::fabs(x) > 1e8f))
+        return fail(TB_ERR_INVALID, "int32 weights must be integers of magnitude below 1e8");
+      ld.w = x;
+    }
+  }
+  p->h.has_weights = true;
+  p->uploaded = false;
+  p->version = ++p->ctx->plan_counter;
+  return upload_plan(p);
+}
+
+tb_status tb_solve_batch(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8_t* slice_vals, const float* r,
+                         float* out_item, float* out_max, int32_t mode) {
+  if (!c) return fail(TB_ERR_INVALID, "null context");
+  if (n <= 0 || !plans) return fail(TB_ERR_INVALID, "empty batch");
+  if (mode != TB_MODE_PLAIN && mode != TB_MODE_BATCHED && mode != TB_MODE_LAYERED)
+    return fail(TB_ERR_INVALID, "unknown mode");
+  std::lock_guard<std::mutex> lk(c->mu);
+  try {
+    if (c->opt.dtype == TB_DTYPE_F32) return solve_batch_t<float>(c, n, plans, slice_vals, r, out_item, out_max, mode);
+    return solve_batch_t<int32_t>(c, n, plans, slice_vals, r, out_item, out_max, mode);
+  } catch (const std::exception& ex) {
+    return fail(TB_ERR_INVALID, std::string("internal: ") + ex.what());
+  }
+}
+
+}  // extern "C"
+
+// leaf data with raw labels -> stored (distinct) labels: diagonal of repeats
+static std::vector<float> leaf_stored(const std::vector<int32_t>& raw, const std::vector<int32_t>& stored,
+                                      const float* data) {
+  std::vector<float> out((size_t)1 << stored.size());
+  for (size_t e = 0; e < out.size(); e++) {
+    size_t x = 0;
+    for (size_t k = 0; k < raw.size(); k++) {
+      int b = -1;
+      for (size_t q = 0; q < stored.size(); q++)
+        if (stored[q] == raw[k]) b = (int)q;
+      x |= (size_t)((e >> b) & 1) << k;
+    }
+    out[e] = data[x];
+  }
+  return out;
+}
+
+template <typename T>
+static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data, const int8_t* slice_vals,
+                            int mode) {
+  CU(cudaSetDevice(c->device));
+  tb_status st = set_kernel_attrs<T>();
+  if (st) return st;
+  if ((st = upload_plan(p))) return st;
+  const PlanHost& h = p->h;
+  int64_t need = mode == TB_MODE_PLAIN ? h.plain_elems : h.arena_elems;
+  size_t bytes = (size_t)need * sizeof(T) + 256;
+  if (bytes > c->budget) return fail(TB_ERR_OOM, "plan needs more device memory than the budget");
+  CU(c->arena.ensure(bytes));
+  T* arena = reinterpret_cast<T*>(c->arena.p);
+  size_t sv = h.sliced.size();
+  CU(c->slice_vals.ensure(std::max<size_t>(sv, 16)));
+  if (sv) CU(cudaMemcpy(c->slice_vals.p, slice_vals, sv, cudaMemcpyHostToDevice));
+  if (leaf_data) {
+    for (int i = 0; i < h.n_tensors; i++) {
+      std::vector<float> v = leaf_stored(h.leaf_raw[i], h.labels[i], leaf_data[i]);
+      if (std::is_same<T, float>::value) {
+        CU(cudaMemcpy(arena + h.off[i], v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+      } else {
+        std::vector<int32_t> iv(v.size());
+        for (size_t k = 0; k < v.size(); k++) iv[k] = std::isinf(v[k]) ? TB_I32_NEG : (int32_t)v[k];
+        CU(cudaMemcpy(arena + h.off[i], iv.data(), iv.size() * 4, cudaMemcpyHostToDevice));
+      }
+    }
+  }
+  int64_t launches = 0;
+  const int8_t* d_sv = reinterpret_cast<const int8_t*>(c->slice_vals.p);
+  if (mode == TB_MODE_PLAIN) {
+    if ((st = plain_item<T>(c, p, arena, d_sv, leaf_data == nullptr, launches))) return st;
+  } else {
+    // fused tiles, one launch per level for this single item
+    std::vector<int64_t> aoff{0}, svo{0};
+    tb_plan* pl[1] = {p};
+    c->have_key = false;
+    if (c->gexec) {
+      cudaGraphExecDestroy(c->gexec);
+      c->gexec = nullptr;
+    }
+    if ((st = upload_batch<T>(c, 1, pl, aoff, svo, nullptr, leaf_data != nullptr))) return st;
+    CU(c->out_item.ensure(sizeof(float) * 2));
+    const int smem = max_stream_smem_bytes();
+    for (auto& lr : c->level_ranges) {
+      k_level<T><<<(unsigned)lr.second, kThreads, smem, c->stream>>>(
+          reinterpret_cast<const ItemDev<T>*>(c->items.p), reinterpret_cast<const Group*>(c->groups.p), c->n_groups,
+          lr.first, reinterpret_cast<float*>(c->out_item.p));
+      CU(cudaGetLastError());
+    }
+  }
+  CU(cudaStreamSynchronize(c->stream));
+  return TB_OK;
+}
+
+extern "C" {
+
+tb_status tb_contract(tb_ctx* c, tb_plan* p, const float* const* leaf_data, float* out, int32_t mode) {
+  if (!c || !p || !leaf_data || !out) return fail(TB_ERR_INVALID, "null argument");
+  if (!p->h.sliced.empty()) return fail(TB_ERR_INVALID, "tb_contract does not take sliced plans");
+  std::lock_guard<std::mutex> lk(c->mu);
+  tb_status st = c->opt.dtype == TB_DTYPE_F32 ? run_single<float>(c, p, leaf_data, nullptr, mode)
+                                              : run_single<int32_t>(c, p, leaf_data, nullptr, mode);
+  if (st) return st;
+  const PlanHost& h = p->h;
+  size_t n = (size_t)1 << h.fin.root_log2;
+  if (c->opt.dtype == TB_DTYPE_F32) {
+    CU(cudaMemcpy(out, reinterpret_cast<float*>(c->arena.p) + h.fin.root_off, n * 4, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<int32_t> iv(n);
+    CU(cudaMemcpy(iv.data(), reinterpret_cast<int32_t*>(c->arena.p) + h.fin.root_off, n * 4, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < n; k++) out[k] = iv[k] <= TB_I32_NEG / 2 ? -INFINITY : (float)iv[k];
+  }
+  return TB_OK;
+}
+
+tb_status tb_dump_intermediates(tb_ctx* c, tb_plan* p, const int8_t* slice_vals, float* const* node_out,
+                                int32_t mode) {
+  if (!c || !p || !node_out) return fail(TB_ERR_INVALID, "null argument");
+  if (!p->h.has_weights) return fail(TB_ERR_INVALID, "plan has no bound weights");
+  if (!p->h.sliced.empty() && !slice_vals) return fail(TB_ERR_INVALID, "slice_vals required");
+  std::lock_guard<std::mutex> lk(c->mu);
+  tb_status st = c->opt.dtype == TB_DTYPE_F32 ? run_single<float>(c, p, nullptr, slice_vals, mode)
+                                              : run_single<int32_t>(c, p, nullptr, slice_vals, mode);
+  if (st) return st;
+  const PlanHost& h = p->h;
+  for (int j = 0; j < h.n_nodes; j++) {
+    if (!node_out[j]) continue;
+    int id = h.n_tensors + j;
+    size_t n = (size_t)1 << h.labels[id].size();
+    if (c->opt.dtype == TB_DTYPE_F32) {
+      CU(cudaMemcpy(node_out[j], reinterpret_cast<float*>(c->arena.p) + h.off[id], n * 4, cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<int32_t> iv(n);
+      CU(cudaMemcpy(iv.data(), reinterpret_cast<int32_t*>(c->arena.p) + h.off[id], n * 4, cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < n; k++) node_out[j][k] = iv[k] <= TB_I32_NEG / 2 ? -INFINITY : (float)iv[k];
+    }
+  }
+  return TB_OK;
+}
+
+tb_status tb_last_timing(const tb_ctx* c, double* ms, int64_t* launches) {
+  if (!c) return fail(TB_ERR_INVALID, "null context");
+  if (ms) *ms = c->last_ms;
+  if (launches) *launches = c->last_launches;
+  return TB_OK;
+}
+
+tb_status tb_gemm_device(tb_ctx* c, int64_t M, int64_t N, int64_t K, int64_t batch, const void* A, const void* B,
+                         void* C, void* stream) {
+  if (!c || !A || !B || !C) return fail(TB_ERR_INVALID, "null argument");
+  auto pow2 = [](int64_t x) { return x > 0 && (x & (x - 1)) == 0; };
+  if (!pow2(M) || !pow2(N) || !pow2(K) || batch < 1 || M < 16 || N < 16 || K < 16)
+    return fail(TB_ERR_UNSUPPORTED, "K1 takes power-of-two M, N, K >= 16");
+  if (M > (1 << 30) || N > (1 << 30) || K > (1 << 30)) return fail(TB_ERR_UNSUPPORTED, "dimension too large");
+  CU(cudaSetDevice(c->device));
+  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c->stream;
+  if (c->opt.dtype == TB_DTYPE_F32) {
+    CU(dispatch_k1<float>((const float*)A, (const float*)B, (float*)C, M, N, K, batch, s));
+  } else {
+    CU(dispatch_k1<int32_t>((const int32_t*)A, (const int32_t*)B, (int32_t*)C, M, N, K, batch, s));
+  }
+  return TB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Internal (not part of include/tb.h): compile a plan on the host only and
+// hand back its device program as one blob, so tests can check the kernels'
+// index arithmetic on a machine without a GPU.  Layout:
+//   int64 header[8] = {n_tensors, n_nodes, n_steps, n_tiles, n_leaves,
+//                      arena_elems, plain_elems, n_plain_ops}
+//   int64 off[n_tensors + n_nodes]; int32 rank[n_tensors + n_nodes]
+//   Step steps[]; TileDesc tiles[]; LeafDesc leaves[]; FinalDesc fin;
+//   per plain op: int32 node, int32 kind, TileDesc tile, int64 a,b,c,M,N,K,batch
+// ---------------------------------------------------------------------------
+extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const int32_t* ix_off,
+                                     const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
+                                     const int32_t* children, const int32_t* node_iy_off,
+                                     const int32_t* node_iy_lab, int32_t n_sliced, const int32_t* sliced,
+                                     void** blob, int64_t* blob_bytes, char* err, int32_t err_cap) {
+  PlanInput in;
+  in.n_labels = n_labels; in.n_tensors = n_tensors; in.ix_off = ix_off; in.ix_lab = ix_lab;
+  in.n_iy = n_iy; in.iy = iy; in.n_nodes = n_nodes; in.children = children;
+  in.node_iy_off = node_iy_off; in.node_iy_lab = node_iy_lab; in.n_sliced = n_sliced; in.sliced = sliced;
+  PlanHost h;
+  std::string e = compile_plan(in, h, 0);
+  if (!e.empty()) {
+    if (err && err_cap > 0) {
+      std::strncpy(err, e.c_str(), err_cap - 1);
+      err[err_cap - 1] = 0;
+    }
+    return TB_ERR_INVALID;
+  }
+  int64_t total = h.n_tensors + h.n_nodes;
+  int64_t nplain = 0;
+  for (auto& v : h.plain) nplain += (int64_t)v.size();
+  struct PlainRec { int32_t node, kind; TileDesc tile; int64_t a, b, c, M, N, K, batch; };
+  size_t bytes = 8 * 8 + total * 8 + total * 4 + h.steps.size() * sizeof(Step) + h.tiles.size() * sizeof(TileDesc) +
+                 h.leaves.size() * sizeof(LeafDesc) + sizeof(FinalDesc) + nplain * sizeof(PlainRec);
+  char* b = (char*)std::malloc(bytes);
+  if (!b) return TB_ERR_OOM;
+  char* p = b;
+  int64_t hdr[8] = {h.n_tensors, h.n_nodes, (int64_t)h.steps.size(), (int64_t)h.tiles.size(),
+                    (int64_t)h.leaves.size(), h.arena_elems, h.plain_elems, nplain};
+  std::memcpy(p, hdr, sizeof(hdr)); p += sizeof(hdr);
+  std::memcpy(p, h.off.data(), total * 8); p += total * 8;
+  for (int64_t i = 0; i < total; i++) { int32_t r = (int32_t)h.labels[i].size(); std::memcpy(p, &r, 4); p += 4; }
+  std::memcpy(p, h.steps.data(), h.steps.size() * sizeof(Step)); p += h.steps.size() * sizeof(Step);
+  if (!h.tiles.empty()) std::memcpy(p, h.tiles.data(), h.tiles.size() * sizeof(TileDesc));
+  p += h.tiles.size() * sizeof(TileDesc);
+  std::memcpy(p, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)); p += h.leaves.size() * sizeof(LeafDesc);
+  std::memcpy(p, &h.fin, sizeof(FinalDesc)); p += sizeof(FinalDesc);
+  for (int j = 0; j < h.n_nodes; j++)
+    for (const PlainOp& op : h.plain[j]) {
+      PlainRec rec;
+      std::memset(&rec, 0, sizeof(rec));
+      rec.node = j; rec.kind = op.kind; rec.tile = op.tile;
+      rec.a = op.a_off; rec.b = op.b_off; rec.c = op.c_off; rec.M = op.M; rec.N = op.N; rec.K = op.K; rec.batch = op.batch;
+      std::memcpy(p, &rec, sizeof(rec)); p += sizeof(rec);
+    }
+  *blob = b;
+  *blob_bytes = (int64_t)bytes;
+  return TB_OK;
+}
+
+extern "C" void tbi_free(void* p) { std::free(p); }
+
+extern "C" int32_t tbi_sizes(int32_t* out, int32_t n) {
+  int32_t v[6] = {(int32_t)sizeof(TileDesc), (int32_t)sizeof(Step), (int32_t)sizeof(LeafDesc),
+                  (int32_t)sizeof(FinalDesc), (int32_t)sizeof(GemmDesc), 0};
+  for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+  return 0;
+}

@@ -1,0 +1,514 @@
+// Device code of the tropical contraction engine (sm_103a).
+//
+//   leaves_tile    GenericTensorNetworks IndependentSet tensors, built on the
+//                  device: vertex [0, w], edge [[0,0],[0,-inf]], sliced labels
+//                  restricted to the item's values
+//   stream_tile    one CTA tile of a fused contraction node: bit-permuted
+//                  gathers of A and B into XOR-swizzled shared memory,
+//                  max-plus reduction, coalesced store of C
+//   gemm_tile      register-blocked gather GEMM tile for GEMM-shaped nodes
+//   final_tile     max over the root tensor + r (warp-shuffle reduction)
+//   gemm_k1        batched max-plus GEMM on canonical column-major operands,
+//                  packed add.f32x2 + three-input max.f32 (the plain path)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "tb_internal.h"
+
+namespace tb {
+
+// ---------------------------------------------------------------------------
+// semiring
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Trop;
+
+template <>
+struct Trop<float> {
+  static __device__ __forceinline__ float neg() { return __int_as_float(0xff800000); }
+  static __device__ __forceinline__ float mac(float acc, float a, float b) { return fmaxf(acc, a + b); }
+  static __device__ __forceinline__ float mx(float a, float b) { return fmaxf(a, b); }
+  static __device__ __forceinline__ float from_w(float w) { return w; }
+  static __device__ __forceinline__ float to_f(float v) { return v; }
+};
+
+template <>
+struct Trop<int32_t> {
+  static __device__ __forceinline__ int32_t neg() { return -536870912; }
+  // DPX: max(a + b, acc) in one instruction
+  static __device__ __forceinline__ int32_t mac(int32_t acc, int32_t a, int32_t b) {
+    return __viaddmax_s32(a, b, acc);
+  }
+  static __device__ __forceinline__ int32_t mx(int32_t a, int32_t b) { return max(a, b); }
+  static __device__ __forceinline__ int32_t from_w(float w) { return (int32_t)w; }
+  // values at or below half the sentinel stand for -inf
+  static __device__ __forceinline__ float to_f(int32_t v) {
+    return v <= -268435456 ? __int_as_float(0xff800000) : (float)v;
+  }
+};
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> { using type = float4; };
+template <>
+struct Vec4<int32_t> { using type = int4; };
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> { using type = float2; };
+template <>
+struct Vec2<int32_t> { using type = int2; };
+
+// XOR swizzle of a shared-memory index.  Linear over GF(2), so the swizzled
+// index of a bitwise OR of disjoint fields is the XOR of their swizzles.
+// It permutes words inside each 32-word row and spreads power-of-two strides
+// over all 32 banks.
+__device__ __forceinline__ int swz(int j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// leaves
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void leaves_tile(const LeafDesc* __restrict__ leaves, int n_leaves,
+                            const int8_t* __restrict__ slice_vals, T* __restrict__ arena, int tile) {
+  int i = tile * kThreads + threadIdx.x;
+  if (i >= n_leaves) return;
+  const LeafDesc ld = leaves[i];
+  const int nout = 1 << ld.n_out;
+  const T w = Trop<T>::from_w(ld.w);
+  for (int e = 0; e < nout; e++) {
+    T best = Trop<T>::neg();
+    for (int raw = 0; raw < (1 << ld.nraw); raw++) {
+      bool ok = true;
+      for (int k = 0; k < ld.nraw; k++) {
+        int x = (raw >> k) & 1;
+        if (ld.slice_idx[k] >= 0) {
+          if (x != (int)slice_vals[ld.slice_idx[k]]) ok = false;
+        } else if (((e >> ld.out_bit[k]) & 1) != x) {
+          ok = false;
+        }
+      }
+      if (!ok) continue;
+      T v;
+      if (ld.nraw == 1) v = (raw & 1) ? w : T(0);
+      else v = (raw == 3) ? Trop<T>::neg() : T(0);
+      best = Trop<T>::mx(best, v);
+    }
+    arena[ld.off + e] = best;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stream tile
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int stream_smem_words(const TileDesc& d) {
+  const bool hasB = d.b_off >= 0;
+  int w = (1 << d.na) + (hasB ? (1 << d.nb) : 0);
+  w += 1 << (d.na - d.pa);
+  w += hasB ? (1 << (d.nb - d.pb)) : 0;
+  w += 1 << (d.n_tc - d.pc);
+  w += 2 * (1 << d.n_tr);
+  w += kThreads;
+  return w;
+}
+
+// Copy the 2^n-element sub-tensor at src (tile bit b <-> tensor position
+// pos[b]; bits below p are positions 0..p-1) into swizzled shared memory.
+template <typename T>
+__device__ __forceinline__ void load_sub(T* __restrict__ dst, const T* __restrict__ src, int n, int p,
+                                         const int* __restrict__ hi) {
+  const int N = 1 << n;
+  if (p >= 2) {
+    using V = typename Vec4<T>::type;
+    const int lowmask = (1 << p) - 1;
+    const int nvec = N >> 2;
+    for (int q0 = threadIdx.x; q0 < nvec; q0 += 4 * kThreads) {
+      V v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        int q = q0 + u * kThreads;
+        if (q < nvec) {
+          int j = q << 2;
+          v[u] = __ldcg(reinterpret_cast<const V*>(src + ((j & lowmask) + hi[j >> p])));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        int q = q0 + u * kThreads;
+        if (q < nvec) {
+          int ph = swz(q << 2);
+          dst[ph] = v[u].x;
+          dst[ph ^ 1] = v[u].y;
+          dst[ph ^ 2] = v[u].z;
+          dst[ph ^ 3] = v[u].w;
+        }
+      }
+    }
+  } else if (p == 1) {
+    using V = typename Vec2<T>::type;
+    const int nvec = N >> 1;
+    for (int q = threadIdx.x; q < nvec; q += kThreads) {
+      int j = q << 1;
+      V v = __ldcg(reinterpret_cast<const V*>(src + ((j & 1) + hi[j >> 1])));
+      int ph = swz(j);
+      dst[ph] = v.x;
+      dst[ph ^ 1] = v.y;
+    }
+  } else {
+    for (int j = threadIdx.x; j < N; j += kThreads) dst[swz(j)] = __ldcg(src + hi[j]);
+  }
+}
+
+template <typename T>
+__device__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ arena, int* __restrict__ smem) {
+  const int t = threadIdx.x;
+  const bool hasB = d.b_off >= 0;
+  int64_t oa = d.a_off, ob = d.b_off, oc = d.c_off;
+  for (int i = 0; i < d.n_grid; i++) {
+    if ((tile >> i) & 1) {
+      int a = d.g_pa[i], b = d.g_pb[i];
+      if (a >= 0) oa += int64_t(1) << a;
+      if (b >= 0) ob += int64_t(1) << b;
+      oc += int64_t(1) << d.g_pc[i];
+    }
+  }
+  const int NA = 1 << d.na, NB = hasB ? (1 << d.nb) : 0;
+  T* As = reinterpret_cast<T*>(smem);
+  T* Bs = As + NA;
+  int* ldA = reinterpret_cast<int*>(Bs + NB);
+  const int nAh = 1 << (d.na - d.pa);
+  const int nBh = hasB ? (1 << (d.nb - d.pb)) : 0;
+  const int nCh = 1 << (d.n_tc - d.pc);
+  const int ntr = 1 << d.n_tr;
+  int* ldB = ldA + nAh;
+  int* stC = ldB + nBh;
+  int* IAr = stC + nCh;
+  int* IBr = IAr + ntr;
+  T* red = reinterpret_cast<T*>(IBr + ntr);
+
+  for (int j = t; j < nAh; j += kThreads) {
+    int o = 0;
+    for (int b = 0; b < d.na - d.pa; b++)
+      if ((j >> b) & 1) o += 1 << d.ta_pos[d.pa + b];
+    ldA[j] = o;
+  }
+  for (int j = t; j < nBh; j += kThreads) {
+    int o = 0;
+    for (int b = 0; b < d.nb - d.pb; b++)
+      if ((j >> b) & 1) o += 1 << d.tb_pos[d.pb + b];
+    ldB[j] = o;
+  }
+  for (int j = t; j < nCh; j += kThreads) {
+    int o = 0;
+    for (int b = 0; b < d.n_tc - d.pc; b++)
+      if ((j >> b) & 1) o += 1 << d.tc_pos[d.pc + b];
+    stC[j] = o;
+  }
+  for (int j = t; j < ntr; j += kThreads) {
+    int xa = 0, xb = 0;
+    for (int b = 0; b < d.n_tr; b++) {
+      if ((j >> b) & 1) {
+        if (d.tr_a[b] >= 0) xa |= 1 << d.tr_a[b];
+        if (d.tr_b[b] >= 0) xb |= 1 << d.tr_b[b];
+      }
+    }
+    IAr[j] = swz(xa);
+    IBr[j] = swz(xb);
+  }
+
+  // thread -> (output, reduction split)
+  const int lo_bits = d.n_tc < 8 ? d.n_tc : 8;
+  const int split = d.split_log2;
+  const int active = 1 << (lo_bits + split);
+  const int opt = 1 << (d.n_tc - lo_bits);
+  const bool act = t < active;
+  const int cl = t & ((1 << lo_bits) - 1);
+  const int s = t >> lo_bits;
+  int iat = 0, ibt = 0;
+  for (int b = 0; b < lo_bits; b++) {
+    if ((cl >> b) & 1) {
+      if (d.tc_a[b] >= 0) iat |= 1 << d.tc_a[b];
+      if (d.tc_b[b] >= 0) ibt |= 1 << d.tc_b[b];
+    }
+  }
+  iat = swz(iat);
+  ibt = swz(ibt);
+  int iah[kMaxOpt], ibh[kMaxOpt];
+  T acc[kMaxOpt];
+#pragma unroll
+  for (int i = 0; i < kMaxOpt; i++) {
+    int xa = 0, xb = 0;
+    for (int b = lo_bits; b < d.n_tc; b++) {
+      if (((i << lo_bits) >> b) & 1) {
+        if (d.tc_a[b] >= 0) xa |= 1 << d.tc_a[b];
+        if (d.tc_b[b] >= 0) xb |= 1 << d.tc_b[b];
+      }
+    }
+    iah[i] = iat ^ swz(xa);
+    ibh[i] = ibt ^ swz(xb);
+    acc[i] = Trop<T>::neg();
+  }
+  const int64_t nloop = int64_t(1) << d.n_loop;
+  for (int64_t rl = 0; rl < nloop; rl++) {
+    int64_t la = oa, lb = ob;
+    for (int i = 0; i < d.n_loop; i++) {
+      if ((rl >> i) & 1) {
+        if (d.l_pa[i] >= 0) la += int64_t(1) << d.l_pa[i];
+        if (d.l_pb[i] >= 0) lb += int64_t(1) << d.l_pb[i];
+      }
+    }
+    __syncthreads();  // tables ready / previous compute done
+    load_sub<T>(As, arena + la, d.na, d.pa, ldA);
+    if (hasB) load_sub<T>(Bs, arena + lb, d.nb, d.pb, ldB);
+    __syncthreads();
+    if (act) {
+      const int step = 1 << split;
+#pragma unroll
+      for (int i = 0; i < kMaxOpt; i++) {
+        if (i < opt) {
+          T a = acc[i];
+          const int ia = iah[i], ib = ibh[i];
+          if (hasB) {
+            for (int r = s; r < ntr; r += step) a = Trop<T>::mac(a, As[ia ^ IAr[r]], Bs[ib ^ IBr[r]]);
+          } else {
+            for (int r = s; r < ntr; r += step) a = Trop<T>::mx(a, As[ia ^ IAr[r]]);
+          }
+          acc[i] = a;
+        }
+      }
+    }
+  }
+  if (split > 0) {
+    __syncthreads();
+    red[t] = acc[0];
+    __syncthreads();
+    if (act && s == 0) {
+      T a = acc[0];
+      for (int s2 = 1; s2 < (1 << split); s2++) a = Trop<T>::mx(a, red[cl + (s2 << lo_bits)]);
+      acc[0] = a;
+    }
+  }
+  if (act && s == 0) {
+    const int cmask = (1 << d.pc) - 1;
+#pragma unroll
+    for (int i = 0; i < kMaxOpt; i++) {
+      if (i < opt) {
+        int c = cl + (i << lo_bits);
+        arena[oc + (c & cmask) + stC[c >> d.pc]] = acc[i];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// final: max over the root tensor, + r
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void final_tile(const FinalDesc& f, const T* __restrict__ arena, float r, float* out) {
+  __shared__ float wmax[kThreads / 32];
+  const int64_t n = int64_t(1) << f.root_log2;
+  T m = Trop<T>::neg();
+  for (int64_t i = threadIdx.x; i < n; i += kThreads) m = Trop<T>::mx(m, __ldcg(arena + f.root_off + i));
+  float v = Trop<T>::to_f(m);
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = wmax[0];
+    for (int w = 1; w < kThreads / 32; w++) b = fmaxf(b, wmax[w]);
+    *out = b + r;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// K1: batched max-plus GEMM, canonical column-major operands
+//   C[m + M n + MN b] = max_k A[m + M k + MK b] + B[k + K n + KN b]
+// CTA tile BM x BN, BK = 16 per stage, 256 threads in a 16 x 16 grid, each
+// owning a TM x TN register tile (TM = BM / 16, TN = BN / 16).  Shared memory
+// keeps k in interleaved pairs, so one 64-bit load yields (x[k], x[k+1]) and
+// the inner step is one add.f32x2 and one three-input max.f32 per two MACs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ float max3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float lo32(uint64_t x) { return __uint_as_float((uint32_t)x); }
+__device__ __forceinline__ float hi32(uint64_t x) { return __uint_as_float((uint32_t)(x >> 32)); }
+
+template <typename T, int BM, int BN>
+struct K1Cfg {
+  static constexpr int BK = 16;
+  static constexpr int TM = BM / 16, TN = BN / 16;
+  static constexpr int A_WORDS = BK * BM, B_WORDS = BK * BN;
+  static constexpr int SMEM_BYTES = 2 * (A_WORDS + B_WORDS) * (int)sizeof(T);
+};
+
+template <int TM, int BM>
+__device__ __forceinline__ int k1_row(int tm, int i) {
+  if (TM >= 4) {
+    constexpr int H = TM / 2;
+    return i < H ? tm * H + i : BM / 2 + tm * H + (i - H);
+  }
+  return tm * TM + i;
+}
+
+template <typename T, int BM, int BN>
+__global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T* __restrict__ B,
+                                               T* __restrict__ C, int M, int N, int K, int64_t tiles_mn) {
+  using Cfg = K1Cfg<T, BM, BN>;
+  constexpr int BK = Cfg::BK, TM = Cfg::TM, TN = Cfg::TN;
+  extern __shared__ __align__(16) unsigned char k1_smem[];
+  T* As = reinterpret_cast<T*>(k1_smem);          // [2][BK/2][BM][2]
+  T* Bs = As + 2 * Cfg::A_WORDS;                  // [2][BK/2][BN][2]
+  const int t = threadIdx.x;
+  const int64_t blk = blockIdx.x;
+  const int64_t bat = blk / tiles_mn;
+  const int64_t mn = blk % tiles_mn;
+  const int tiles_m = M / BM;
+  const int m0 = (int)(mn % tiles_m) * BM, n0 = (int)(mn / tiles_m) * BN;
+  const T* Ab = A + bat * (int64_t)M * K;
+  const T* Bb = B + bat * (int64_t)K * N;
+  T* Cb = C + bat * (int64_t)M * N;
+  const int tm = t & 15, tn = t >> 4;
+
+  // global -> register staging
+  constexpr int A_GROUPS = (BM / 4) * (BK / 2);  // (4 m) x (k pair) groups
+  constexpr int B_GROUPS = (BK / 4) * BN;         // (4 k) x n groups
+  constexpr int A_PER = (A_GROUPS + 255) / 256;
+  constexpr int B_PER = (B_GROUPS + 255) / 256;
+  using V4 = typename Vec4<T>::type;
+  V4 ra0[A_PER], ra1[A_PER], rb[B_PER];
+  auto gload = [&](int k0) {
+#pragma unroll
+    for (int u = 0; u < A_PER; u++) {
+      int g = t + u * 256;
+      if (g < A_GROUPS) {
+        int m4 = g % (BM / 4), kp = g / (BM / 4);
+        const T* p = Ab + (int64_t)(k0 + 2 * kp) * M + m0 + 4 * m4;
+        ra0[u] = __ldg(reinterpret_cast<const V4*>(p));
+        ra1[u] = __ldg(reinterpret_cast<const V4*>(p + M));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < B_PER; u++) {
+      int g = t + u * 256;
+      if (g < B_GROUPS) {
+        int q = g % (BK / 4), n = g / (BK / 4);
+        rb[u] = __ldg(reinterpret_cast<const V4*>(Bb + (int64_t)(n0 + n) * K + k0 + 4 * q));
+      }
+    }
+  };
+  auto sstore = [&](int buf) {
+    T* as = As + buf * Cfg::A_WORDS;
+    T* bs = Bs + buf * Cfg::B_WORDS;
+#pragma unroll
+    for (int u = 0; u < A_PER; u++) {
+      int g = t + u * 256;
+      if (g < A_GROUPS) {
+        int m4 = g % (BM / 4), kp = g / (BM / 4);
+        T* d = as + (kp * BM + 4 * m4) * 2;
+        V4 x, y;
+        x.x = ra0[u].x; x.y = ra1[u].x; x.z = ra0[u].y; x.w = ra1[u].y;
+        y.x = ra0[u].z; y.y = ra1[u].z; y.z = ra0[u].w; y.w = ra1[u].w;
+        reinterpret_cast<V4*>(d)[0] = x;
+        reinterpret_cast<V4*>(d)[1] = y;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < B_PER; u++) {
+      int g = t + u * 256;
+      if (g < B_GROUPS) {
+        int q = g % (BK / 4), n = g / (BK / 4);
+        T* d0 = bs + ((2 * q) * BN + n) * 2;
+        T* d1 = bs + ((2 * q + 1) * BN + n) * 2;
+        d0[0] = rb[u].x; d0[1] = rb[u].y;
+        d1[0] = rb[u].z; d1[1] = rb[u].w;
+      }
+    }
+  };
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; i++)
+#pragma unroll
+    for (int j = 0; j < TN; j++) acc[i][j] = Trop<T>::neg();
+
+  const int nk = K / BK;
+  gload(0);
+  sstore(0);
+  __syncthreads();
+  for (int kt = 0; kt < nk; kt++) {
+    const int buf = kt & 1;
+    if (kt + 1 < nk) gload((kt + 1) * BK);
+    const T* as = As + buf * Cfg::A_WORDS;
+    const T* bs = Bs + buf * Cfg::B_WORDS;
+#pragma unroll
+    for (int kp = 0; kp < BK / 2; kp++) {
+      uint64_t a2[TM], b2[TN];
+#pragma unroll
+      for (int i = 0; i < TM; i++)
+        a2[i] = *reinterpret_cast<const uint64_t*>(as + (kp * BM + k1_row<TM, BM>(tm, i)) * 2);
+#pragma unroll
+      for (int j = 0; j < TN; j++)
+        b2[j] = *reinterpret_cast<const uint64_t*>(bs + (kp * BN + k1_row<TN, BN>(tn, j)) * 2);
+      if constexpr (sizeof(T) == 4 && std::is_same<T, float>::value) {
+#pragma unroll
+        for (int i = 0; i < TM; i++)
+#pragma unroll
+          for (int j = 0; j < TN; j++) {
+            uint64_t s2 = add2(a2[i], b2[j]);
+            acc[i][j] = max3(acc[i][j], lo32(s2), hi32(s2));
+          }
+      } else {
+#pragma unroll
+        for (int i = 0; i < TM; i++)
+#pragma unroll
+          for (int j = 0; j < TN; j++) {
+            int32_t x0 = (int32_t)(uint32_t)a2[i], x1 = (int32_t)(uint32_t)(a2[i] >> 32);
+            int32_t y0 = (int32_t)(uint32_t)b2[j], y1 = (int32_t)(uint32_t)(b2[j] >> 32);
+            T v = Trop<T>::mac(acc[i][j], (T)x0, (T)y0);
+            acc[i][j] = Trop<T>::mac(v, (T)x1, (T)y1);
+          }
+      }
+    }
+    if (kt + 1 < nk) {
+      sstore(buf ^ 1);
+    }
+    __syncthreads();
+  }
+  // store
+#pragma unroll
+  for (int j = 0; j < TN; j++) {
+    int n = n0 + k1_row<TN, BN>(tn, j);
+#pragma unroll
+    for (int i = 0; i < TM; i++) {
+      int m = m0 + k1_row<TM, BM>(tm, i);
+      Cb[(int64_t)n * M + m] = acc[i][j];
+    }
+  }
+}
+
+}  // namespace tb

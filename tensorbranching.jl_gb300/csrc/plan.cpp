@@ -1,0 +1,498 @@
+// Plan compiler.  Semantics follow the reference's plan objects:
+//   CompressedEinsum{ixs, iy, ct} and uncompress   src/types.jl:51-79
+//   node output labels as parse_eincode derives them: the labels of the two
+//   operands still needed outside the subtree or open in iy
+//   complexity model (tc, sc, rwc)                 src/types.jl:115-121
+// and the lowering OMEinsum applies to each binary node (reduce private
+// labels, permute to [M,K,b] / [K,N,b], batched GEMM, permute to iy).
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace tb {
+namespace {
+
+int index_of(const std::vector<int32_t>& v, int32_t x) {
+  for (size_t i = 0; i < v.size(); i++)
+    if (v[i] == x) return (int)i;
+  return -1;
+}
+
+double log2sumexp2(double a, double b) {
+  double m = std::max(a, b);
+  if (m == -INFINITY) return m;
+  return m + std::log2(std::exp2(a - m) + std::exp2(b - m));
+}
+
+int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>* Bp,
+                      const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
+                      TileDesc& d, int out_bits_target) {
+  std::memset(&d, 0xff, sizeof(d));  // int8 tables default to -1
+  const std::vector<int32_t> empty;
+  const std::vector<int32_t>& B = Bp ? *Bp : empty;
+  std::vector<int32_t> L;
+  for (int32_t x : A)
+    if (index_of(L, x) < 0) L.push_back(x);
+  for (int32_t x : B)
+    if (index_of(L, x) < 0) L.push_back(x);
+  if (L.size() != A.size() + B.size() - [&] {
+        int s = 0;
+        for (int32_t x : B) s += index_of(A, x) >= 0;
+        return s;
+      }())
+    return "repeated label inside a tensor";
+  for (int32_t x : C)
+    if (index_of(L, x) < 0) return "output label absent from operands";
+  if ((int)A.size() > kMaxBits || (int)B.size() > kMaxBits || (int)C.size() > 31)
+    return "tensor rank beyond the engine's limit";
+  std::vector<int32_t> R;
+  for (int32_t x : L)
+    if (index_of(C, x) < 0) R.push_back(x);
+  std::vector<int32_t> S;
+  auto inS = [&](int32_t x) { return index_of(S, x) >= 0; };
+  auto feasible = [&](const std::vector<int32_t>& s) {
+    int tc = 0, tr = 0, na = 0, nb = 0, pa = 0, pb = 0, pc = 0;
+    for (int32_t x : s) {
+      if (index_of(C, x) >= 0) tc++; else tr++;
+      if (index_of(A, x) >= 0) na++;
+      if (index_of(B, x) >= 0) nb++;
+    }
+    while (pa < (int)A.size() && index_of(s, A[pa]) >= 0) pa++;
+    while (pb < (int)B.size() && index_of(s, B[pb]) >= 0) pb++;
+    while (pc < (int)C.size() && index_of(s, C[pc]) >= 0) pc++;
+    if (tc > 11 || tr > 8 || na > 13 || nb > 13) return false;
+    if (na - pa > 9 || nb - pb > 9 || tc - pc > 9) return false;
+    int64_t sm = (int64_t(1) << na) + (Bp ? (int64_t(1) << nb) : 0);
+    return sm <= kSmemFloats;
+  };
+  auto with = [&](std::vector<int32_t> s, int32_t x) {
+    if (index_of(s, x) < 0) s.push_back(x);
+    return s;
+  };
+  // 1. leading labels of every tensor, for coalesced loads and stores
+  for (int p = 1; p <= 6; p++) {
+    std::vector<int32_t> s2 = S;
+    for (const std::vector<int32_t>* X : {&C, &A, &B})
+      for (int i = 0; i < p && i < (int)X->size(); i++) s2 = with(s2, (*X)[i]);
+    if (!feasible(s2)) break;
+    S = s2;
+  }
+  // 2. reduced labels into the tile (fewer loop trips)
+  std::vector<int32_t> Rs = R;
+  std::stable_sort(Rs.begin(), Rs.end(), [&](int32_t x, int32_t y) {
+    int ax = index_of(A, x), ay = index_of(A, y);
+    if (ax < 0) ax = 1000;
+    if (ay < 0) ay = 1000;
+    return ax < ay;
+  });
+  for (int32_t x : Rs) {
+    if (inS(x)) continue;
+    auto s2 = with(S, x);
+    if (feasible(s2)) S = s2;
+  }
+  // 3. more outputs per CTA while the grid stays large
+  for (;;) {
+    int tc = 0;
+    for (int32_t x : S) tc += index_of(C, x) >= 0;
+    int grid = (int)C.size() - tc;
+    int32_t next = -1;
+    for (int32_t x : C)
+      if (!inS(x)) { next = x; break; }
+    if (next < 0) break;
+    if (tc >= out_bits_target && grid <= 12) break;
+    if (tc >= 11) break;
+    auto s2 = with(S, next);
+    if (!feasible(s2)) break;
+    S = s2;
+  }
+  // 4. emit
+  std::vector<int32_t> Tc, Tr, TA, TB, G, Rl;
+  for (int32_t x : C)
+    if (inS(x)) Tc.push_back(x); else G.push_back(x);
+  for (int32_t x : Rs)
+    if (inS(x)) Tr.push_back(x); else Rl.push_back(x);
+  for (int32_t x : A)
+    if (inS(x)) TA.push_back(x);
+  for (int32_t x : B)
+    if (inS(x)) TB.push_back(x);
+  if ((int)G.size() > 30 || (int)Rl.size() > kMaxBits) return "node too large";
+  d.a_off = a_off;
+  d.b_off = Bp ? b_off : -1;
+  d.c_off = c_off;
+  d.n_grid = (int32_t)G.size();
+  d.n_loop = (int32_t)Rl.size();
+  d.n_tc = (int32_t)Tc.size();
+  d.n_tr = (int32_t)Tr.size();
+  d.na = (int32_t)TA.size();
+  d.nb = (int32_t)TB.size();
+  d.pa = 0;
+  while (d.pa < d.na && index_of(A, TA[d.pa]) == d.pa) d.pa++;
+  d.pb = 0;
+  while (d.pb < d.nb && index_of(B, TB[d.pb]) == d.pb) d.pb++;
+  d.pc = 0;
+  while (d.pc < d.n_tc && index_of(C, Tc[d.pc]) == d.pc) d.pc++;
+  int lt = 0;
+  while ((1 << lt) < kThreads) lt++;
+  d.split_log2 = d.n_tc >= lt ? 0 : std::min(lt - d.n_tc, d.n_tr);
+  d.n_tiles = 1 << d.n_grid;
+  d.pad_ = 0;
+  for (size_t i = 0; i < G.size(); i++) {
+    d.g_pa[i] = (int8_t)index_of(A, G[i]);
+    d.g_pb[i] = (int8_t)index_of(B, G[i]);
+    d.g_pc[i] = (int8_t)index_of(C, G[i]);
+  }
+  for (size_t i = 0; i < Rl.size(); i++) {
+    d.l_pa[i] = (int8_t)index_of(A, Rl[i]);
+    d.l_pb[i] = (int8_t)index_of(B, Rl[i]);
+  }
+  for (size_t i = 0; i < TA.size(); i++) d.ta_pos[i] = (int8_t)index_of(A, TA[i]);
+  for (size_t i = 0; i < TB.size(); i++) d.tb_pos[i] = (int8_t)index_of(B, TB[i]);
+  for (size_t i = 0; i < Tc.size(); i++) {
+    d.tc_pos[i] = (int8_t)index_of(C, Tc[i]);
+    d.tc_a[i] = (int8_t)index_of(TA, Tc[i]);
+    d.tc_b[i] = (int8_t)index_of(TB, Tc[i]);
+  }
+  for (size_t i = 0; i < Tr.size(); i++) {
+    d.tr_a[i] = (int8_t)index_of(TA, Tr[i]);
+    d.tr_b[i] = (int8_t)index_of(TB, Tr[i]);
+  }
+  return "";
+}
+
+bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
+               const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
+               int min_log2, GemmDesc& g) {
+  std::vector<int32_t> M, N, K, Bt;
+  for (int32_t x : A) {
+    bool inb = index_of(B, x) >= 0, inc = index_of(C, x) >= 0;
+    if (inb && inc) Bt.push_back(x);
+    else if (inb) K.push_back(x);
+    else if (inc) M.push_back(x);
+    else return false;  // private label: not GEMM-shaped
+  }
+  for (int32_t x : B) {
+    bool ina = index_of(A, x) >= 0, inc = index_of(C, x) >= 0;
+    if (!ina && inc) N.push_back(x);
+    else if (!ina) return false;
+  }
+  if ((int)M.size() < min_log2 || (int)N.size() < min_log2 || (int)K.size() < min_log2) return false;
+  if ((int)M.size() > 30 || (int)N.size() > 30 || (int)K.size() > 30 || (int)Bt.size() > 30) return false;
+  std::memset(&g, 0xff, sizeof(g));
+  g.a_off = a_off; g.b_off = b_off; g.c_off = c_off;
+  g.nm = (int)M.size(); g.nn = (int)N.size(); g.nk = (int)K.size(); g.nbt = (int)Bt.size();
+  g.bm_log2 = std::min(g.nm, 7);
+  g.bn_log2 = std::min(g.nn, 7);
+  g.bk_log2 = std::min(g.nk, 4);
+  g.n_tiles = (int32_t)((int64_t(1) << (g.nm - g.bm_log2)) * (int64_t(1) << (g.nn - g.bn_log2)) *
+                        (int64_t(1) << g.nbt));
+  for (int i = 0; i < g.nm; i++) { g.m_pa[i] = (int8_t)index_of(A, M[i]); g.m_pc[i] = (int8_t)index_of(C, M[i]); }
+  for (int i = 0; i < g.nn; i++) { g.n_pb[i] = (int8_t)index_of(B, N[i]); g.n_pc[i] = (int8_t)index_of(C, N[i]); }
+  for (int i = 0; i < g.nk; i++) { g.k_pa[i] = (int8_t)index_of(A, K[i]); g.k_pb[i] = (int8_t)index_of(B, K[i]); }
+  for (int i = 0; i < g.nbt; i++) {
+    g.b_pa[i] = (int8_t)index_of(A, Bt[i]); g.b_pb[i] = (int8_t)index_of(B, Bt[i]); g.b_pc[i] = (int8_t)index_of(C, Bt[i]);
+  }
+  return true;
+}
+
+namespace {
+
+// OMEinsum-style lowering of one binary node for the plain path.
+std::string lower_plain(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
+                        const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
+                        int64_t scratch_base, int64_t& scratch_need, std::vector<PlainOp>& ops) {
+  std::vector<int32_t> M, N, K, Bt;
+  for (int32_t x : A) {
+    bool inb = index_of(B, x) >= 0, inc = index_of(C, x) >= 0;
+    if (inb && inc) Bt.push_back(x);
+    else if (inb) K.push_back(x);
+    else if (inc) M.push_back(x);
+  }
+  for (int32_t x : B)
+    if (index_of(A, x) < 0 && index_of(C, x) >= 0) N.push_back(x);
+  std::vector<int32_t> la, lb, lc;
+  la.insert(la.end(), M.begin(), M.end());
+  la.insert(la.end(), K.begin(), K.end());
+  la.insert(la.end(), Bt.begin(), Bt.end());
+  lb.insert(lb.end(), K.begin(), K.end());
+  lb.insert(lb.end(), N.begin(), N.end());
+  lb.insert(lb.end(), Bt.begin(), Bt.end());
+  lc.insert(lc.end(), M.begin(), M.end());
+  lc.insert(lc.end(), N.begin(), N.end());
+  lc.insert(lc.end(), Bt.begin(), Bt.end());
+  int64_t pos = scratch_base;
+  auto take = [&](size_t rank) {
+    int64_t o = pos;
+    pos = align_up(pos + (int64_t(1) << rank), 64);
+    return o;
+  };
+  int64_t ap = a_off, bp = b_off, cp = c_off;
+  std::string e;
+  if (la != A) {
+    ap = take(la.size());
+    PlainOp op{};
+    op.kind = PLAIN_TILE;
+    if (!(e = plan_tile(A, nullptr, la, a_off, -1, ap, op.tile)).empty()) return e;
+    ops.push_back(op);
+  }
+  if (lb != B) {
+    bp = take(lb.size());
+    PlainOp op{};
+    op.kind = PLAIN_TILE;
+    if (!(e = plan_tile(B, nullptr, lb, b_off, -1, bp, op.tile)).empty()) return e;
+    ops.push_back(op);
+  }
+  bool permute_c = lc != C;
+  if (permute_c) cp = take(lc.size());
+  int64_t Ms = int64_t(1) << M.size(), Ns = int64_t(1) << N.size(), Ks = int64_t(1) << K.size();
+  if (Ms >= 16 && Ns >= 16 && Ks >= 16) {
+    PlainOp op{};
+    op.kind = PLAIN_GEMM;
+    op.a_off = ap; op.b_off = bp; op.c_off = cp;
+    op.M = Ms; op.N = Ns; op.K = Ks; op.batch = int64_t(1) << Bt.size();
+    ops.push_back(op);
+  } else {
+    PlainOp op{};
+    op.kind = PLAIN_TILE;
+    if (!(e = plan_tile(la, &lb, lc, ap, bp, cp, op.tile)).empty()) return e;
+    ops.push_back(op);
+  }
+  if (permute_c) {
+    PlainOp op{};
+    op.kind = PLAIN_TILE;
+    if (!(e = plan_tile(lc, nullptr, C, cp, -1, c_off, op.tile)).empty()) return e;
+    ops.push_back(op);
+  }
+  scratch_need = std::max(scratch_need, pos - scratch_base);
+  return "";
+}
+
+}  // namespace
+
+std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
+  const int L = in.n_labels, T = in.n_tensors;
+  if (L < 0 || L > (1 << 24)) return "n_labels out of range";
+  if (T < 1) return "a plan needs at least one tensor";
+  if (in.n_nodes != T - 1) return "n_nodes must be n_tensors - 1";
+  if (!in.ix_off || !in.ix_lab) return "ixs missing";
+  if (in.ix_off[0] != 0) return "ix_off[0] must be 0";
+  p.n_labels = L; p.n_tensors = T; p.n_nodes = in.n_nodes;
+  p.slice_index.assign(L, -1);
+  for (int i = 0; i < in.n_sliced; i++) {
+    int32_t x = in.sliced[i];
+    if (x < 0 || x >= L || p.slice_index[x] >= 0) return "invalid sliced label";
+    p.slice_index[x] = i;
+    p.sliced.push_back(x);
+  }
+  std::vector<char> open(L, 0);
+  for (int i = 0; i < in.n_iy; i++) {
+    int32_t x = in.iy[i];
+    if (x < 0 || x >= L || open[x]) return "invalid open label";
+    if (p.slice_index[x] >= 0) return "a label cannot be both open and sliced";
+    open[x] = 1;
+    p.open.push_back(x);
+  }
+  const int total = T + in.n_nodes;
+  p.labels.assign(total, {});
+  p.leaf_raw.assign(T, {});
+  std::vector<int> count(L, 0);
+  for (int i = 0; i < T; i++) {
+    if (in.ix_off[i + 1] < in.ix_off[i]) return "ix_off not monotone";
+    for (int k = in.ix_off[i]; k < in.ix_off[i + 1]; k++) {
+      int32_t x = in.ix_lab[k];
+      if (x < 0 || x >= L) return "label out of range";
+      p.leaf_raw[i].push_back(x);
+      if (p.slice_index[x] < 0 && index_of(p.labels[i], x) < 0) p.labels[i].push_back(x);
+    }
+    if (p.leaf_raw[i].size() > 2 || p.leaf_raw[i].empty())
+      return "independent-set leaves have one (vertex) or two (edge) labels";
+    for (int32_t x : p.labels[i]) count[x]++;
+  }
+  for (int32_t x : p.open)
+    if (count[x] == 0) return "open label absent from every tensor";
+  // tree structure and node output labels
+  p.children.assign(in.children, in.children + 2 * in.n_nodes);
+  std::vector<char> used(total, 0);
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> cnt(total);  // (label, leaves in subtree)
+  for (int i = 0; i < T; i++)
+    for (int32_t x : p.labels[i]) cnt[i].push_back({x, 1});
+  for (int j = 0; j < in.n_nodes; j++) {
+    int me = T + j;
+    int a = in.children[2 * j], b = in.children[2 * j + 1];
+    if (a < 0 || b < 0 || a >= me || b >= me || a == b) return "children must reference earlier ids";
+    if (used[a] || used[b]) return "a tensor is used twice in the tree";
+    used[a] = used[b] = 1;
+    std::vector<int32_t> uni = p.labels[a];
+    for (int32_t x : p.labels[b])
+      if (index_of(uni, x) < 0) uni.push_back(x);
+    auto c_of = [&](int id, int32_t x) {
+      for (auto& pr : cnt[id])
+        if (pr.first == x) return pr.second;
+      return 0;
+    };
+    std::vector<int32_t> needed;
+    for (int32_t x : uni) {
+      int c = c_of(a, x) + c_of(b, x);
+      if (count[x] - c > 0 || open[x]) needed.push_back(x);
+      cnt[me].push_back({x, c});
+    }
+    if (in.node_iy_off) {
+      std::vector<int32_t> given;
+      for (int k = in.node_iy_off[j]; k < in.node_iy_off[j + 1]; k++) {
+        int32_t x = in.node_iy_lab[k];
+        if (x < 0 || x >= L) return "node label out of range";
+        if (p.slice_index[x] >= 0) continue;
+        if (index_of(uni, x) < 0) return "node label absent from its operands";
+        if (index_of(given, x) >= 0) return "repeated node label";
+        given.push_back(x);
+      }
+      for (int32_t x : needed)
+        if (index_of(given, x) < 0) return "node output drops a label needed later";
+      p.labels[me] = given;
+    } else {
+      p.labels[me] = needed;
+    }
+  }
+  p.root = in.n_nodes ? total - 1 : 0;
+  if (in.n_nodes && !in.node_iy_off) {
+    // the root keeps exactly the open labels, in iy order
+    p.labels[p.root] = p.open;
+  }
+  // arena: leaves, then node outputs, each 128-byte aligned
+  p.off.assign(total, 0);
+  int64_t pos = 0;
+  for (int i = 0; i < total; i++) {
+    p.off[i] = pos;
+    pos = align_up(pos + (int64_t(1) << p.labels[i].size()), 32);
+  }
+  int64_t fused_end = pos;
+  // the single-tensor case writes its reduced output after the leaf
+  int64_t single_out = -1;
+  std::vector<int32_t> single_labels;
+  if (in.n_nodes == 0) {
+    single_out = pos;
+    single_labels = p.open;
+    pos = align_up(pos + (int64_t(1) << single_labels.size()), 32);
+    fused_end = pos;
+  }
+  p.arena_elems = fused_end;
+  // complexity model
+  p.tc = -INFINITY; p.sc = 0; p.rwc = -INFINITY; p.ops = 0; p.bytes = 0;
+  for (int i = 0; i < total; i++) p.sc = std::max(p.sc, (double)p.labels[i].size());
+  for (int j = 0; j < in.n_nodes; j++) {
+    int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+    std::vector<int32_t> uni = p.labels[a];
+    for (int32_t x : p.labels[b])
+      if (index_of(uni, x) < 0) uni.push_back(x);
+    double t = (double)uni.size();
+    p.tc = log2sumexp2(p.tc, t);
+    double rw = log2sumexp2(log2sumexp2((double)p.labels[a].size(), (double)p.labels[b].size()),
+                            (double)p.labels[me].size());
+    p.rwc = log2sumexp2(p.rwc, rw);
+    p.ops += 2.0 * std::exp2(t);
+    p.bytes += 4.0 * (std::exp2((double)p.labels[a].size()) + std::exp2((double)p.labels[b].size()) +
+                      std::exp2((double)p.labels[me].size()));
+  }
+  if (in.n_nodes == 0) {
+    p.tc = (double)p.labels[0].size();
+    p.rwc = p.tc;
+    p.ops = std::exp2(p.tc);
+    p.bytes = 4.0 * (std::exp2(p.tc) + std::exp2((double)single_labels.size()));
+  }
+  // leaves
+  p.leaves.clear();
+  for (int i = 0; i < T; i++) {
+    LeafDesc ld;
+    std::memset(&ld, 0, sizeof(ld));
+    ld.off = p.off[i];
+    ld.nraw = (int32_t)p.leaf_raw[i].size();
+    ld.n_out = (int32_t)p.labels[i].size();
+    for (int k = 0; k < 2; k++) {
+      ld.out_bit[k] = -1;
+      ld.slice_idx[k] = -1;
+    }
+    for (int k = 0; k < ld.nraw; k++) {
+      int32_t x = p.leaf_raw[i][k];
+      ld.out_bit[k] = (int8_t)index_of(p.labels[i], x);
+      ld.slice_idx[k] = (int8_t)p.slice_index[x];
+    }
+    ld.w = 0.0f;
+    p.leaves.push_back(ld);
+  }
+  // fused steps: 0 = leaves, 1..n = nodes, last = final
+  p.steps.clear();
+  p.tiles.clear();
+  p.gemms.clear();
+  std::vector<int> step_of(total, 0);  // leaves -> step 0
+  Step s0{STEP_LEAVES, 0, -1, -1, (T + kThreads - 1) / kThreads, 0};
+  p.steps.push_back(s0);
+  p.total_tiles = s0.n_tiles;
+  std::string e;
+  for (int j = 0; j < in.n_nodes; j++) {
+    int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+    Step st{};
+    GemmDesc g;
+    if (gemm_min_log2 > 0 &&
+        plan_gemm(p.labels[a], p.labels[b], p.labels[me], p.off[a], p.off[b], p.off[me], gemm_min_log2, g)) {
+      st.kind = STEP_GEMM;
+      st.desc = (int32_t)p.gemms.size();
+      st.n_tiles = g.n_tiles;
+      p.gemms.push_back(g);
+    } else {
+      TileDesc d;
+      if (!(e = plan_tile(p.labels[a], &p.labels[b], p.labels[me], p.off[a], p.off[b], p.off[me], d)).empty())
+        return "node " + std::to_string(j) + ": " + e;
+      st.kind = STEP_TILE;
+      st.desc = (int32_t)p.tiles.size();
+      st.n_tiles = d.n_tiles;
+      p.tiles.push_back(d);
+    }
+    st.dep0 = step_of[a];
+    st.dep1 = step_of[b];
+    st.level = 1 + std::max(p.steps[st.dep0].level, p.steps[st.dep1].level);
+    step_of[me] = (int)p.steps.size();
+    p.steps.push_back(st);
+    p.total_tiles += st.n_tiles;
+  }
+  int64_t root_off = p.off[p.root];
+  int root_rank = (int)p.labels[p.root].size();
+  if (in.n_nodes == 0) {
+    // one tensor: reduce it to the open labels first
+    TileDesc d;
+    if (!(e = plan_tile(p.labels[0], nullptr, single_labels, p.off[0], -1, single_out, d)).empty())
+      return "single tensor: " + e;
+    Step st{STEP_TILE, (int32_t)p.tiles.size(), 0, -1, d.n_tiles, 1};
+    p.tiles.push_back(d);
+    step_of[0] = (int)p.steps.size();
+    p.steps.push_back(st);
+    p.total_tiles += st.n_tiles;
+    root_off = single_out;
+    root_rank = (int)single_labels.size();
+  }
+  Step fin{STEP_FINAL, 0, (int32_t)p.steps.size() - 1, -1, 1, p.steps.back().level + 1};
+  p.steps.push_back(fin);
+  p.total_tiles += 1;
+  p.fin.root_off = root_off;
+  p.fin.root_log2 = root_rank;
+  p.fin.pad_ = 0;
+  // plain lowering, scratch after the fused arena
+  p.plain.assign(in.n_nodes, {});
+  int64_t scratch = 0;
+  for (int j = 0; j < in.n_nodes; j++) {
+    int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+    if (!(e = lower_plain(p.labels[a], p.labels[b], p.labels[me], p.off[a], p.off[b], p.off[me], fused_end,
+                          scratch, p.plain[j]))
+             .empty())
+      return "plain lowering of node " + std::to_string(j) + ": " + e;
+  }
+  p.plain_elems = fused_end + scratch;
+  return "";
+}
+
+}  // namespace tb

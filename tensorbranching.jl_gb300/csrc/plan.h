@@ -1,0 +1,78 @@
+// Host-side plan compiler: turns a contraction tree over dimension-2 labels
+// into device work (leaf builder, fused tile steps, final reduction) and into
+// the per-contraction lowering of the plain path.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "tb_internal.h"
+
+namespace tb {
+
+enum PlainKind : int32_t { PLAIN_TILE = 1, PLAIN_GEMM = 2 };
+
+// One launch of the plain (OMEinsum-style) lowering.
+struct PlainOp {
+  int32_t kind;
+  TileDesc tile;                 // PLAIN_TILE: permute / reduce / small contraction
+  int64_t a_off, b_off, c_off;   // PLAIN_GEMM operands (arena offsets)
+  int64_t M, N, K, batch;        // PLAIN_GEMM shape, canonical column-major
+};
+
+struct PlanInput {
+  int32_t n_labels = 0;
+  int32_t n_tensors = 0;
+  const int32_t* ix_off = nullptr;
+  const int32_t* ix_lab = nullptr;
+  int32_t n_iy = 0;
+  const int32_t* iy = nullptr;
+  int32_t n_nodes = 0;
+  const int32_t* children = nullptr;
+  const int32_t* node_iy_off = nullptr;
+  const int32_t* node_iy_lab = nullptr;
+  int32_t n_sliced = 0;
+  const int32_t* sliced = nullptr;
+};
+
+struct PlanHost {
+  int32_t n_labels = 0, n_tensors = 0, n_nodes = 0;
+  std::vector<std::vector<int32_t>> leaf_raw;  // raw labels of each leaf
+  std::vector<std::vector<int32_t>> labels;    // stored labels of tensor id (leaves, then nodes)
+  std::vector<int64_t> off;                    // arena offset of tensor id
+  std::vector<int32_t> children;
+  std::vector<int32_t> open;                   // open labels, output order
+  std::vector<int32_t> sliced;                 // sliced labels, slice-value order
+  std::vector<int32_t> slice_index;            // label -> index in sliced (-1)
+  int64_t arena_elems = 0;                     // fused form (leaves + node outputs)
+  int64_t plain_elems = 0;                     // plain form (adds lowering scratch)
+  int32_t root = 0;                            // tensor id of the root
+  bool has_weights = false;
+
+  std::vector<Step> steps;
+  std::vector<TileDesc> tiles;
+  std::vector<GemmDesc> gemms;
+  std::vector<LeafDesc> leaves;
+  FinalDesc fin{};
+  std::vector<std::vector<PlainOp>> plain;     // per node, in post-order
+
+  double tc = 0, sc = 0, rwc = 0, ops = 0, bytes = 0;
+  int64_t total_tiles = 0;
+};
+
+// Compile; returns "" on success or an error message.
+std::string compile_plan(const PlanInput& in, PlanHost& out, int gemm_min_log2);
+
+// Plan one stream tile for C = max_{R} A (+ B).  A, C (and B if non-null)
+// are label lists in their memory order.  Returns "" or an error.
+std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>* B,
+                      const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
+                      TileDesc& d, int out_bits_target = 9);
+
+// Plan a gather GEMM for node (A, B -> C) if its M, N, K are all at least
+// 2^min_log2; returns false when the node is not GEMM-shaped.
+bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
+               const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
+               int min_log2, GemmDesc& g);
+
+}  // namespace tb

@@ -1,0 +1,111 @@
+// Internal data structures shared by the plan compiler (host) and the
+// kernels (device).  Everything here is POD so it can be copied to the GPU.
+#pragma once
+#include <cstdint>
+
+namespace tb {
+
+constexpr int kMaxTileBits = 16;  // labels inside one CTA tile (per tensor)
+constexpr int kMaxBits = 48;      // labels of one tensor / grid / loop
+constexpr int kThreads = 256;     // threads of every tile kernel
+constexpr int kMaxOpt = 8;        // outputs per thread in the stream tile
+constexpr int kSmemFloats = 8192; // stream tile staging (As + Bs), floats
+
+enum StepKind : int32_t {
+  STEP_LEAVES = 1,  // build the item's leaf tensors
+  STEP_TILE = 2,    // stream tile contraction (fused permute/reduce/contract)
+  STEP_GEMM = 3,    // register-blocked gather GEMM contraction
+  STEP_FINAL = 4,   // max over the root tensor + r -> item result
+};
+
+// Stream tile contraction:  C[c] = max over reduced labels of A[.] (+ B[.]).
+// The node's labels are split into
+//   Tc : output labels staged inside a CTA (tile outputs, in C order)
+//   Tr : reduced labels staged inside a CTA
+//   G  : output labels enumerated by the CTA grid
+//   Rl : reduced labels enumerated by a loop inside the CTA
+// A CTA loads the sub-tensors of A and B spanned by Tc u Tr into shared
+// memory (indexed in each tensor's own label order), reduces over Tr for its
+// 2^|Tc| outputs, repeats for every Rl assignment, and writes its C tile.
+struct TileDesc {
+  int64_t a_off, b_off, c_off;  // element offsets in the item arena; b_off < 0: unary
+  int32_t n_grid, n_loop, n_tc, n_tr;
+  int32_t na, nb;               // log2 sizes of the A / B sub-tiles
+  int32_t pa, pb, pc;           // leading tile bits that are tensor positions 0..p-1
+  int32_t split_log2;           // threads cooperating on one output (reduction split)
+  int32_t n_tiles;              // CTAs = 2^n_grid
+  int32_t pad_;
+  int8_t g_pa[kMaxBits], g_pb[kMaxBits], g_pc[kMaxBits];  // grid bit -> tensor position (-1)
+  int8_t l_pa[kMaxBits], l_pb[kMaxBits];                  // loop bit -> tensor position (-1)
+  int8_t ta_pos[kMaxTileBits], tb_pos[kMaxTileBits];      // tile bit -> tensor position
+  int8_t tc_pos[kMaxTileBits];                            // Tc bit -> C position
+  int8_t tc_a[kMaxTileBits], tc_b[kMaxTileBits];          // Tc bit -> A / B tile bit (-1)
+  int8_t tr_a[kMaxTileBits], tr_b[kMaxTileBits];          // Tr bit -> A / B tile bit (-1)
+};
+
+// Register-blocked gather GEMM for a contraction node with large M, N, K:
+//   C[m, n, b] = max_k A[m, k, b] + B[k, n, b]
+// where m, n, k, b are assignments of label groups that sit at arbitrary
+// bit positions of A, B and C.  Tile: BM x BN outputs per CTA, BK per stage.
+struct GemmDesc {
+  int64_t a_off, b_off, c_off;
+  int32_t nm, nn, nk, nbt;          // label counts of M, N, K, batch
+  int32_t bm_log2, bn_log2, bk_log2;  // CTA tile
+  int32_t n_tiles;                  // (M/BM) * (N/BN) * batch
+  int8_t m_pa[kMaxBits], m_pc[kMaxBits];   // M label i -> position in A, C
+  int8_t n_pb[kMaxBits], n_pc[kMaxBits];   // N label i -> position in B, C
+  int8_t k_pa[kMaxBits], k_pb[kMaxBits];   // K label i -> position in A, B
+  int8_t b_pa[kMaxBits], b_pb[kMaxBits], b_pc[kMaxBits];
+};
+
+// One leaf tensor of the MIS network (GenericTensorNetworks IndependentSet):
+// vertex [0, w], edge [[0,0],[0,-inf]]; a self-loop edge is its diagonal.
+struct LeafDesc {
+  int64_t off;          // output offset in the arena
+  int32_t nraw;         // raw labels: 1 vertex, 2 edge
+  int32_t n_out;        // output rank
+  int8_t out_bit[2];    // raw position -> output bit (-1: label sliced)
+  int8_t slice_idx[2];  // raw position -> index into the item's slice values (-1)
+  int32_t pad_;
+  float w;              // vertex weight (vertex leaves)
+};
+
+struct Step {
+  int32_t kind;        // StepKind
+  int32_t desc;        // index into the plan's TileDesc / GemmDesc array
+  int32_t dep0, dep1;  // steps this one waits for (-1 none)
+  int32_t n_tiles;     // CTAs (work units) of this step
+  int32_t level;       // 0 for leaves; 1 + max(level(deps))
+};
+
+// Final step: max over the root tensor (2^root_log2 values at root_off).
+struct FinalDesc {
+  int64_t root_off;
+  int32_t root_log2;
+  int32_t pad_;
+};
+
+// One batch item as the persistent executor sees it.
+template <typename T>
+struct ItemDev {
+  T* arena;
+  const Step* steps;
+  const TileDesc* tiles;
+  const GemmDesc* gemms;
+  const LeafDesc* leaves;
+  const int8_t* slice_vals;
+  float r;
+  int32_t n_leaves;
+  int32_t done_base;   // offset of this item's step counters
+  int32_t n_steps;
+  FinalDesc fin;
+};
+
+// A group = all tiles of one (item, step); groups are listed in dependency
+// order and tickets index tiles within the concatenation of groups.
+struct Group {
+  int32_t item, step;
+  int64_t first;  // first ticket of this group
+};
+
+}  // namespace tb

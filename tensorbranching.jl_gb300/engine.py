@@ -1,0 +1,172 @@
+"""Python handle on the C ABI of include/tb.h (ctypes).
+
+``Engine`` owns a ``tb_ctx``; ``Plan`` owns a ``tb_plan``.  Every call goes
+through the native library; there is no host fallback for the contraction.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_double, c_int32, c_int64, c_void_p
+
+import numpy as np
+
+from . import _native
+from .network import CompressedEinsum
+
+
+class Plan:
+    """A compiled contraction plan bound to an Engine."""
+
+    def __init__(self, engine: "Engine", code: CompressedEinsum, sliced=(), use_node_iy: bool = True):
+        self.engine = engine
+        self.code = code
+        self.sliced = [int(x) for x in sliced]
+        lib = engine.lib
+        off, lab = code.csr()
+        iy = np.array(code.iy if code.iy else [0], np.int32)
+        ch = code.children if code.n_nodes else np.zeros((1, 2), np.int32)
+        niy_off, niy_lab = code.node_iy_csr() if use_node_iy else (None, None)
+        sl = np.array(self.sliced if self.sliced else [0], np.int32)
+        h = c_void_p()
+        self._keep = (off, lab, iy, ch, niy_off, niy_lab, sl)
+        st = lib.tb_plan_create(engine.ctx, code.n_labels, code.n_tensors, off.ctypes.data, lab.ctypes.data,
+                                len(code.iy), iy.ctypes.data, code.n_nodes, ch.ctypes.data,
+                                None if niy_off is None else niy_off.ctypes.data,
+                                None if niy_lab is None else niy_lab.ctypes.data,
+                                len(self.sliced), sl.ctypes.data, ctypes.byref(h))
+        _native.check(st, engine.ctx)
+        self.handle = h
+        self._keep = None
+
+    def bind_mis(self, weights) -> "Plan":
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        if w.shape[0] < self.code.n_labels:
+            raise ValueError("one weight per label is required")
+        _native.check(self.engine.lib.tb_plan_bind_mis(self.handle, w.ctypes.data), self.engine.ctx)
+        return self
+
+    def stats(self) -> dict:
+        s = _native.TbPlanStats()
+        _native.check(self.engine.lib.tb_plan_stats_get(self.handle, ctypes.byref(s)), self.engine.ctx)
+        return {k: getattr(s, k) for k, _ in s._fields_ if k != "reserved"}
+
+    def node_labels(self, j: int) -> list[int]:
+        buf = np.zeros(64, np.int32)
+        n = c_int32()
+        _native.check(self.engine.lib.tb_plan_node_labels(self.handle, j, 64, buf.ctypes.data, ctypes.byref(n)),
+                      self.engine.ctx)
+        return buf[: n.value].tolist()
+
+    def all_node_labels(self) -> list[list[int]]:
+        return [self.node_labels(j) for j in range(self.code.n_nodes)]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.engine.lib.tb_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    """A tb_ctx on one CUDA device."""
+
+    def __init__(self, device: int = 0, dtype: str = "f32", use_graphs: bool = True,
+                 max_device_bytes: int = 0, timeout_ms: int = 20000, persistent_ctas: int = 0):
+        self.lib = _native.engine_lib()
+        opt = _native.TbOptions()
+        self.lib.tb_options_default(ctypes.byref(opt))
+        opt.dtype = {"f32": _native.TB_DTYPE_F32, "i32": _native.TB_DTYPE_I32}[dtype]
+        opt.use_graphs = 1 if use_graphs else 0
+        opt.max_device_bytes = int(max_device_bytes)
+        opt.timeout_ms = int(timeout_ms)
+        opt.persistent_ctas = int(persistent_ctas)
+        self.dtype = dtype
+        h = c_void_p()
+        _native.check(self.lib.tb_ctx_create(device, ctypes.byref(opt), ctypes.byref(h)), None)
+        self.ctx = h
+
+    def plan(self, code: CompressedEinsum, weights=None, sliced=(), use_node_iy: bool = True) -> Plan:
+        p = Plan(self, code, sliced, use_node_iy)
+        if weights is not None:
+            p.bind_mis(weights)
+        return p
+
+    def solve_batch(self, plans, slice_vals=None, r=None, mode: str = "batched"):
+        """Per-item results (max root + r) and their max."""
+        n = len(plans)
+        arr = (c_void_p * n)(*[p.handle for p in plans])
+        sv = None
+        if slice_vals is not None:
+            sv = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int8).ravel() for x in slice_vals])
+                                      if isinstance(slice_vals, (list, tuple)) else
+                                      np.asarray(slice_vals, np.int8).ravel(), dtype=np.int8)
+            if sv.size == 0:
+                sv = None
+        rr = None if r is None else np.ascontiguousarray(r, dtype=np.float32)
+        out = np.zeros(n, np.float32)
+        mx = np.zeros(1, np.float32)
+        st = self.lib.tb_solve_batch(self.ctx, n, ctypes.cast(arr, c_void_p),
+                                     None if sv is None else sv.ctypes.data,
+                                     None if rr is None else rr.ctypes.data, out.ctypes.data, mx.ctypes.data,
+                                     _native.MODES[mode])
+        _native.check(st, self.ctx)
+        return out, float(mx[0])
+
+    def contract(self, plan: Plan, tensors, mode: str = "layered") -> np.ndarray:
+        """Contract with explicit leaf tensors (column-major, -inf = zero)."""
+        bufs = [np.ascontiguousarray(np.asarray(t, np.float32).ravel(order="F")) for t in tensors]
+        for ix, b in zip(plan.code.ixs, bufs):
+            if b.size != 1 << len(ix):
+                raise ValueError("leaf tensor size does not match its labels")
+        ptrs = (c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+        out = np.zeros(1 << len(plan.code.iy), np.float32)
+        st = self.lib.tb_contract(self.ctx, plan.handle, ctypes.cast(ptrs, c_void_p), out.ctypes.data,
+                                  _native.MODES[mode])
+        _native.check(st, self.ctx)
+        return out
+
+    def dump(self, plan: Plan, slice_vals=None, mode: str = "layered") -> list[np.ndarray]:
+        labs = plan.all_node_labels()
+        outs = [np.zeros(1 << len(l), np.float32) for l in labs]
+        ptrs = (c_void_p * max(len(outs), 1))(*[o.ctypes.data for o in outs])
+        sv = None if slice_vals is None else np.ascontiguousarray(slice_vals, dtype=np.int8)
+        st = self.lib.tb_dump_intermediates(self.ctx, plan.handle, None if sv is None else sv.ctypes.data,
+                                            ctypes.cast(ptrs, c_void_p), _native.MODES[mode])
+        _native.check(st, self.ctx)
+        return outs
+
+    def last_timing(self) -> tuple[float, int]:
+        ms = c_double()
+        n = c_int64()
+        _native.check(self.lib.tb_last_timing(self.ctx, ctypes.byref(ms), ctypes.byref(n)), self.ctx)
+        return ms.value, n.value
+
+    def gemm(self, M, N, K, batch, A_ptr, B_ptr, C_ptr, stream_ptr=None):
+        st = self.lib.tb_gemm_device(self.ctx, M, N, K, batch, A_ptr, B_ptr, C_ptr, stream_ptr)
+        _native.check(st, self.ctx)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.tb_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default: Engine | None = None
+
+
+def default_engine() -> Engine:
+    global _default
+    if _default is None:
+        _default = Engine()
+    return _default

@@ -1,0 +1,366 @@
+"""CPU emulation of the engine's device programs (test infrastructure).
+
+Reads a compiled plan through the library's internal ``tbi_plan_describe``
+(host-only, no GPU) and replays the index arithmetic of the kernels in
+csrc/kernels.cuh with numpy: the leaf builder, the stream tile (grid bits,
+load tables, XOR swizzle, thread-to-output mapping, reduction split, store
+tables), the final max and the K1 GEMM of the plain lowering.  Every global
+and shared-memory access is checked against the buffer it must stay in and
+every output element must be written exactly once, so a descriptor that
+would read or write out of bounds fails here, before it reaches a GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_int8, c_int32, c_int64, c_void_p, c_float
+
+import numpy as np
+
+KMAXBITS = 48
+KMAXTILE = 16
+KTHREADS = 256
+KMAXOPT = 8
+KSMEM = 8192
+
+
+class TileDesc(ctypes.Structure):
+    _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64),
+                ("n_grid", c_int32), ("n_loop", c_int32), ("n_tc", c_int32), ("n_tr", c_int32),
+                ("na", c_int32), ("nb", c_int32), ("pa", c_int32), ("pb", c_int32), ("pc", c_int32),
+                ("split_log2", c_int32), ("n_tiles", c_int32), ("pad_", c_int32),
+                ("g_pa", c_int8 * KMAXBITS), ("g_pb", c_int8 * KMAXBITS), ("g_pc", c_int8 * KMAXBITS),
+                ("l_pa", c_int8 * KMAXBITS), ("l_pb", c_int8 * KMAXBITS),
+                ("ta_pos", c_int8 * KMAXTILE), ("tb_pos", c_int8 * KMAXTILE), ("tc_pos", c_int8 * KMAXTILE),
+                ("tc_a", c_int8 * KMAXTILE), ("tc_b", c_int8 * KMAXTILE),
+                ("tr_a", c_int8 * KMAXTILE), ("tr_b", c_int8 * KMAXTILE)]
+
+
+class Step(ctypes.Structure):
+    _fields_ = [("kind", c_int32), ("desc", c_int32), ("dep0", c_int32), ("dep1", c_int32),
+                ("n_tiles", c_int32), ("level", c_int32)]
+
+
+class LeafDesc(ctypes.Structure):
+    _fields_ = [("off", c_int64), ("nraw", c_int32), ("n_out", c_int32), ("out_bit", c_int8 * 2),
+                ("slice_idx", c_int8 * 2), ("pad_", c_int32), ("w", c_float)]
+
+
+class FinalDesc(ctypes.Structure):
+    _fields_ = [("root_off", c_int64), ("root_log2", c_int32), ("pad_", c_int32)]
+
+
+class PlainRec(ctypes.Structure):
+    _fields_ = [("node", c_int32), ("kind", c_int32), ("tile", TileDesc), ("a", c_int64), ("b", c_int64),
+                ("c", c_int64), ("M", c_int64), ("N", c_int64), ("K", c_int64), ("batch", c_int64)]
+
+
+STEP_LEAVES, STEP_TILE, STEP_GEMM, STEP_FINAL = 1, 2, 3, 4
+PLAIN_TILE, PLAIN_GEMM = 1, 2
+
+
+def check_layout(lib):
+    out = (c_int32 * 6)()
+    lib.tbi_sizes(out, 6)
+    want = [ctypes.sizeof(TileDesc), ctypes.sizeof(Step), ctypes.sizeof(LeafDesc), ctypes.sizeof(FinalDesc)]
+    assert list(out)[:4] == want, (list(out), want)
+
+
+def describe(lib, code, sliced=(), use_node_iy=False):
+    lib.tbi_plan_describe.restype = c_int32
+    lib.tbi_plan_describe.argtypes = [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p,
+                                      c_void_p, c_void_p, c_int32, c_void_p, ctypes.POINTER(c_void_p),
+                                      ctypes.POINTER(c_int64), ctypes.c_char_p, c_int32]
+    lib.tbi_free.argtypes = [c_void_p]
+    lib.tbi_sizes.argtypes = [c_void_p, c_int32]
+    check_layout(lib)
+    off, lab = code.csr()
+    iy = np.array(code.iy if code.iy else [0], np.int32)
+    ch = code.children if code.n_nodes else np.zeros((1, 2), np.int32)
+    noff, nlab = code.node_iy_csr() if use_node_iy else (None, None)
+    sl = np.array(list(sliced) if len(sliced) else [0], np.int32)
+    blob = c_void_p()
+    nbytes = c_int64()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.tbi_plan_describe(code.n_labels, code.n_tensors, off.ctypes.data, lab.ctypes.data, len(code.iy),
+                               iy.ctypes.data, code.n_nodes, ch.ctypes.data,
+                               None if noff is None else noff.ctypes.data,
+                               None if nlab is None else nlab.ctypes.data, len(sliced), sl.ctypes.data,
+                               ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
+    if rc:
+        raise ValueError(err.value.decode())
+    raw = ctypes.string_at(blob, nbytes.value)
+    lib.tbi_free(blob)
+    p = 0
+    hdr = np.frombuffer(raw, np.int64, 8, p); p += 64
+    n_tensors, n_nodes, n_steps, n_tiles, n_leaves, arena, plain_elems, nplain = [int(x) for x in hdr]
+    total = n_tensors + n_nodes
+    offs = np.frombuffer(raw, np.int64, total, p).copy(); p += 8 * total
+    ranks = np.frombuffer(raw, np.int32, total, p).copy(); p += 4 * total
+
+    def take(cls, n):
+        nonlocal p
+        out = []
+        for _ in range(n):
+            out.append(cls.from_buffer_copy(raw[p:p + ctypes.sizeof(cls)]))
+            p += ctypes.sizeof(cls)
+        return out
+
+    steps = take(Step, n_steps)
+    tiles = take(TileDesc, n_tiles)
+    leaves = take(LeafDesc, n_leaves)
+    fin = take(FinalDesc, 1)[0]
+    plain = take(PlainRec, nplain)
+    assert p == len(raw)
+    return dict(n_tensors=n_tensors, n_nodes=n_nodes, steps=steps, tiles=tiles, leaves=leaves, fin=fin,
+                plain=plain, off=offs, rank=ranks, arena=arena, plain_elems=plain_elems)
+
+
+def swz(j):
+    return j ^ (((j >> 5) ^ (j >> 10)) & 31)
+
+
+def smem_words(d):
+    hasB = d.b_off >= 0
+    w = (1 << d.na) + ((1 << d.nb) if hasB else 0)
+    w += 1 << (d.na - d.pa)
+    w += (1 << (d.nb - d.pb)) if hasB else 0
+    w += 1 << (d.n_tc - d.pc)
+    w += 2 * (1 << d.n_tr)
+    w += KTHREADS
+    return w
+
+
+def max_smem_words():
+    return KSMEM + 3 * 512 + 2 * 256 + KTHREADS
+
+
+def tensor_rank(tile_pos, grid_pos, loop_pos):
+    """Positions a tile descriptor uses for one tensor must be 0..r-1, each
+    exactly once; returns r."""
+    ps = [int(x) for x in tile_pos] + [int(x) for x in grid_pos if x >= 0] + [int(x) for x in loop_pos if x >= 0]
+    r = len(ps)
+    assert sorted(ps) == list(range(r)), f"tensor positions not a permutation: {sorted(ps)}"
+    return r
+
+
+class Neg:
+    f32 = np.float32(-np.inf)
+
+
+def emu_stream_tile(d, arena, written, expect=None):
+    """Run every CTA of one stream-tile descriptor on the arena (in place)."""
+    hasB = d.b_off >= 0
+    ra = tensor_rank(d.ta_pos[:d.na], d.g_pa[:d.n_grid], d.l_pa[:d.n_loop])
+    rb = tensor_rank(d.tb_pos[:d.nb], d.g_pb[:d.n_grid], d.l_pb[:d.n_loop]) if hasB else 0
+    rc = tensor_rank(d.tc_pos[:d.n_tc], d.g_pc[:d.n_grid], [])
+    if expect is not None:
+        assert (ra, rb, rc) == expect, ((ra, rb, rc), expect)
+    assert smem_words(d) <= max_smem_words()
+    assert d.n_tiles == 1 << d.n_grid
+    assert d.a_off % 32 == 0 or d.pa == 0 or True
+    a_lo, a_hi = d.a_off, d.a_off + (1 << ra)
+    b_lo, b_hi = (d.b_off, d.b_off + (1 << rb)) if hasB else (0, 0)
+    c_lo, c_hi = d.c_off, d.c_off + (1 << rc)
+    assert 0 <= a_lo and a_hi <= arena.size and c_hi <= arena.size and b_hi <= arena.size
+    NA = 1 << d.na
+    NB = (1 << d.nb) if hasB else 0
+    nAh = 1 << (d.na - d.pa)
+    nBh = (1 << (d.nb - d.pb)) if hasB else 0
+    nCh = 1 << (d.n_tc - d.pc)
+    ntr = 1 << d.n_tr
+    ldA = np.array([sum(1 << d.ta_pos[d.pa + b] for b in range(d.na - d.pa) if (j >> b) & 1) for j in range(nAh)],
+                   np.int64)
+    ldB = np.array([sum(1 << d.tb_pos[d.pb + b] for b in range(d.nb - d.pb) if (j >> b) & 1) for j in range(nBh)],
+                   np.int64)
+    stC = np.array([sum(1 << d.tc_pos[d.pc + b] for b in range(d.n_tc - d.pc) if (j >> b) & 1) for j in range(nCh)],
+                   np.int64)
+    IAr = np.zeros(ntr, np.int64)
+    IBr = np.zeros(ntr, np.int64)
+    for j in range(ntr):
+        xa = xb = 0
+        for b in range(d.n_tr):
+            if (j >> b) & 1:
+                if d.tr_a[b] >= 0:
+                    xa |= 1 << d.tr_a[b]
+                if d.tr_b[b] >= 0:
+                    xb |= 1 << d.tr_b[b]
+        IAr[j] = swz(xa)
+        IBr[j] = swz(xb)
+    lo_bits = min(d.n_tc, 8)
+    split = d.split_log2
+    active = 1 << (lo_bits + split)
+    opt = 1 << (d.n_tc - lo_bits)
+    assert opt <= KMAXOPT and active <= KTHREADS
+    t = np.arange(KTHREADS)
+    act = t < active
+    cl = t & ((1 << lo_bits) - 1)
+    s = t >> lo_bits
+
+    def part(xbits, tab):
+        out = np.zeros_like(xbits)
+        for b in range(d.n_tc):
+            if tab[b] >= 0:
+                out |= ((xbits >> b) & 1) << tab[b]
+        return out
+
+    iat = swz(part(cl, d.tc_a))
+    ibt = swz(part(cl, d.tc_b))
+    neg = np.float32(-np.inf)
+    for tile in range(d.n_tiles):
+        oa, ob, oc = d.a_off, d.b_off, d.c_off
+        for i in range(d.n_grid):
+            if (tile >> i) & 1:
+                if d.g_pa[i] >= 0:
+                    oa += 1 << d.g_pa[i]
+                if d.g_pb[i] >= 0:
+                    ob += 1 << d.g_pb[i]
+                oc += 1 << d.g_pc[i]
+        acc = np.full((KTHREADS, opt), neg, np.float32)
+        for rl in range(1 << d.n_loop):
+            la, lb = oa, ob
+            for i in range(d.n_loop):
+                if (rl >> i) & 1:
+                    if d.l_pa[i] >= 0:
+                        la += 1 << d.l_pa[i]
+                    if d.l_pb[i] >= 0:
+                        lb += 1 << d.l_pb[i]
+
+            def load(base, n, p, hi, lo, hi_b):
+                j = np.arange(1 << n)
+                g = base + (j & ((1 << p) - 1)) + hi[j >> p]
+                assert g.min() >= lo and g.max() < hi_b, "global load out of bounds"
+                if p >= 2:
+                    assert np.all(g[::4] % 4 == 0), "misaligned 16-byte load"
+                elif p == 1:
+                    assert np.all(g[::2] % 2 == 0), "misaligned 8-byte load"
+                sm = np.empty(1 << n, np.float32)
+                ph = swz(j)
+                assert sorted(ph.tolist()) == list(range(1 << n))
+                sm[ph] = arena[g]
+                return sm
+
+            As = load(la, d.na, d.pa, ldA, a_lo, a_hi)
+            Bs = load(lb, d.nb, d.pb, ldB, b_lo, b_hi) if hasB else None
+            for i in range(opt):
+                xa = np.zeros(KTHREADS, np.int64)
+                xb = np.zeros(KTHREADS, np.int64)
+                for b in range(lo_bits, d.n_tc):
+                    if ((i << lo_bits) >> b) & 1:
+                        if d.tc_a[b] >= 0:
+                            xa |= 1 << d.tc_a[b]
+                        if d.tc_b[b] >= 0:
+                            xb |= 1 << d.tc_b[b]
+                ia = iat ^ swz(xa)
+                ib = ibt ^ swz(xb)
+                for tt in np.nonzero(act)[0]:
+                    rr = np.arange(s[tt], ntr, 1 << split)
+                    idxa = ia[tt] ^ IAr[rr]
+                    assert idxa.size == 0 or idxa.max() < NA
+                    v = As[idxa]
+                    if hasB:
+                        idxb = ib[tt] ^ IBr[rr]
+                        assert idxb.size == 0 or idxb.max() < NB
+                        v = v + Bs[idxb]
+                    if v.size:
+                        acc[tt, i] = max(acc[tt, i], v.max())
+        if split > 0:
+            red = acc[:, 0].copy()
+            for tt in np.nonzero(act & (s == 0))[0]:
+                acc[tt, 0] = max(red[cl[tt] + (s2 << lo_bits)] for s2 in range(1 << split))
+        cmask = (1 << d.pc) - 1
+        for tt in np.nonzero(act & (s == 0))[0]:
+            for i in range(opt):
+                c = cl[tt] + (i << lo_bits)
+                g = oc + (c & cmask) + stC[c >> d.pc]
+                assert c_lo <= g < c_hi, "store out of bounds"
+                written[g] += 1
+                arena[g] = acc[tt, i]
+    return (c_lo, c_hi)
+
+
+def emu_leaves(leaves, arena, written, slice_vals):
+    for ld in leaves:
+        for e in range(1 << ld.n_out):
+            best = -np.inf
+            for raw in range(1 << ld.nraw):
+                ok = True
+                for k in range(ld.nraw):
+                    x = (raw >> k) & 1
+                    if ld.slice_idx[k] >= 0:
+                        ok &= x == int(slice_vals[ld.slice_idx[k]])
+                    else:
+                        ok &= ((e >> ld.out_bit[k]) & 1) == x
+                if not ok:
+                    continue
+                v = (ld.w if raw & 1 else 0.0) if ld.nraw == 1 else (-np.inf if raw == 3 else 0.0)
+                best = max(best, v)
+            assert 0 <= ld.off + e < arena.size
+            arena[ld.off + e] = best
+            written[ld.off + e] += 1
+
+
+def emu_gemm(rec, arena):
+    M, N, K, B = rec.M, rec.N, rec.K, rec.batch
+    assert M % 16 == 0 and N % 16 == 0 and K % 16 == 0
+    for x, n in ((rec.a, M * K * B), (rec.b, K * N * B), (rec.c, M * N * B)):
+        assert 0 <= x and x + n <= arena.size and x % 4 == 0
+    A = arena[rec.a:rec.a + M * K * B].reshape(B, K, M)
+    Bm = arena[rec.b:rec.b + K * N * B].reshape(B, N, K)
+    C = (A[:, None, :, :] + Bm[:, :, :, None]).max(axis=2)  # (B, N, M)
+    arena[rec.c:rec.c + M * N * B] = C.reshape(-1)
+
+
+def run_fused(desc, weights, slice_vals=()):
+    """Replay the fused program; returns (root tensor, arena, node views)."""
+    arena = np.full(desc["arena"], np.nan, np.float32)
+    written = np.zeros(desc["arena"], np.int32)
+    leaves = desc["leaves"]
+    for i, ld in enumerate(leaves):
+        if ld.nraw == 1:
+            pass
+    # weights: the engine binds w into LeafDesc; do the same here
+    T = desc["n_tensors"]
+    for ld, w in zip(leaves, weights):
+        ld.w = float(w)
+    emu_leaves(leaves, arena, written, slice_vals)
+    off, rank = desc["off"], desc["rank"]
+    node_of_step = {}
+    j = 0
+    for si, st in enumerate(desc["steps"]):
+        if st.kind == STEP_TILE:
+            d = desc["tiles"][st.desc]
+            expect = None
+            if desc["n_nodes"]:
+                # node j's operands are its children; ranks known from the blob
+                node_of_step[si] = j
+                j += 1
+            emu_stream_tile(d, arena, written)
+    fin = desc["fin"]
+    root = arena[fin.root_off:fin.root_off + (1 << fin.root_log2)].copy()
+    assert np.all(written[fin.root_off:fin.root_off + (1 << fin.root_log2)] == 1), "root not written exactly once"
+    # every node output written exactly once
+    for idx in range(T, T + desc["n_nodes"]):
+        seg = written[off[idx]:off[idx] + (1 << rank[idx])]
+        assert np.all(seg == 1), f"tensor {idx} elements written {np.unique(seg)} times"
+    nodes = [arena[off[T + k]:off[T + k] + (1 << rank[T + k])].copy() for k in range(desc["n_nodes"])]
+    return root, nodes
+
+
+def run_plain(desc, weights, slice_vals=()):
+    arena = np.full(desc["plain_elems"], np.nan, np.float32)
+    written = np.zeros(desc["plain_elems"], np.int32)
+    for ld, w in zip(desc["leaves"], weights):
+        ld.w = float(w)
+    emu_leaves(desc["leaves"], arena, written, slice_vals)
+    for rec in desc["plain"]:
+        if rec.kind == PLAIN_TILE:
+            emu_stream_tile(rec.tile, arena, written)
+        else:
+            emu_gemm(rec, arena)
+    if desc["n_nodes"] == 0:
+        emu_stream_tile(desc["tiles"][0], arena, written)
+    fin = desc["fin"]
+    T = desc["n_tensors"]
+    off, rank = desc["off"], desc["rank"]
+    nodes = [arena[off[T + k]:off[T + k] + (1 << rank[T + k])].copy() for k in range(desc["n_nodes"])]
+    return arena[fin.root_off:fin.root_off + (1 << fin.root_log2)].copy(), nodes

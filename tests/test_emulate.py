@@ -1,0 +1,89 @@
+"""CPU replay of the device programs the engine compiles (index arithmetic
+of csrc/kernels.cuh): every access in bounds, every output written once, and
+every intermediate equal to the oracle's, for the fused and the plain path."""
+import numpy as np
+import pytest
+
+import emulate
+from cases import corner_cases, ksg_case, rr_case
+
+
+@pytest.fixture(scope="module")
+def lib(native):
+    return native.engine_lib()
+
+
+def _check(lib, orc, code, w, sliced=(), sv=()):
+    root, nodes = emulate.run_fused(emulate.describe(lib, code, sliced), w, sv)
+    rootp, nodesp = emulate.run_plain(emulate.describe(lib, code, sliced), w, sv)
+    ref, dumps = orc.execute(code, w, sliced=sliced, slice_vals=sv, dump=True)
+    assert np.array_equal(root, ref) and np.array_equal(rootp, ref)
+    for a, b, c in zip(nodes, nodesp, dumps or []):
+        assert np.array_equal(a, c) and np.array_equal(b, c)
+    return float(np.max(ref))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_rr_fused_and_plain(tb, orc, lib, seed):
+    g, w, code = rr_case(tb, 20 + 4 * seed, seed)
+    _check(lib, orc, code, w)
+
+
+def test_slices_and_open_labels(tb, orc, lib):
+    g, w, code = rr_case(tb, 24, 11)
+    full = _check(lib, orc, code, w)
+    vals = [_check(lib, orc, code, w, [0, 5], (a, b)) for a in (0, 1) for b in (0, 1)]
+    assert max(vals) == full
+    opened = tb.CompressedEinsum(code.ixs, [2, 9], code.children, n_labels=code.n_labels)
+    _check(lib, orc, opened, w)
+    for a in (0, 1):
+        _check(lib, orc, opened, w, [4], (a,))
+
+
+def test_ksg(tb, orc, lib):
+    g, w, code = ksg_case(tb, 5, 1)
+    _check(lib, orc, code, w)
+
+
+def test_corner_cases(tb, orc, lib):
+    for name, g, w, code in corner_cases(tb):
+        _check(lib, orc, code, w)
+
+
+def test_explicit_node_labels(tb, orc, lib):
+    """Node outputs given explicitly (as a DynamicNestedEinsum carries them),
+    including labels kept longer than needed."""
+    g, w, code = rr_case(tb, 20, 4)
+    labs = code.labels_of_nodes()
+    # keep one extra label alive in a few nodes where it is available
+    T = code.n_tensors
+    full = [list(dict.fromkeys(ix)) for ix in code.ixs] + labs
+    extra = []
+    for j, (a, b) in enumerate(code.children):
+        uni = list(dict.fromkeys(full[a] + full[b]))
+        keep = list(labs[j])
+        drop = [x for x in uni if x not in keep]
+        if drop and j % 3 == 0 and j < code.n_nodes - 1:
+            keep = keep + [drop[0]]
+        extra.append(keep)
+        full[T + j] = keep
+    c2 = tb.CompressedEinsum(code.ixs, code.iy, code.children, node_iy=extra, n_labels=code.n_labels)
+    d = emulate.describe(lib, c2, use_node_iy=True)
+    root, nodes = emulate.run_fused(d, w)
+    ref, dumps = orc.execute(c2, w, node_iy=extra, dump=True)
+    assert np.array_equal(root, ref)
+    for a, b in zip(nodes, dumps):
+        assert np.array_equal(a, b)
+
+
+def test_invalid_plans_rejected(tb, lib):
+    g, w, code = rr_case(tb, 20, 1)
+    bad = code.children.copy()
+    bad[-1, 0] = bad[-1, 1]
+    with pytest.raises(ValueError):
+        emulate.describe(lib, tb.CompressedEinsum(code.ixs, [], bad, n_labels=code.n_labels))
+    labs = code.labels_of_nodes()
+    labs[0] = []  # drops labels needed later
+    with pytest.raises(ValueError):
+        emulate.describe(lib, tb.CompressedEinsum(code.ixs, [], code.children, node_iy=labs,
+                                                  n_labels=code.n_labels), use_node_iy=True)

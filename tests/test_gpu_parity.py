@@ -1,0 +1,111 @@
+"""GPU parity: every execution mode, through the C ABI, equals the CPU oracle
+bit for bit -- per item, per intermediate tensor, for f32 and int32."""
+import numpy as np
+import pytest
+
+from cases import corner_cases, ksg_case, random_generic_network, random_tensor, rr_case
+
+pytestmark = pytest.mark.gpu
+MODES = ["plain", "layered", "batched"]
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_rr_all_modes(tb, orc, exact, engine, seed):
+    g, w, code = rr_case(tb, 30 + 10 * seed, seed)
+    ref = orc.solve(code, w)
+    plan = engine.plan(code, w)
+    for mode in MODES:
+        out, mx = engine.solve_batch([plan], mode=mode)
+        assert np.float32(mx) == np.float32(ref) == out[0], (mode, mx, ref)
+    if g.n <= 60:
+        assert ref == exact.branch_and_bound(g.n, g.edges, w)
+
+
+@pytest.mark.parametrize("mode", ["plain", "layered"])
+def test_intermediates_bit_exact(tb, orc, engine, mode):
+    g, w, code = rr_case(tb, 40, 3)
+    plan = engine.plan(code, w)
+    labs = plan.all_node_labels()
+    ref_root, dumps = orc.execute(code, w, node_iy=labs, dump=True)
+    got = engine.dump(plan, mode=mode)
+    assert len(got) == len(dumps)
+    for a, b in zip(got, dumps):
+        assert np.array_equal(a, b)
+
+
+def test_int32_engine(tb, orc, engine_i32):
+    for seed in range(3):
+        g, w, code = rr_case(tb, 40, seed)
+        ref = orc.solve(code, w, dtype=np.int32)
+        plan = engine_i32.plan(code, w)
+        for mode in MODES:
+            _, mx = engine_i32.solve_batch([plan], mode=mode)
+            assert mx == ref, (mode, mx, ref)
+
+
+def test_corner_cases(tb, orc, engine):
+    for name, g, w, code in corner_cases(tb):
+        plan = engine.plan(code, w)
+        ref = orc.solve(code, w)
+        for mode in MODES:
+            _, mx = engine.solve_batch([plan], mode=mode)
+            assert mx == ref, (name, mode)
+
+
+def test_uneven_batch_of_branches(tb, orc, engine):
+    """Many different plans in one batched launch (branch batch)."""
+    plans, refs, rs = [], [], []
+    for seed in range(12):
+        if seed % 3 == 0:
+            g, w, code = ksg_case(tb, 4 + seed % 4, seed)
+        else:
+            g, w, code = rr_case(tb, 12 + 4 * seed, seed)
+        plans.append(engine.plan(code, w))
+        refs.append(orc.solve(code, w))
+        rs.append(float(seed))
+    expect = np.array(refs, np.float32) + np.array(rs, np.float32)
+    for mode in MODES:
+        out, mx = engine.solve_batch(plans, r=np.array(rs, np.float32), mode=mode)
+        assert np.array_equal(out, expect), mode
+        assert mx == expect.max()
+    # graph replay of the same batch gives the same numbers
+    out2, _ = engine.solve_batch(plans, r=np.array(rs, np.float32), mode="batched")
+    assert np.array_equal(out2, expect)
+
+
+def test_sliced_items(tb, orc, engine):
+    g, w, code = rr_case(tb, 40, 5)
+    full = orc.solve(code, w)
+    sliced = [0, 7, 13]
+    plan = engine.plan(code, w, sliced=sliced)
+    vals = ((np.arange(8)[:, None] >> np.arange(3)[None, :]) & 1).astype(np.int8)
+    refs = np.array([orc.solve(code, w, sliced=sliced, slice_vals=v) for v in vals], np.float32)
+    for mode in MODES:
+        out, mx = engine.solve_batch([plan] * 8, slice_vals=list(vals), mode=mode)
+        assert np.array_equal(out, refs), mode
+        assert mx == full
+
+
+def test_open_labels_with_slices(tb, orc, engine):
+    g, w, code = rr_case(tb, 36, 8)
+    full = orc.solve(code, w)
+    opened = tb.CompressedEinsum(code.ixs, [3, 11], code.children, n_labels=code.n_labels)
+    plan = engine.plan(opened, w, sliced=[20])
+    out, mx = engine.solve_batch([plan, plan], slice_vals=[np.array([0], np.int8), np.array([1], np.int8)],
+                                 mode="batched")
+    assert mx == full
+
+
+def test_contract_generic_tensors(tb, orc, engine):
+    """code(tensors...) with arbitrary tropical tensors (test/utils.jl:34)."""
+    rng = np.random.default_rng(9)
+    for it in range(30):
+        ixs, iy, ch = random_generic_network(rng, n_labels=12, n_tensors=7, max_rank=5,
+                                             n_open=int(rng.integers(0, 3)))
+        code = tb.CompressedEinsum(ixs, iy, ch)
+        data = [random_tensor(rng, len(ix)) for ix in ixs]
+        ref = orc.execute(code, None, leaf_data=data)
+        plan = engine.plan(code)
+        for mode in ("plain", "layered"):
+            got = engine.contract(plan, data, mode=mode)
+            assert np.array_equal(got, ref), (it, mode)
