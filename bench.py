@@ -1,0 +1,403 @@
+"""Benchmark: MIS solves/s of the tropical contraction on GB300.
+
+Default workload: ``rr220`` -- one random 3-regular graph, n=220, unit
+weights, contracted in one piece with no slicing (a step = one full MIS solve
+= one contraction of the whole network).  Other workloads: ``--config``.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config rr220|rr100_b10|rr300_s22|ksg32_b20] [--mode batched|layered|plain]
+    python bench.py --make rr220 ...     # (re)build workload fixtures
+
+Under torchrun each rank runs its own replica of the workload on its own GPU
+(independent units, no collective on the data path): scaling is weak and
+``value`` is the units of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as _ge  # noqa: E402
+
+METRIC = "MIS solves/s"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_workload(tb, name):
+    from tensorbranching_gb300 import workloads
+
+    return workloads.load(name)
+
+
+def make_items(engine, wl, tb):
+    """Plans and per-item inputs of one step of the workload."""
+    plans, svs, rs = [], [], []
+    sliced = wl["sliced"]
+    for b in wl["branches"]:
+        if b.code is None:
+            continue
+        p = engine.plan(b.code, b.p.weight_array(), sliced=sliced)
+        if sliced:
+            k = len(sliced)
+            vals = ((np.arange(1 << k)[:, None] >> np.arange(k)[None, :]) & 1).astype(np.int8)
+            for row in vals:
+                plans.append(p)
+                svs.append(row)
+                rs.append(b.r)
+        else:
+            plans.append(p)
+            svs.append(np.zeros(0, np.int8))
+            rs.append(b.r)
+    return plans, svs, np.array(rs, np.float32)
+
+
+def expected_answer(wl):
+    """Units a step solves: graphs (MIS values) per step."""
+    if wl["name"] == "rr100_b10":
+        return len(wl["graphs"])
+    return 1
+
+
+def run_cpu_baseline(tb, orc, wl, budget_s: float):
+    """The oracle port (GEMM lowering, OpenMP on every host core) on a bounded
+    sample: the first nodes of the tree in post-order until ~budget_s of CPU
+    work, extrapolated by algorithmic ops to full solves."""
+    import ctypes
+
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    b = [x for x in wl["branches"] if x.code is not None]
+    total_ops = 0.0
+    done_ops = 0.0
+    t_used = 0.0
+    nodes_done = 0
+    nodes_total = 0
+    sliced = wl["sliced"]
+    for br in b:
+        code = br.code
+        if sliced:
+            code = code.remove_labels(sliced)
+        labs = [list(dict.fromkeys(ix)) for ix in code.ixs] + code.labels_of_nodes()
+        ops = [2.0 * 2 ** len(set(labs[int(a)]) | set(labs[int(c)])) for a, c in code.children]
+        mult = (1 << len(sliced)) if sliced else 1
+        total_ops += sum(ops) * mult
+        nodes_total += code.n_nodes * mult
+    # time prefixes of the first network until the budget is used
+    br = b[0]
+    code = br.code.remove_labels(sliced) if sliced else br.code
+    labs = [list(dict.fromkeys(ix)) for ix in code.ixs] + code.labels_of_nodes()
+    ops = np.array([2.0 * 2 ** len(set(labs[int(a)]) | set(labs[int(c)])) for a, c in code.children])
+    w = br.p.weight_array()
+    k = min(code.n_nodes, 16)
+    sample = ""
+    while True:
+        sub = _prefix_code(tb, code, k)
+        t0 = time.perf_counter()
+        orc.execute(sub, w, mode="gemm")
+        dt = time.perf_counter() - t0
+        if dt >= budget_s * 0.5 or k >= code.n_nodes:
+            done_ops = float(ops[:k].sum())
+            t_used = dt
+            nodes_done = k
+            break
+        # grow the prefix toward the budget
+        k = min(code.n_nodes, max(k + 1, int(k * 2)))
+    rate = done_ops / t_used  # tropical ops per second on the host
+    solves_per_s = rate / total_ops * expected_answer(wl)
+    sample = (f"first {nodes_done} of {code.n_nodes} contraction nodes (post-order) of one network, "
+              f"{done_ops:.3g} of {total_ops:.3g} ops per step, {t_used:.1f}s; extrapolated by algorithmic ops")
+    return {"value": solves_per_s, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
+            "ops_per_s": rate}
+
+
+def _prefix_code(tb, code, k):
+    """The sub-network formed by the first k nodes (post-order) and the
+    leaves they use: the forest's roots are merged at the end with the open
+    labels that the full tree still needs (roots keep their own outputs)."""
+    if k >= code.n_nodes:
+        return code
+    T = code.n_tensors
+    labs = [list(dict.fromkeys(ix)) for ix in code.ixs] + code.labels_of_nodes()
+    used = set()
+    for a, b in code.children[:k]:
+        used.add(int(a))
+        used.add(int(b))
+    nodes = list(range(k))
+    roots = [T + j for j in nodes if T + j not in used]
+    leaves = sorted(x for x in used if x < T)
+    # renumber
+    idmap = {old: i for i, old in enumerate(leaves)}
+    ixs = [code.ixs[x] for x in leaves]
+    ch = []
+    niy = []
+    for j in nodes:
+        a, b = (int(x) for x in code.children[j])
+        idmap[T + j] = len(leaves) + len(ch)
+        ch.append((idmap[a], idmap[b]))
+        niy.append(labs[T + j])
+    # merge remaining roots (outer products)
+    cur = idmap[roots[0]]
+    cur_l = labs[roots[0]]
+    for r in roots[1:]:
+        ch.append((cur, idmap[r]))
+        cur_l = cur_l + [x for x in labs[r] if x not in cur_l]
+        niy.append(cur_l)
+        cur = len(leaves) + len(ch) - 1
+    # unused leaves are ignored: a sample only needs a valid tree
+    iy = niy[-1]
+    return tb.CompressedEinsum(ixs, iy, np.array(ch, np.int32), node_iy=niy, n_labels=code.n_labels)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="rr220")
+    ap.add_argument("--mode", default="batched", choices=["batched", "layered", "plain"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--make", nargs="*")
+    args = ap.parse_args()
+
+    tb = _ge.load_package()
+    if args.make is not None:
+        from tensorbranching_gb300 import workloads
+
+        for nm in args.make or list(workloads.BUILDERS):
+            workloads.make(nm)
+        return
+
+    ws, rank, local = dist_env()
+    wl = load_workload(tb, args.config)
+    units = expected_answer(wl)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        orc = _ge.load_oracle()
+        orc.build()
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = run_cpu_baseline(tb, orc, wl, max(2.0, args.cpu_budget / 4))
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = statistics.median(vals)
+        out = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * units / v,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded graphs)",
+               "config": {"workload": args.config, "detail": _desc(args.config)},
+               "cpu_baseline": {"value": v, "unit": "solves/s", "cores": r["cores"], "kind": "port",
+                                "sample": r["sample"]},
+               "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    eng = tb.Engine(device=dev)
+    plans, svs, rs = make_items(eng, wl, tb)
+    st = plans[0].stats()
+    uniq = {id(p): p for p in plans}
+    ops = sum(uniq[k].stats()["ops"] for k in uniq) if not wl["sliced"] else st["ops"] * len(plans)
+    byts = sum(uniq[k].stats()["bytes"] for k in uniq) if not wl["sliced"] else st["bytes"] * len(plans)
+    # check the answer once
+    out0, mx0 = eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
+    # L2 flush buffer (larger than the 129 MB L2)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def step():
+        return eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
+
+    for _ in range(args.warmup):
+        step()
+    # device-timed region: inputs resident, L2 flushed between steps
+    dev_ms = []
+    launches = 0
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            o, m = step()
+            ms, nl = eng.last_timing()
+            dev_ms.append(ms)
+            launches += nl
+            assert m == mx0
+    torch.cuda.synchronize()
+    t_dev = sum(dev_ms) / 1000.0
+    # e2e: bind weights from host (H2D) + solve + result read-back (D2H), wall clock
+    uplans = list(uniq.values())
+    weights = [p.code for p in uplans]
+    h2d = sum(int(p.stats()["n_tensors"]) * 32 for p in uplans) + 4 * len(plans) + sum(len(x) for x in svs)
+    d2h = 4 * (len(plans) + 1)
+    wts = {id(p): None for p in uplans}
+    for b in wl["branches"]:
+        pass
+    host_w = [np.ascontiguousarray(_weights_of(wl, p), np.float32) for p in uplans]
+    if ws > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for p, w in zip(uplans, host_w):
+            p.bind_mis(w)
+        o, m = step()
+        assert m == mx0
+    t_e2e = time.perf_counter() - t0
+    if ws > 1:
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    value = ws * args.steps * units / t_dev
+    ms_per_step = 1000.0 * t_dev / args.steps
+    hbm, peak_kind = _peaks()
+    achieved = byts / (ms_per_step / 1000.0) / 1e9
+    traffic = _profiled_traffic(args.config, args.mode)
+    res = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded graphs, weights as described)",
+        "config": {"workload": args.config, "detail": _desc(args.config), "mode": args.mode,
+                   "items_per_step": len(plans), "graphs_per_step": units, "tc": st["tc"], "sc": st["sc"],
+                   "rwc": st["rwc"], "l2": "flushed between steps (256 MiB write)",
+                   "answer": mx0, "parallelism": f"replicas x{ws}"},
+        "tropical_gops": ops / (ms_per_step / 1000.0) / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "note": f"peak is the {peak_kind} copy bandwidth; achieved = algorithmic bytes "
+                             f"4(|A|+|B|+|C|) summed over nodes per step / device time of the step"},
+        "e2e": {"value": ws * args.steps * units / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        orc = _ge.load_oracle()
+        orc.build()
+        res["cpu_baseline"] = run_cpu_baseline(tb, orc, wl, args.cpu_budget)
+    print(json.dumps(res))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _weights_of(wl, plan):
+    for b in wl["branches"]:
+        if b.code is plan.code:
+            return b.p.weight_array()
+    return np.ones(plan.code.n_labels, np.float32)
+
+
+def _profiled_traffic(config, mode):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary, if one exists for this workload (line 'traffic_bytes_per_step: X')."""
+    p = os.path.join(ROOT, "profiles", f"traffic_{config}_{mode}.txt")
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_step:"):
+                return float(line.split(":")[1])
+    return None
+
+
+def _desc(name):
+    from tensorbranching_gb300 import workloads
+
+    return workloads.WORKLOADS.get(name, name)
+
+
+if __name__ == "__main__":
+    main()

@@ -64,8 +64,11 @@ __global__ void __launch_bounds__(kThreads) k_reduce_max(const float* v, int n, 
 
 template <typename T>
 __device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, int64_t tile, int* smem,
-                                         float* out_item, int item) {
+                                         float* out_item, const float* r, int item, int* err) {
   switch (st.kind) {
+    case STEP_GEMM:
+      gemm_tile_any<T>(it.gemms[st.desc], tile, it.arena, smem, err);
+      break;
     case STEP_LEAVES:
       leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile);
       break;
@@ -73,7 +76,7 @@ __device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, i
       stream_tile<T>(it.tiles[st.desc], tile, it.arena, smem);
       break;
     case STEP_FINAL:
-      final_tile<T>(it.fin, it.arena, it.r, out_item + item);
+      final_tile<T>(it.fin, it.arena, r ? r[item] : 0.0f, out_item + item);
       break;
     default:
       break;
@@ -93,7 +96,8 @@ __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int
 // waiting: the previous launch on the stream finished every dependency.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
-                                                   int64_t first_ticket, float* out_item) {
+                                                   int64_t first_ticket, float* out_item, const float* r,
+                                                   int* err) {
   extern __shared__ int tb_smem[];
   __shared__ int s_g;
   int64_t tk = first_ticket + blockIdx.x;
@@ -101,7 +105,7 @@ __global__ void __launch_bounds__(kThreads) k_level(const ItemDev<T>* items, con
   __syncthreads();
   const Group g = groups[s_g];
   const ItemDev<T>& it = items[g.item];
-  run_step<T>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, g.item);
+  run_step<T>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, r, g.item, err);
 }
 
 // Persistent executor.  Tickets are handed out in dependency order, so a
@@ -110,7 +114,8 @@ __global__ void __launch_bounds__(kThreads) k_level(const ItemDev<T>* items, con
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_persistent(const ItemDev<T>* items, const Group* groups, int n_groups,
                                                         int64_t n_tickets, int* done, unsigned long long* ticket,
-                                                        int* err, float* out_item, int64_t timeout_ns) {
+                                                        int* err, float* out_item, const float* r,
+                                                        int64_t timeout_ns) {
   extern __shared__ int tb_smem[];
   __shared__ long long s_tk;
   __shared__ int s_g, s_stop;
@@ -149,7 +154,7 @@ __global__ void __launch_bounds__(kThreads) k_persistent(const ItemDev<T>* items
     if (s_stop) break;
     const Group g = groups[s_g];
     const ItemDev<T>& it = items[g.item];
-    run_step<T>(it, it.steps[g.step], s_tk - g.first, tb_smem, out_item, g.item);
+    run_step<T>(it, it.steps[g.step], s_tk - g.first, tb_smem, out_item, r, g.item, err);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) atomicAdd(done + it.done_base + g.step, 1);
@@ -231,7 +236,8 @@ struct tb_plan {
   PlanHost h;
   DevBuf d_steps, d_tiles, d_gemms, d_leaves;
   bool uploaded = false;
-  uint64_t version = 0;  // bumps on bind
+  bool structure_uploaded = false;
+  uint64_t version = 0;  // bumps when device buffers move
 };
 
 struct GraphKey {
@@ -249,7 +255,7 @@ struct tb_ctx {
   int sms = 0;
   int persistent_ctas = 0;
   size_t budget = 0;
-  DevBuf arena, items, groups, done, misc, slice_vals, out_item;
+  DevBuf arena, items, groups, done, misc, slice_vals, out_item, rvals;
   HostBuf h_items, h_groups, h_in, h_out;
   // batch state of the last upload (reused when the same plans come again)
   GraphKey key;
@@ -287,8 +293,10 @@ static size_t elem() { return sizeof(T); }
 static size_t dtype_size(const tb_ctx*) { return 4; }
 
 static int max_stream_smem_bytes() {
-  // largest dynamic shared memory a stream tile may ask for (see plan_tile)
-  return (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4;
+  // largest dynamic shared memory a stream tile may ask for (see plan_tile),
+  // or a GEMM tile's staging stages
+  int st = (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4;
+  return st > gemm_smem_bytes_max() ? st : gemm_smem_bytes_max();
 }
 
 template <typename T>
@@ -313,9 +321,13 @@ static tb_status upload_plan(tb_plan* p) {
     return cudaSuccess;
   };
   const PlanHost& h = p->h;
-  CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
-  CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
-  CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
+  if (!p->structure_uploaded) {
+    CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
+    CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
+    CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
+    p->structure_uploaded = true;
+  }
+  // the leaves carry the weights: the only part a re-bind changes
   CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
   p->uploaded = true;
   return TB_OK;
@@ -361,7 +373,7 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
 // ---------------------------------------------------------------------------
 template <typename T>
 static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std::vector<int64_t>& arena_off,
-                              const std::vector<int64_t>& sv_off, const float* r, bool skip_leaves) {
+                              const std::vector<int64_t>& sv_off, bool skip_leaves) {
   // items
   CU(c->h_items.ensure(sizeof(ItemDev<T>) * n));
   ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(c->h_items.p);
@@ -375,7 +387,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
     it.slice_vals = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
-    it.r = r ? r[i] : 0.0f;
+    it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = done_base;
     it.n_steps = (int)p->h.steps.size();
@@ -439,22 +451,25 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
   const ItemDev<T>* items = reinterpret_cast<const ItemDev<T>*>(c->items.p);
   const Group* groups = reinterpret_cast<const Group*>(c->groups.p);
   float* out_item = reinterpret_cast<float*>(c->out_item.p);
+  const float* rv = reinterpret_cast<const float*>(c->rvals.p);
   const int smem = max_stream_smem_bytes();
+  CU(cudaMemsetAsync(c->misc.p, 0, 64, s));
   if (mode == TB_MODE_BATCHED) {
     CU(cudaMemsetAsync(c->done.p, 0, sizeof(int) * done_words, s));
-    CU(cudaMemsetAsync(c->misc.p, 0, 64, s));
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
     int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
     int64_t timeout_ns = (int64_t)c->opt.timeout_ms * 1000000LL;
     k_persistent<T><<<c->persistent_ctas, kThreads, smem, s>>>(items, groups, c->n_groups, c->n_tickets,
                                                                reinterpret_cast<int*>(c->done.p), ticket, err,
-                                                               out_item, timeout_ns);
+                                                               out_item, rv, timeout_ns);
     CU(cudaGetLastError());
     launches++;
   } else {
     for (auto& lr : c->level_ranges) {
       if (lr.second > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
-      k_level<T><<<(unsigned)lr.second, kThreads, smem, s>>>(items, groups, c->n_groups, lr.first, out_item);
+      k_level<T><<<(unsigned)lr.second, kThreads, smem, s>>>(items, groups, c->n_groups, lr.first, out_item, rv,
+                                                             reinterpret_cast<int*>(
+                                                                 reinterpret_cast<char*>(c->misc.p) + 16));
       CU(cudaGetLastError());
       launches++;
     }
@@ -490,8 +505,14 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
   CU(c->slice_vals.ensure(std::max<size_t>(sv, 16)));
   CU(c->out_item.ensure(sizeof(float) * (n + 1)));
   CU(c->h_out.ensure(sizeof(float) * (n + 1) + 64));
-  CU(c->h_in.ensure(std::max<size_t>(sv, 16)));
-  if (sv) std::memcpy(c->h_in.p, slice_vals, sv);
+  // pinned staging of the per-call inputs: r values, then slice values
+  const size_t r_bytes = align_up(sizeof(float) * n, 16);
+  CU(c->h_in.ensure(r_bytes + std::max<size_t>(sv, 16)));
+  CU(c->rvals.ensure(r_bytes));
+  float* h_r = reinterpret_cast<float*>(c->h_in.p);
+  int8_t* h_sv = reinterpret_cast<int8_t*>(c->h_in.p) + r_bytes;
+  for (int i = 0; i < n; i++) h_r[i] = r ? r[i] : 0.0f;
+  if (sv) std::memcpy(h_sv, slice_vals, sv);
   float* hout = reinterpret_cast<float*>(c->h_out.p);
   int64_t launches = 0;
   CU(cudaEventRecord(c->ev0, c->stream));
@@ -502,7 +523,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     size_t bytes = (size_t)need * sizeof(T) + 256;
     if (bytes > c->budget) return fail(TB_ERR_OOM, "plan needs more device memory than the budget");
     CU(c->arena.ensure(bytes));
-    if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, c->h_in.p, sv, cudaMemcpyHostToDevice, c->stream));
+    if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, h_sv, sv, cudaMemcpyHostToDevice, c->stream));
     T* arena = reinterpret_cast<T*>(c->arena.p);
     for (int i = 0; i < n; i++) {
       tb_plan* p = plans[i];
@@ -565,17 +586,6 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
       key.versions.push_back(plans[i]->version);
     }
     bool reuse = c->have_key && c->key == key && c->n_items == n;
-    // r values live in the items table; changing r means re-upload
-    if (reuse && r) {
-      const ItemDev<T>* hi = reinterpret_cast<const ItemDev<T>*>(c->h_items.p);
-      for (int i = 0; i < n && reuse; i++)
-        if (hi[i].r != r[i]) reuse = false;
-    }
-    if (reuse && !r) {
-      const ItemDev<T>* hi = reinterpret_cast<const ItemDev<T>*>(c->h_items.p);
-      for (int i = 0; i < n && reuse; i++)
-        if (hi[i].r != 0.0f) reuse = false;
-    }
     int done_words = 0;
     for (int i = 0; i < n; i++) done_words += (int)plans[i]->h.steps.size();
     if (!reuse) {
@@ -584,7 +594,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
         c->gexec = nullptr;
       }
       c->have_key = false;
-      if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, r, false))) return st;
+      if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, false))) return st;
       CU(cudaStreamSynchronize(c->stream));
       c->key = key;
       c->have_key = true;
@@ -594,12 +604,11 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
         cudaGraph_t g;
         CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         int64_t l2 = 0;
-        if (sv) {
-          cudaError_t e = cudaMemcpyAsync(c->slice_vals.p, c->h_in.p, sv, cudaMemcpyHostToDevice, c->stream);
-          if (e != cudaSuccess) {
-            cudaStreamEndCapture(c->stream, &g);
-            return fail(TB_ERR_CUDA, cudaGetErrorString(e));
-          }
+        cudaError_t e = cudaMemcpyAsync(c->rvals.p, h_r, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess && sv) e = cudaMemcpyAsync(c->slice_vals.p, h_sv, sv, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) {
+          cudaStreamEndCapture(c->stream, &g);
+          return fail(TB_ERR_CUDA, cudaGetErrorString(e));
         }
         st = enqueue_batched<T>(c, n, mode, done_words, l2);
         cudaError_t e1 = cudaMemcpyAsync(hout, c->out_item.p, sizeof(float) * (n + 1), cudaMemcpyDeviceToHost,
@@ -618,18 +627,19 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
       CU(cudaGraphLaunch(c->gexec, c->stream));
       launches += c->launches_graph;
     } else {
-      if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, c->h_in.p, sv, cudaMemcpyHostToDevice, c->stream));
+      CU(cudaMemcpyAsync(c->rvals.p, h_r, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+      if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, h_sv, sv, cudaMemcpyHostToDevice, c->stream));
       if ((st = enqueue_batched<T>(c, n, mode, done_words, launches))) return st;
       CU(cudaMemcpyAsync(hout, c->out_item.p, sizeof(float) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
     }
     CU(cudaEventRecord(c->ev1, c->stream));
     CU(cudaEventSynchronize(c->ev1));
-    if (mode == TB_MODE_BATCHED) {
+    {
       int err = 0;
       CU(cudaMemcpy(&err, reinterpret_cast<char*>(c->misc.p) + 16, sizeof(int), cudaMemcpyDeviceToHost));
       if (err) {
         c->have_key = false;
-        return fail(TB_ERR_TIMEOUT, "a device-side wait of the persistent executor timed out");
+        return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
       }
     }
   }
@@ -733,7 +743,7 @@ tb_status tb_plan_create(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const
   p->ctx = ctx;
   std::string e;
   try {
-    e = compile_plan(in, p->h, 0);
+    e = compile_plan(in, p->h, 4);
   } catch (const std::exception& ex) {
     e = std::string("plan compiler: ") + ex.what();
   }
@@ -786,6 +796,9 @@ tb_status tb_plan_node_labels(const tb_plan* p, int32_t node, int32_t cap, int32
 tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   if (!p || !w) return fail(TB_ERR_INVALID, "null argument");
   const bool is_int = p->ctx->opt.dtype == TB_DTYPE_I32;
+  for (int i = 0; i < p->h.n_tensors; i++)
+    if (p->h.leaves[i].nraw < 1 || p->h.leaves[i].nraw > 2)
+      return fail(TB_ERR_INVALID, "independent-set leaves have one (vertex) or two (edge) labels");
   for (int i = 0; i < p->h.n_tensors; i++) {
     LeafDesc& ld = p->h.leaves[i];
     if (ld.nraw == 1) {
@@ -798,8 +811,13 @@ tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   }
   p->h.has_weights = true;
   p->uploaded = false;
-  p->version = ++p->ctx->plan_counter;
-  return upload_plan(p);
+  void* before[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
+  tb_status st = upload_plan(p);
+  if (st) return st;
+  void* after[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
+  // captured graphs hold these device pointers: a move invalidates them
+  if (std::memcmp(before, after, sizeof(before)) != 0) p->version = ++p->ctx->plan_counter;
+  return TB_OK;
 }
 
 tb_status tb_solve_batch(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8_t* slice_vals, const float* r,
@@ -877,18 +895,43 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
       cudaGraphExecDestroy(c->gexec);
       c->gexec = nullptr;
     }
-    if ((st = upload_batch<T>(c, 1, pl, aoff, svo, nullptr, leaf_data != nullptr))) return st;
+    if ((st = upload_batch<T>(c, 1, pl, aoff, svo, leaf_data != nullptr))) return st;
     CU(c->out_item.ensure(sizeof(float) * 2));
+    CU(cudaMemsetAsync(c->misc.p, 0, 64, c->stream));
     const int smem = max_stream_smem_bytes();
     for (auto& lr : c->level_ranges) {
       k_level<T><<<(unsigned)lr.second, kThreads, smem, c->stream>>>(
           reinterpret_cast<const ItemDev<T>*>(c->items.p), reinterpret_cast<const Group*>(c->groups.p), c->n_groups,
-          lr.first, reinterpret_cast<float*>(c->out_item.p));
+          lr.first, reinterpret_cast<float*>(c->out_item.p), nullptr,
+          reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16));
       CU(cudaGetLastError());
     }
   }
   CU(cudaStreamSynchronize(c->stream));
+  if (mode != TB_MODE_PLAIN) {
+    int err = 0;
+    CU(cudaMemcpy(&err, reinterpret_cast<char*>(c->misc.p) + 16, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
+  }
   return TB_OK;
+}
+
+// Device layout (fused form) -> reported layout of tensor id, on the host.
+static std::vector<float> to_reported(const PlanHost& h, int id, const std::vector<float>& v) {
+  const auto& from = h.flabels[id];
+  const auto& to = h.labels[id];
+  if (from == to) return v;
+  std::vector<int> pos(to.size());
+  for (size_t q = 0; q < to.size(); q++)
+    for (size_t r = 0; r < from.size(); r++)
+      if (from[r] == to[q]) pos[q] = (int)r;
+  std::vector<float> out(v.size());
+  for (size_t e = 0; e < v.size(); e++) {
+    size_t x = 0;
+    for (size_t q = 0; q < to.size(); q++) x |= ((e >> q) & 1) << pos[q];
+    out[e] = v[x];
+  }
+  return out;
 }
 
 extern "C" {
@@ -926,13 +969,16 @@ tb_status tb_dump_intermediates(tb_ctx* c, tb_plan* p, const int8_t* slice_vals,
     if (!node_out[j]) continue;
     int id = h.n_tensors + j;
     size_t n = (size_t)1 << h.labels[id].size();
+    std::vector<float> v(n);
     if (c->opt.dtype == TB_DTYPE_F32) {
-      CU(cudaMemcpy(node_out[j], reinterpret_cast<float*>(c->arena.p) + h.off[id], n * 4, cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(v.data(), reinterpret_cast<float*>(c->arena.p) + h.off[id], n * 4, cudaMemcpyDeviceToHost));
     } else {
       std::vector<int32_t> iv(n);
       CU(cudaMemcpy(iv.data(), reinterpret_cast<int32_t*>(c->arena.p) + h.off[id], n * 4, cudaMemcpyDeviceToHost));
-      for (size_t k = 0; k < n; k++) node_out[j][k] = iv[k] <= TB_I32_NEG / 2 ? -INFINITY : (float)iv[k];
+      for (size_t k = 0; k < n; k++) v[k] = iv[k] <= TB_I32_NEG / 2 ? -INFINITY : (float)iv[k];
     }
+    if (mode != TB_MODE_PLAIN) v = to_reported(h, id, v);
+    std::memcpy(node_out[j], v.data(), n * 4);
   }
   return TB_OK;
 }
@@ -977,13 +1023,14 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
                                      const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
                                      const int32_t* children, const int32_t* node_iy_off,
                                      const int32_t* node_iy_lab, int32_t n_sliced, const int32_t* sliced,
-                                     void** blob, int64_t* blob_bytes, char* err, int32_t err_cap) {
+                                     int32_t gemm_min, void** blob, int64_t* blob_bytes, char* err,
+                                     int32_t err_cap) {
   PlanInput in;
   in.n_labels = n_labels; in.n_tensors = n_tensors; in.ix_off = ix_off; in.ix_lab = ix_lab;
   in.n_iy = n_iy; in.iy = iy; in.n_nodes = n_nodes; in.children = children;
   in.node_iy_off = node_iy_off; in.node_iy_lab = node_iy_lab; in.n_sliced = n_sliced; in.sliced = sliced;
   PlanHost h;
-  std::string e = compile_plan(in, h, 0);
+  std::string e = compile_plan(in, h, gemm_min);
   if (!e.empty()) {
     if (err && err_cap > 0) {
       std::strncpy(err, e.c_str(), err_cap - 1);
@@ -994,22 +1041,31 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
   int64_t total = h.n_tensors + h.n_nodes;
   int64_t nplain = 0;
   for (auto& v : h.plain) nplain += (int64_t)v.size();
+  int64_t nlab = 0;
+  for (int64_t i = 0; i < total; i++) nlab += (int64_t)h.labels[i].size();
   struct PlainRec { int32_t node, kind; TileDesc tile; int64_t a, b, c, M, N, K, batch; };
-  size_t bytes = 8 * 8 + total * 8 + total * 4 + h.steps.size() * sizeof(Step) + h.tiles.size() * sizeof(TileDesc) +
-                 h.leaves.size() * sizeof(LeafDesc) + sizeof(FinalDesc) + nplain * sizeof(PlainRec);
+  size_t bytes = 8 * 9 + total * 8 + total * 4 + nlab * 8 + h.steps.size() * sizeof(Step) +
+                 h.tiles.size() * sizeof(TileDesc) + h.leaves.size() * sizeof(LeafDesc) + sizeof(FinalDesc) +
+                 h.gemms.size() * sizeof(GemmDesc) + nplain * sizeof(PlainRec);
   char* b = (char*)std::malloc(bytes);
   if (!b) return TB_ERR_OOM;
   char* p = b;
-  int64_t hdr[8] = {h.n_tensors, h.n_nodes, (int64_t)h.steps.size(), (int64_t)h.tiles.size(),
-                    (int64_t)h.leaves.size(), h.arena_elems, h.plain_elems, nplain};
+  int64_t hdr[9] = {h.n_tensors, h.n_nodes, (int64_t)h.steps.size(), (int64_t)h.tiles.size(),
+                    (int64_t)h.leaves.size(), h.arena_elems, h.plain_elems, nplain, (int64_t)h.gemms.size()};
   std::memcpy(p, hdr, sizeof(hdr)); p += sizeof(hdr);
   std::memcpy(p, h.off.data(), total * 8); p += total * 8;
   for (int64_t i = 0; i < total; i++) { int32_t r = (int32_t)h.labels[i].size(); std::memcpy(p, &r, 4); p += 4; }
+  for (int64_t i = 0; i < total; i++) {
+    std::memcpy(p, h.labels[i].data(), h.labels[i].size() * 4); p += h.labels[i].size() * 4;
+    std::memcpy(p, h.flabels[i].data(), h.flabels[i].size() * 4); p += h.flabels[i].size() * 4;
+  }
   std::memcpy(p, h.steps.data(), h.steps.size() * sizeof(Step)); p += h.steps.size() * sizeof(Step);
   if (!h.tiles.empty()) std::memcpy(p, h.tiles.data(), h.tiles.size() * sizeof(TileDesc));
   p += h.tiles.size() * sizeof(TileDesc);
   std::memcpy(p, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)); p += h.leaves.size() * sizeof(LeafDesc);
   std::memcpy(p, &h.fin, sizeof(FinalDesc)); p += sizeof(FinalDesc);
+  if (!h.gemms.empty()) std::memcpy(p, h.gemms.data(), h.gemms.size() * sizeof(GemmDesc));
+  p += h.gemms.size() * sizeof(GemmDesc);
   for (int j = 0; j < h.n_nodes; j++)
     for (const PlainOp& op : h.plain[j]) {
       PlainRec rec;

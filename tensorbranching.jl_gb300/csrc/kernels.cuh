@@ -366,13 +366,51 @@ struct K1Cfg {
   static constexpr int SMEM_BYTES = 2 * (A_WORDS + B_WORDS) * (int)sizeof(T);
 };
 
+// Thread layout of the 256-thread GEMM tiles: 8 warps as 2 (m) x 4 (n), each
+// warp 8 (m) x 4 (n) lanes, each thread a TM x TN register tile split in two
+// halves per dimension.  A warp reads 8 m-groups and 4 n-groups per k pair,
+// which keeps shared-memory traffic near 96 B/clk/SM at full issue rate.
 template <int TM, int BM>
-__device__ __forceinline__ int k1_row(int tm, int i) {
-  if (TM >= 4) {
-    constexpr int H = TM / 2;
-    return i < H ? tm * H + i : BM / 2 + tm * H + (i - H);
+__device__ __forceinline__ int gm_row(int wm, int lm, int i) {
+  constexpr int H = TM >= 2 ? TM / 2 : 1;
+  return wm * (BM / 2) + (i / H) * (BM / 4) + lm * H + (i % H);
+}
+template <int TN, int BN>
+__device__ __forceinline__ int gm_col(int wn, int ln, int j) {
+  constexpr int H = TN >= 2 ? TN / 2 : 1;
+  return wn * (BN / 4) + (j / H) * (BN / 8) + ln * H + (j % H);
+}
+
+// One k-pair step of the register tile: shared tiles hold [kp][x][2].
+template <typename T, int TM, int TN, int BM, int BN>
+__device__ __forceinline__ void mp_step(const T* __restrict__ as, const T* __restrict__ bs, int kp, int wm,
+                                        int wn, int lm, int ln, T (&acc)[TM][TN]) {
+  uint64_t a2[TM], b2[TN];
+#pragma unroll
+  for (int i = 0; i < TM; i++)
+    a2[i] = *reinterpret_cast<const uint64_t*>(as + (kp * BM + gm_row<TM, BM>(wm, lm, i)) * 2);
+#pragma unroll
+  for (int j = 0; j < TN; j++)
+    b2[j] = *reinterpret_cast<const uint64_t*>(bs + (kp * BN + gm_col<TN, BN>(wn, ln, j)) * 2);
+  if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+      for (int j = 0; j < TN; j++) {
+        uint64_t s2 = add2(a2[i], b2[j]);
+        acc[i][j] = max3(acc[i][j], lo32(s2), hi32(s2));
+      }
+  } else {
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+      for (int j = 0; j < TN; j++) {
+        int32_t x0 = (int32_t)(uint32_t)a2[i], x1 = (int32_t)(uint32_t)(a2[i] >> 32);
+        int32_t y0 = (int32_t)(uint32_t)b2[j], y1 = (int32_t)(uint32_t)(b2[j] >> 32);
+        T v = Trop<T>::mac(acc[i][j], (T)x0, (T)y0);
+        acc[i][j] = Trop<T>::mac(v, (T)x1, (T)y1);
+      }
   }
-  return tm * TM + i;
 }
 
 template <typename T, int BM, int BN>
@@ -392,7 +430,8 @@ __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T*
   const T* Ab = A + bat * (int64_t)M * K;
   const T* Bb = B + bat * (int64_t)K * N;
   T* Cb = C + bat * (int64_t)M * N;
-  const int tm = t & 15, tn = t >> 4;
+  const int warp = t >> 5, lane = t & 31;
+  const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
 
   // global -> register staging
   constexpr int A_GROUPS = (BM / 4) * (BK / 2);  // (4 m) x (k pair) groups
@@ -466,34 +505,7 @@ __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T*
     const T* as = As + buf * Cfg::A_WORDS;
     const T* bs = Bs + buf * Cfg::B_WORDS;
 #pragma unroll
-    for (int kp = 0; kp < BK / 2; kp++) {
-      uint64_t a2[TM], b2[TN];
-#pragma unroll
-      for (int i = 0; i < TM; i++)
-        a2[i] = *reinterpret_cast<const uint64_t*>(as + (kp * BM + k1_row<TM, BM>(tm, i)) * 2);
-#pragma unroll
-      for (int j = 0; j < TN; j++)
-        b2[j] = *reinterpret_cast<const uint64_t*>(bs + (kp * BN + k1_row<TN, BN>(tn, j)) * 2);
-      if constexpr (sizeof(T) == 4 && std::is_same<T, float>::value) {
-#pragma unroll
-        for (int i = 0; i < TM; i++)
-#pragma unroll
-          for (int j = 0; j < TN; j++) {
-            uint64_t s2 = add2(a2[i], b2[j]);
-            acc[i][j] = max3(acc[i][j], lo32(s2), hi32(s2));
-          }
-      } else {
-#pragma unroll
-        for (int i = 0; i < TM; i++)
-#pragma unroll
-          for (int j = 0; j < TN; j++) {
-            int32_t x0 = (int32_t)(uint32_t)a2[i], x1 = (int32_t)(uint32_t)(a2[i] >> 32);
-            int32_t y0 = (int32_t)(uint32_t)b2[j], y1 = (int32_t)(uint32_t)(b2[j] >> 32);
-            T v = Trop<T>::mac(acc[i][j], (T)x0, (T)y0);
-            acc[i][j] = Trop<T>::mac(v, (T)x1, (T)y1);
-          }
-      }
-    }
+    for (int kp = 0; kp < BK / 2; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
     if (kt + 1 < nk) {
       sstore(buf ^ 1);
     }
@@ -502,13 +514,179 @@ __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T*
   // store
 #pragma unroll
   for (int j = 0; j < TN; j++) {
-    int n = n0 + k1_row<TN, BN>(tn, j);
+    int n = n0 + gm_col<TN, BN>(wn, ln, j);
 #pragma unroll
     for (int i = 0; i < TM; i++) {
-      int m = m0 + k1_row<TM, BM>(tm, i);
+      int m = m0 + gm_row<TM, BM>(wm, lm, i);
       Cb[(int64_t)n * M + m] = acc[i][j];
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// fused GEMM tile: k-pair interleaved operands staged by bulk async copies
+// ---------------------------------------------------------------------------
+constexpr int kGemmStages = 3;
+constexpr int kGemmBK = 16;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on one phase of an mbarrier: false when the limit is reached.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 22); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+template <int BM, int BN>
+struct GemmSmem {
+  static constexpr int KP = kGemmBK / 2;
+  static constexpr int BAR_BYTES = 128;
+  static constexpr int A_STAGE = KP * BM * 2;  // elements
+  static constexpr int B_STAGE = KP * BN * 2;
+  static constexpr int BYTES = BAR_BYTES + kGemmStages * (A_STAGE + B_STAGE) * 4;
+};
+
+// One BM x BN output tile of batch point b.  Returns false after a timed-out
+// wait (err is set; copies in flight are drained with a bounded wait).
+template <typename T, int BM, int BN>
+__device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena, int* __restrict__ smem,
+                          int* err) {
+  using SM = GemmSmem<BM, BN>;
+  constexpr int KP = SM::KP, S = kGemmStages;
+  constexpr int TM = BM / 16, TN = BN / 16;
+  const int t = threadIdx.x;
+  const int M = 1 << d.m_log2, N = 1 << d.n_log2;
+  const int64_t K = int64_t(1) << d.k_log2;
+  const int64_t tiles_m = M / BM, tiles_mn = tiles_m * (N / BN);
+  const int64_t b = tile / tiles_mn, mn = tile % tiles_mn;
+  const int m0 = (int)(mn % tiles_m) * BM, n0 = (int)(mn / tiles_m) * BN;
+  const T* Ab = arena + d.a_off + b * (int64_t)M * K;
+  const T* Bb = arena + d.b_off + b * (int64_t)N * K;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  T* As = reinterpret_cast<T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES);
+  T* Bs = As + S * SM::A_STAGE;
+  const int nk = (int)(K / kGemmBK);
+
+  __syncthreads();  // the previous user of this shared memory is done
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (t == 0)
+    for (int i = 0; i < S; i++) mbar_init(&bars[i], 1);
+  __syncthreads();
+
+  auto issue = [&](int kc, int slot) {
+    mbar_expect_tx(&bars[slot], (uint32_t)((SM::A_STAGE + SM::B_STAGE) * sizeof(T)));
+    for (int kp = 0; kp < KP; kp++) {
+      const int64_t row = (int64_t)kc * KP + kp;
+      bulk_g2s(As + slot * SM::A_STAGE + kp * BM * 2, Ab + row * 2 * M + 2 * m0, BM * 2 * sizeof(T), &bars[slot]);
+      bulk_g2s(Bs + slot * SM::B_STAGE + kp * BN * 2, Bb + row * 2 * N + 2 * n0, BN * 2 * sizeof(T), &bars[slot]);
+    }
+  };
+  if (t == 0)
+    for (int kc = 0; kc < S - 1 && kc < nk; kc++) issue(kc, kc);
+
+  const int warp = t >> 5, lane = t & 31;
+  const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; i++)
+#pragma unroll
+    for (int j = 0; j < TN; j++) acc[i][j] = Trop<T>::neg();
+
+  int issued = S - 1 < nk ? S - 1 : nk;
+  bool ok = true;
+  for (int kc = 0; kc < nk; kc++) {
+    const int slot = kc % S;
+    if (t == 0 && kc + S - 1 < nk) {
+      issue(kc + S - 1, (kc + S - 1) % S);
+    }
+    if (kc + S - 1 < nk) issued = kc + S;
+    const bool mine = mbar_wait(&bars[slot], (uint32_t)((kc / S) & 1));
+    ok = __syncthreads_and(mine) != 0;
+    if (!ok) break;
+    const T* as = As + slot * SM::A_STAGE;
+    const T* bs = Bs + slot * SM::B_STAGE;
+#pragma unroll
+    for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
+    __syncthreads();  // slot free for the next copy
+  }
+  if (!ok) {
+    if (t == 0) {
+      atomicExch(err, 3 /* TB_ERR_TIMEOUT */);
+      // drain what was issued, bounded, before the shared memory is reused
+      for (int kc = 0; kc < issued; kc++) mbar_wait(&bars[kc % S], (uint32_t)((kc / S) & 1));
+    }
+    __syncthreads();
+    return false;
+  }
+  if (t == 0)
+    for (int i = 0; i < S; i++) mbar_inval(&bars[i]);
+  // epilogue: scatter the tile into C's layout
+  int* scM = reinterpret_cast<int*>(As);
+  int* scN = scM + BM;
+  for (int i = t; i < BM; i += kThreads) {
+    int m = m0 + i, o = 0;
+    for (int q = 0; q < d.m_log2; q++)
+      if ((m >> q) & 1) o += 1 << d.m_pc[q];
+    scM[i] = o;
+  }
+  for (int j = t; j < BN; j += kThreads) {
+    int n = n0 + j, o = 0;
+    for (int q = 0; q < d.n_log2; q++)
+      if ((n >> q) & 1) o += 1 << d.n_pc[q];
+    scN[j] = o;
+  }
+  int64_t cb = d.c_off;
+  for (int q = 0; q < d.bt_log2; q++)
+    if ((b >> q) & 1) cb += int64_t(1) << d.b_pc[q];
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < TM; i++) {
+    const int64_t ro = cb + scM[gm_row<TM, BM>(wm, lm, i)];
+#pragma unroll
+    for (int j = 0; j < TN; j++) arena[ro + scN[gm_col<TN, BN>(wn, ln, j)]] = acc[i][j];
+  }
+  return true;
+}
+
+// Dispatch on the CTA tile shape chosen by the plan compiler.
+template <typename T>
+__device__ __forceinline__ bool gemm_tile_any(const GemmDesc& d, int64_t tile, T* arena, int* smem, int* err) {
+  const int bm = d.bm_log2, bn = d.bn_log2;
+  if (bm == 7 && bn == 7) return gemm_tile<T, 128, 128>(d, tile, arena, smem, err);
+  if (bm == 7 && bn == 6) return gemm_tile<T, 128, 64>(d, tile, arena, smem, err);
+  if (bm == 6 && bn == 7) return gemm_tile<T, 64, 128>(d, tile, arena, smem, err);
+  if (bm == 6 && bn == 6) return gemm_tile<T, 64, 64>(d, tile, arena, smem, err);
+  if (bm >= 5 && bn >= 5) return gemm_tile<T, 32, 32>(d, tile, arena, smem, err);
+  return gemm_tile<T, 16, 16>(d, tile, arena, smem, err);
+}
+
+__host__ __device__ constexpr int gemm_smem_bytes_max() { return GemmSmem<128, 128>::BYTES; }
 
 }  // namespace tb

@@ -167,37 +167,41 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
 }
 
 bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
-               const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
-               int min_log2, GemmDesc& g) {
-  std::vector<int32_t> M, N, K, Bt;
-  for (int32_t x : A) {
-    bool inb = index_of(B, x) >= 0, inc = index_of(C, x) >= 0;
-    if (inb && inc) Bt.push_back(x);
-    else if (inb) K.push_back(x);
-    else if (inc) M.push_back(x);
-    else return false;  // private label: not GEMM-shaped
-  }
-  for (int32_t x : B) {
-    bool ina = index_of(A, x) >= 0, inc = index_of(C, x) >= 0;
-    if (!ina && inc) N.push_back(x);
-    else if (!ina) return false;
-  }
-  if ((int)M.size() < min_log2 || (int)N.size() < min_log2 || (int)K.size() < min_log2) return false;
-  if ((int)M.size() > 30 || (int)N.size() > 30 || (int)K.size() > 30 || (int)Bt.size() > 30) return false;
+               const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off, GemmDesc& g) {
+  // A = [k0, M..., K1..., Bt...], B = [k0, N..., K1..., Bt...]
+  if (A.empty() || B.empty() || A[0] != B[0] || index_of(C, A[0]) >= 0) return false;
+  std::vector<int32_t> M, N, K{A[0]}, Bt;
+  size_t i = 1;
+  while (i < A.size() && index_of(C, A[i]) >= 0 && index_of(B, A[i]) < 0) M.push_back(A[i++]);
+  while (i < A.size() && index_of(C, A[i]) < 0) K.push_back(A[i++]);
+  while (i < A.size() && index_of(C, A[i]) >= 0 && index_of(B, A[i]) >= 0) Bt.push_back(A[i++]);
+  if (i != A.size()) return false;
+  size_t j = 1;
+  while (j < B.size() && index_of(C, B[j]) >= 0 && index_of(A, B[j]) < 0) N.push_back(B[j++]);
+  for (size_t q = 1; q < K.size(); q++, j++)
+    if (j >= B.size() || B[j] != K[q]) return false;
+  for (size_t q = 0; q < Bt.size(); q++, j++)
+    if (j >= B.size() || B[j] != Bt[q]) return false;
+  if (j != B.size()) return false;
+  if (C.size() != M.size() + N.size() + Bt.size()) return false;
+  if (M.size() < 4 || N.size() < 4 || K.size() < 4) return false;
+  if (M.size() > 30 || N.size() > 30 || K.size() > 30 || Bt.size() > 30) return false;
   std::memset(&g, 0xff, sizeof(g));
   g.a_off = a_off; g.b_off = b_off; g.c_off = c_off;
-  g.nm = (int)M.size(); g.nn = (int)N.size(); g.nk = (int)K.size(); g.nbt = (int)Bt.size();
-  g.bm_log2 = std::min(g.nm, 7);
-  g.bn_log2 = std::min(g.nn, 7);
-  g.bk_log2 = std::min(g.nk, 4);
-  g.n_tiles = (int32_t)((int64_t(1) << (g.nm - g.bm_log2)) * (int64_t(1) << (g.nn - g.bn_log2)) *
-                        (int64_t(1) << g.nbt));
-  for (int i = 0; i < g.nm; i++) { g.m_pa[i] = (int8_t)index_of(A, M[i]); g.m_pc[i] = (int8_t)index_of(C, M[i]); }
-  for (int i = 0; i < g.nn; i++) { g.n_pb[i] = (int8_t)index_of(B, N[i]); g.n_pc[i] = (int8_t)index_of(C, N[i]); }
-  for (int i = 0; i < g.nk; i++) { g.k_pa[i] = (int8_t)index_of(A, K[i]); g.k_pb[i] = (int8_t)index_of(B, K[i]); }
-  for (int i = 0; i < g.nbt; i++) {
-    g.b_pa[i] = (int8_t)index_of(A, Bt[i]); g.b_pb[i] = (int8_t)index_of(B, Bt[i]); g.b_pc[i] = (int8_t)index_of(C, Bt[i]);
-  }
+  g.m_log2 = (int)M.size(); g.n_log2 = (int)N.size(); g.k_log2 = (int)K.size(); g.bt_log2 = (int)Bt.size();
+  // CTA tiles the device dispatches: 128x128, 128x64, 64x128, 64x64, 32x32, 16x16
+  int bm = std::min(g.m_log2, 7), bn = std::min(g.n_log2, 7);
+  if (bm < 6 || bn < 6) bm = bn = std::min(std::min(bm, bn), 5);
+  g.bm_log2 = bm;
+  g.bn_log2 = bn;
+  int64_t nt = (int64_t(1) << (g.m_log2 - g.bm_log2)) * (int64_t(1) << (g.n_log2 - g.bn_log2)) *
+               (int64_t(1) << g.bt_log2);
+  if (nt > 0x7fffffffLL) return false;
+  g.n_tiles = (int32_t)nt;
+  g.pad_ = 0;
+  for (size_t q = 0; q < M.size(); q++) g.m_pc[q] = (int8_t)index_of(C, M[q]);
+  for (size_t q = 0; q < N.size(); q++) g.n_pc[q] = (int8_t)index_of(C, N[q]);
+  for (size_t q = 0; q < Bt.size(); q++) g.b_pc[q] = (int8_t)index_of(C, Bt[q]);
   return true;
 }
 
@@ -310,8 +314,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       p.leaf_raw[i].push_back(x);
       if (p.slice_index[x] < 0 && index_of(p.labels[i], x) < 0) p.labels[i].push_back(x);
     }
-    if (p.leaf_raw[i].size() > 2 || p.leaf_raw[i].empty())
-      return "independent-set leaves have one (vertex) or two (edge) labels";
+    if (p.leaf_raw[i].size() > 30) return "leaf tensor of rank above 30";
     for (int32_t x : p.labels[i]) count[x]++;
   }
   for (int32_t x : p.open)
@@ -417,13 +420,86 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       ld.out_bit[k] = -1;
       ld.slice_idx[k] = -1;
     }
-    for (int k = 0; k < ld.nraw; k++) {
+    // MIS leaves have one or two labels; others only take explicit data
+    for (int k = 0; k < ld.nraw && k < 2; k++) {
       int32_t x = p.leaf_raw[i][k];
       ld.out_bit[k] = (int8_t)index_of(p.labels[i], x);
       ld.slice_idx[k] = (int8_t)p.slice_index[x];
     }
     ld.w = 0.0f;
     p.leaves.push_back(ld);
+  }
+  // fused-form layouts, parents first: a GEMM-shaped node asks for its
+  // operands in the k-pair interleaved layouts; any other node asks for its
+  // operands ordered like its own output (shared labels first, in C order).
+  p.flabels = p.labels;
+  const int gmin = gemm_min_log2;
+  std::vector<char> gemm_node(in.n_nodes, 0);
+  auto loose = [&](int id) {
+    // labels of tensor id that its own node keeps from exactly one operand
+    std::vector<int32_t> out;
+    if (id < T) return out;
+    int jj = id - T, x = p.children[2 * jj], y = p.children[2 * jj + 1];
+    for (int32_t l : p.labels[id]) {
+      bool inx = index_of(p.labels[x], l) >= 0, iny = index_of(p.labels[y], l) >= 0;
+      if (inx != iny) out.push_back(l);
+    }
+    return out;
+  };
+  for (int j = in.n_nodes - 1; j >= 0; j--) {
+    int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+    const std::vector<int32_t>& C = p.flabels[me];
+    const std::vector<int32_t>& SA = p.labels[a];
+    const std::vector<int32_t>& SB = p.labels[b];
+    std::vector<int32_t> M, N, K, Bt;
+    bool priv = false;
+    for (int32_t l : SA) {
+      bool inb = index_of(SB, l) >= 0, inc = index_of(C, l) >= 0;
+      if (inb && inc) Bt.push_back(l);
+      else if (inb) K.push_back(l);
+      else if (inc) M.push_back(l);
+      else priv = true;
+    }
+    for (int32_t l : SB) {
+      bool ina = index_of(SA, l) >= 0, inc = index_of(C, l) >= 0;
+      if (!ina && inc) N.push_back(l);
+      else if (!ina) priv = true;
+    }
+    bool gemm = gmin > 0 && !priv && a >= T && b >= T && (int)M.size() >= gmin && (int)N.size() >= gmin &&
+                (int)K.size() >= gmin;
+    auto by_c = [&](std::vector<int32_t>& v, const std::vector<int32_t>& pref) {
+      std::stable_sort(v.begin(), v.end(), [&](int32_t x, int32_t y) {
+        bool px = index_of(pref, x) >= 0, py = index_of(pref, y) >= 0;
+        if (px != py) return px;
+        int cx = index_of(C, x), cy = index_of(C, y);
+        if (cx < 0) cx = 1 << 20;
+        if (cy < 0) cy = 1 << 20;
+        return cx < cy;
+      });
+    };
+    if (gemm) {
+      gemm_node[j] = 1;
+      std::vector<int32_t> la = loose(a), lb = loose(b), none;
+      by_c(M, la);
+      by_c(N, lb);
+      by_c(Bt, none);
+      std::vector<int32_t> fa{K[0]}, fb{K[0]};
+      fa.insert(fa.end(), M.begin(), M.end());
+      fb.insert(fb.end(), N.begin(), N.end());
+      fa.insert(fa.end(), K.begin() + 1, K.end());
+      fb.insert(fb.end(), K.begin() + 1, K.end());
+      fa.insert(fa.end(), Bt.begin(), Bt.end());
+      fb.insert(fb.end(), Bt.begin(), Bt.end());
+      p.flabels[a] = fa;
+      p.flabels[b] = fb;
+    } else {
+      for (int c : {a, b}) {
+        if (c < T) continue;  // leaves keep their natural layout
+        std::vector<int32_t> v = p.labels[c], none;
+        by_c(v, none);
+        p.flabels[c] = v;
+      }
+    }
   }
   // fused steps: 0 = leaves, 1..n = nodes, last = final
   p.steps.clear();
@@ -438,15 +514,15 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
     int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
     Step st{};
     GemmDesc g;
-    if (gemm_min_log2 > 0 &&
-        plan_gemm(p.labels[a], p.labels[b], p.labels[me], p.off[a], p.off[b], p.off[me], gemm_min_log2, g)) {
+    if (gemm_node[j] &&
+        plan_gemm(p.flabels[a], p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], g)) {
       st.kind = STEP_GEMM;
       st.desc = (int32_t)p.gemms.size();
       st.n_tiles = g.n_tiles;
       p.gemms.push_back(g);
     } else {
       TileDesc d;
-      if (!(e = plan_tile(p.labels[a], &p.labels[b], p.labels[me], p.off[a], p.off[b], p.off[me], d)).empty())
+      if (!(e = plan_tile(p.flabels[a], &p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], d)).empty())
         return "node " + std::to_string(j) + ": " + e;
       st.kind = STEP_TILE;
       st.desc = (int32_t)p.tiles.size();

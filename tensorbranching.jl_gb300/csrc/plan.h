@@ -38,7 +38,8 @@ struct PlanInput {
 struct PlanHost {
   int32_t n_labels = 0, n_tensors = 0, n_nodes = 0;
   std::vector<std::vector<int32_t>> leaf_raw;  // raw labels of each leaf
-  std::vector<std::vector<int32_t>> labels;    // stored labels of tensor id (leaves, then nodes)
+  std::vector<std::vector<int32_t>> labels;    // reported labels of tensor id (leaves, then nodes)
+  std::vector<std::vector<int32_t>> flabels;   // device layout of tensor id in the fused form
   std::vector<int64_t> off;                    // arena offset of tensor id
   std::vector<int32_t> children;
   std::vector<int32_t> open;                   // open labels, output order
@@ -69,10 +70,9 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
                       const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
                       TileDesc& d, int out_bits_target = 9);
 
-// Plan a gather GEMM for node (A, B -> C) if its M, N, K are all at least
-// 2^min_log2; returns false when the node is not GEMM-shaped.
+// GEMM descriptor for node (A, B -> C) whose operands are already in the
+// k-pair interleaved layouts; returns false if they are not.
 bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
-               const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off,
-               int min_log2, GemmDesc& g);
+               const std::vector<int32_t>& C, int64_t a_off, int64_t b_off, int64_t c_off, GemmDesc& g);
 
 }  // namespace tb

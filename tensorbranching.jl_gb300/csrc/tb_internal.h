@@ -43,19 +43,20 @@ struct TileDesc {
   int8_t tr_a[kMaxTileBits], tr_b[kMaxTileBits];          // Tr bit -> A / B tile bit (-1)
 };
 
-// Register-blocked gather GEMM for a contraction node with large M, N, K:
-//   C[m, n, b] = max_k A[m, k, b] + B[k, n, b]
-// where m, n, k, b are assignments of label groups that sit at arbitrary
-// bit positions of A, B and C.  Tile: BM x BN outputs per CTA, BK per stage.
+// Register-blocked GEMM for a contraction node with large M, N and K label
+// groups.  The plan compiler lays the operands out "k-pair interleaved":
+//   A[(k & 1) + 2 m + 2 M (k >> 1) + M K b]    labels [k0, M..., K1..., batch...]
+//   B[(k & 1) + 2 n + 2 N (k >> 1) + N K b]    labels [k0, N..., K1..., batch...]
+// so each CTA stage is a set of contiguous rows (bulk async copies) and one
+// 64-bit shared load yields (x[k], x[k+1]) for a packed f32x2 add.  The
+// output C[m, n, b] is scattered to C's own layout through m_pc / n_pc / b_pc.
 struct GemmDesc {
   int64_t a_off, b_off, c_off;
-  int32_t nm, nn, nk, nbt;          // label counts of M, N, K, batch
-  int32_t bm_log2, bn_log2, bk_log2;  // CTA tile
-  int32_t n_tiles;                  // (M/BM) * (N/BN) * batch
-  int8_t m_pa[kMaxBits], m_pc[kMaxBits];   // M label i -> position in A, C
-  int8_t n_pb[kMaxBits], n_pc[kMaxBits];   // N label i -> position in B, C
-  int8_t k_pa[kMaxBits], k_pb[kMaxBits];   // K label i -> position in A, B
-  int8_t b_pa[kMaxBits], b_pb[kMaxBits], b_pc[kMaxBits];
+  int32_t m_log2, n_log2, k_log2, bt_log2;
+  int32_t bm_log2, bn_log2;  // CTA tile BM x BN
+  int32_t n_tiles;           // (M / BM) (N / BN) 2^bt
+  int32_t pad_;
+  int8_t m_pc[32], n_pc[32], b_pc[32];  // C position of m / n / batch bit i
 };
 
 // One leaf tensor of the MIS network (GenericTensorNetworks IndependentSet):

@@ -49,6 +49,13 @@ class FinalDesc(ctypes.Structure):
     _fields_ = [("root_off", c_int64), ("root_log2", c_int32), ("pad_", c_int32)]
 
 
+class GemmDesc(ctypes.Structure):
+    _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64),
+                ("m_log2", c_int32), ("n_log2", c_int32), ("k_log2", c_int32), ("bt_log2", c_int32),
+                ("bm_log2", c_int32), ("bn_log2", c_int32), ("n_tiles", c_int32), ("pad_", c_int32),
+                ("m_pc", c_int8 * 32), ("n_pc", c_int8 * 32), ("b_pc", c_int8 * 32)]
+
+
 class PlainRec(ctypes.Structure):
     _fields_ = [("node", c_int32), ("kind", c_int32), ("tile", TileDesc), ("a", c_int64), ("b", c_int64),
                 ("c", c_int64), ("M", c_int64), ("N", c_int64), ("K", c_int64), ("batch", c_int64)]
@@ -61,14 +68,15 @@ PLAIN_TILE, PLAIN_GEMM = 1, 2
 def check_layout(lib):
     out = (c_int32 * 6)()
     lib.tbi_sizes(out, 6)
-    want = [ctypes.sizeof(TileDesc), ctypes.sizeof(Step), ctypes.sizeof(LeafDesc), ctypes.sizeof(FinalDesc)]
-    assert list(out)[:4] == want, (list(out), want)
+    want = [ctypes.sizeof(TileDesc), ctypes.sizeof(Step), ctypes.sizeof(LeafDesc), ctypes.sizeof(FinalDesc),
+            ctypes.sizeof(GemmDesc)]
+    assert list(out)[:5] == want, (list(out), want)
 
 
-def describe(lib, code, sliced=(), use_node_iy=False):
+def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4):
     lib.tbi_plan_describe.restype = c_int32
     lib.tbi_plan_describe.argtypes = [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p,
-                                      c_void_p, c_void_p, c_int32, c_void_p, ctypes.POINTER(c_void_p),
+                                      c_void_p, c_void_p, c_int32, c_void_p, c_int32, ctypes.POINTER(c_void_p),
                                       ctypes.POINTER(c_int64), ctypes.c_char_p, c_int32]
     lib.tbi_free.argtypes = [c_void_p]
     lib.tbi_sizes.argtypes = [c_void_p, c_int32]
@@ -85,17 +93,22 @@ def describe(lib, code, sliced=(), use_node_iy=False):
                                iy.ctypes.data, code.n_nodes, ch.ctypes.data,
                                None if noff is None else noff.ctypes.data,
                                None if nlab is None else nlab.ctypes.data, len(sliced), sl.ctypes.data,
-                               ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
+                               gemm_min, ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
     if rc:
         raise ValueError(err.value.decode())
     raw = ctypes.string_at(blob, nbytes.value)
     lib.tbi_free(blob)
     p = 0
-    hdr = np.frombuffer(raw, np.int64, 8, p); p += 64
-    n_tensors, n_nodes, n_steps, n_tiles, n_leaves, arena, plain_elems, nplain = [int(x) for x in hdr]
+    hdr = np.frombuffer(raw, np.int64, 9, p); p += 72
+    n_tensors, n_nodes, n_steps, n_tiles, n_leaves, arena, plain_elems, nplain, ngemm = [int(x) for x in hdr]
     total = n_tensors + n_nodes
     offs = np.frombuffer(raw, np.int64, total, p).copy(); p += 8 * total
     ranks = np.frombuffer(raw, np.int32, total, p).copy(); p += 4 * total
+    labels, flabels = [], []
+    for i in range(total):
+        r = int(ranks[i])
+        labels.append(np.frombuffer(raw, np.int32, r, p).tolist()); p += 4 * r
+        flabels.append(np.frombuffer(raw, np.int32, r, p).tolist()); p += 4 * r
 
     def take(cls, n):
         nonlocal p
@@ -109,10 +122,12 @@ def describe(lib, code, sliced=(), use_node_iy=False):
     tiles = take(TileDesc, n_tiles)
     leaves = take(LeafDesc, n_leaves)
     fin = take(FinalDesc, 1)[0]
+    gemms = take(GemmDesc, ngemm)
     plain = take(PlainRec, nplain)
     assert p == len(raw)
     return dict(n_tensors=n_tensors, n_nodes=n_nodes, steps=steps, tiles=tiles, leaves=leaves, fin=fin,
-                plain=plain, off=offs, rank=ranks, arena=arena, plain_elems=plain_elems)
+                plain=plain, off=offs, rank=ranks, arena=arena, plain_elems=plain_elems, gemms=gemms,
+                labels=labels, flabels=flabels)
 
 
 def swz(j):
@@ -241,6 +256,10 @@ def emu_stream_tile(d, arena, written, expect=None):
 
             As = load(la, d.na, d.pa, ldA, a_lo, a_hi)
             Bs = load(lb, d.nb, d.pb, ldB, b_lo, b_hi) if hasB else None
+            act_idx = np.nonzero(act)[0]
+            step = 1 << split
+            nq = ntr // step
+            rmat = s[act_idx][:, None] + step * np.arange(nq)[None, :]  # reductions per thread
             for i in range(opt):
                 xa = np.zeros(KTHREADS, np.int64)
                 xb = np.zeros(KTHREADS, np.int64)
@@ -250,31 +269,28 @@ def emu_stream_tile(d, arena, written, expect=None):
                             xa |= 1 << d.tc_a[b]
                         if d.tc_b[b] >= 0:
                             xb |= 1 << d.tc_b[b]
-                ia = iat ^ swz(xa)
-                ib = ibt ^ swz(xb)
-                for tt in np.nonzero(act)[0]:
-                    rr = np.arange(s[tt], ntr, 1 << split)
-                    idxa = ia[tt] ^ IAr[rr]
-                    assert idxa.size == 0 or idxa.max() < NA
-                    v = As[idxa]
-                    if hasB:
-                        idxb = ib[tt] ^ IBr[rr]
-                        assert idxb.size == 0 or idxb.max() < NB
-                        v = v + Bs[idxb]
-                    if v.size:
-                        acc[tt, i] = max(acc[tt, i], v.max())
+                ia = (iat ^ swz(xa))[act_idx]
+                ib = (ibt ^ swz(xb))[act_idx]
+                idxa = ia[:, None] ^ IAr[rmat]
+                assert idxa.max() < NA and idxa.min() >= 0
+                v = As[idxa]
+                if hasB:
+                    idxb = ib[:, None] ^ IBr[rmat]
+                    assert idxb.max() < NB and idxb.min() >= 0
+                    v = v + Bs[idxb]
+                acc[act_idx, i] = np.maximum(acc[act_idx, i], v.max(axis=1))
         if split > 0:
             red = acc[:, 0].copy()
             for tt in np.nonzero(act & (s == 0))[0]:
                 acc[tt, 0] = max(red[cl[tt] + (s2 << lo_bits)] for s2 in range(1 << split))
         cmask = (1 << d.pc) - 1
-        for tt in np.nonzero(act & (s == 0))[0]:
-            for i in range(opt):
-                c = cl[tt] + (i << lo_bits)
-                g = oc + (c & cmask) + stC[c >> d.pc]
-                assert c_lo <= g < c_hi, "store out of bounds"
-                written[g] += 1
-                arena[g] = acc[tt, i]
+        wr = np.nonzero(act & (s == 0))[0]
+        for i in range(opt):
+            c = cl[wr] + (i << lo_bits)
+            g = oc + (c & cmask) + stC[c >> d.pc]
+            assert g.min() >= c_lo and g.max() < c_hi, "store out of bounds"
+            np.add.at(written, g, 1)
+            arena[g] = acc[wr, i]
     return (c_lo, c_hi)
 
 
@@ -310,6 +326,52 @@ def emu_gemm(rec, arena):
     arena[rec.c:rec.c + M * N * B] = C.reshape(-1)
 
 
+GEMM_TILES = {(7, 7), (7, 6), (6, 7), (6, 6), (5, 5), (4, 4)}
+
+
+def emu_gemm_step(g, arena, written):
+    """Fused GEMM tile: k-pair interleaved operands, scatter store to C."""
+    assert (g.bm_log2, g.bn_log2) in GEMM_TILES
+    assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 4
+    M, N, K, Bt = 1 << g.m_log2, 1 << g.n_log2, 1 << g.k_log2, 1 << g.bt_log2
+    assert g.n_tiles == (M >> g.bm_log2) * (N >> g.bn_log2) * Bt
+    rc = tensor_rank([g.m_pc[i] for i in range(g.m_log2)] + [g.n_pc[i] for i in range(g.n_log2)] +
+                     [g.b_pc[i] for i in range(g.bt_log2)], [], [])
+    for x, n in ((g.a_off, M * K * Bt), (g.b_off, N * K * Bt), (g.c_off, 1 << rc)):
+        assert 0 <= x and x + n <= arena.size and x % 32 == 0
+    # bulk copies: rows of 2*BM (2*BN) elements at 2*m0 within a k-pair row
+    BM, BN = 1 << g.bm_log2, 1 << g.bn_log2
+    assert (2 * BM * 4) % 16 == 0 and (2 * BN * 4) % 16 == 0
+    A = arena[g.a_off:g.a_off + M * K * Bt].reshape(Bt, K // 2, M, 2)   # [b][kp][m][k&1]
+    B = arena[g.b_off:g.b_off + N * K * Bt].reshape(Bt, K // 2, N, 2)
+    A = A.transpose(0, 1, 3, 2).reshape(Bt, K, M)
+    B = B.transpose(0, 1, 3, 2).reshape(Bt, K, N)
+    C = (A[:, :, None, :] + B[:, :, :, None]).max(axis=1)  # (Bt, N, M)
+    def scat(nbits, pos):
+        idx = np.arange(1 << nbits)
+        out = np.zeros(1 << nbits, np.int64)
+        for q in range(nbits):
+            out |= ((idx >> q) & 1) << pos[q]
+        return out
+    sm = scat(g.m_log2, g.m_pc)
+    sn = scat(g.n_log2, g.n_pc)
+    sb = scat(g.bt_log2, g.b_pc)
+    addr = g.c_off + sb[:, None, None] + sn[None, :, None] + sm[None, None, :]
+    arena[addr.ravel()] = C.ravel()
+    np.add.at(written, addr.ravel(), 1)
+
+
+def to_reported(v, flab, lab):
+    if flab == lab:
+        return v
+    pos = [flab.index(x) for x in lab]
+    e = np.arange(v.size)
+    x = np.zeros(v.size, np.int64)
+    for q, pq in enumerate(pos):
+        x |= ((e >> q) & 1) << pq
+    return v[x]
+
+
 def run_fused(desc, weights, slice_vals=()):
     """Replay the fused program; returns (root tensor, arena, node views)."""
     arena = np.full(desc["arena"], np.nan, np.float32)
@@ -335,6 +397,8 @@ def run_fused(desc, weights, slice_vals=()):
                 node_of_step[si] = j
                 j += 1
             emu_stream_tile(d, arena, written)
+        elif st.kind == STEP_GEMM:
+            emu_gemm_step(desc["gemms"][st.desc], arena, written)
     fin = desc["fin"]
     root = arena[fin.root_off:fin.root_off + (1 << fin.root_log2)].copy()
     assert np.all(written[fin.root_off:fin.root_off + (1 << fin.root_log2)] == 1), "root not written exactly once"
@@ -342,7 +406,8 @@ def run_fused(desc, weights, slice_vals=()):
     for idx in range(T, T + desc["n_nodes"]):
         seg = written[off[idx]:off[idx] + (1 << rank[idx])]
         assert np.all(seg == 1), f"tensor {idx} elements written {np.unique(seg)} times"
-    nodes = [arena[off[T + k]:off[T + k] + (1 << rank[T + k])].copy() for k in range(desc["n_nodes"])]
+    nodes = [to_reported(arena[off[T + k]:off[T + k] + (1 << rank[T + k])].copy(), desc["flabels"][T + k],
+                         desc["labels"][T + k]) for k in range(desc["n_nodes"])]
     return root, nodes
 
 

@@ -87,3 +87,17 @@ def test_invalid_plans_rejected(tb, lib):
     with pytest.raises(ValueError):
         emulate.describe(lib, tb.CompressedEinsum(code.ixs, [], code.children, node_iy=labs,
                                                   n_labels=code.n_labels), use_node_iy=True)
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 4, 1), (5, 4, 6, 2), (6, 6, 4, 0), (7, 5, 4, 1)])
+def test_gemm_steps(tb, orc, lib, shape):
+    from cases import gemm_case
+
+    g, w, code = gemm_case(tb, *shape)
+    d = emulate.describe(lib, code)
+    assert [s.kind for s in d["steps"]].count(emulate.STEP_GEMM) == 1
+    root, nodes = emulate.run_fused(d, w)
+    ref, dumps = orc.execute(code, w, dump=True)
+    assert np.array_equal(root, ref)
+    for a, b in zip(nodes, dumps):
+        assert np.array_equal(a, b)

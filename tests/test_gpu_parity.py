@@ -109,3 +109,21 @@ def test_contract_generic_tensors(tb, orc, engine):
         for mode in ("plain", "layered"):
             got = engine.contract(plan, data, mode=mode)
             assert np.array_equal(got, ref), (it, mode)
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 4, 1), (5, 4, 6, 2), (6, 6, 4, 0), (7, 5, 4, 1), (7, 7, 6, 2),
+                                   (8, 7, 5, 1)])
+def test_fused_gemm_nodes(tb, orc, engine, shape):
+    from cases import gemm_case
+
+    g, w, code = gemm_case(tb, *shape)
+    plan = engine.plan(code, w)
+    labs = plan.all_node_labels()
+    ref, dumps = orc.execute(code, w, node_iy=labs, dump=True)
+    for mode in MODES:
+        _, mx = engine.solve_batch([plan], mode=mode)
+        assert mx == np.max(ref), mode
+    for mode in ("layered", "plain"):
+        got = engine.dump(plan, mode=mode)
+        for a, b in zip(got, dumps):
+            assert np.array_equal(a, b), mode
