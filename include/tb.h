@@ -187,7 +187,8 @@ tb_status tb_last_timing(const tb_ctx* ctx, double* device_ms, int64_t* launches
 /*
  * Standalone batched tropical GEMM (the K1 kernel), device pointers:
  *   C[m + M n + M N b] = max_k A[m + M k + M K b] + B[k + K n + K N b]
- * for b < batch.  M, N, K >= 1.  `stream` is a cudaStream_t (NULL: default).
+ * for b < batch; M, N, K powers of two >= 16.  `stream` is a cudaStream_t
+ * (NULL: the default stream); the call only enqueues the kernel.
  * Uses the dtype of ctx.  Exposed for benchmarking the kernel at dense
  * square shapes.
  */

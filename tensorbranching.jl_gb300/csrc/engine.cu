@@ -62,13 +62,18 @@ __global__ void __launch_bounds__(kThreads) k_reduce_max(const float* v, int n, 
   }
 }
 
-template <typename T>
+// KINDS: 1 = leaves / stream tiles / final, 2 = GEMM tiles, 3 = both.
+template <typename T, int KINDS = 3>
 __device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, int64_t tile, int* smem,
                                          float* out_item, const float* r, int item, int* err) {
-  switch (st.kind) {
-    case STEP_GEMM:
+  if constexpr ((KINDS & 2) != 0) {
+    if (st.kind == STEP_GEMM) {
       gemm_tile_any<T>(it.gemms[st.desc], tile, it.arena, smem, err);
-      break;
+      return;
+    }
+  }
+  if constexpr ((KINDS & 1) == 0) return;
+  switch (st.kind) {
     case STEP_LEAVES:
       leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile);
       break;
@@ -94,8 +99,8 @@ __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int
 
 // One launch per tree level: block b runs ticket first_ticket + b.  No
 // waiting: the previous launch on the stream finished every dependency.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
+template <typename T, int KINDS>
+__global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
                                                    int64_t first_ticket, float* out_item, const float* r,
                                                    int* err) {
   extern __shared__ int tb_smem[];
@@ -105,7 +110,7 @@ __global__ void __launch_bounds__(kThreads) k_level(const ItemDev<T>* items, con
   __syncthreads();
   const Group g = groups[s_g];
   const ItemDev<T>& it = items[g.item];
-  run_step<T>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, r, g.item, err);
+  run_step<T, KINDS>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, r, g.item, err);
 }
 
 // Persistent executor.  Tickets are handed out in dependency order, so a
@@ -262,7 +267,11 @@ struct tb_ctx {
   bool have_key = false;
   int64_t n_tickets = 0;
   int n_groups = 0;
-  std::vector<std::pair<int64_t, int64_t>> level_ranges;  // (first ticket, count)
+  struct LevelRange {
+    int64_t first, count;
+    int kinds;  // 1 stream-like, 2 GEMM
+  };
+  std::vector<LevelRange> level_ranges;
   size_t sv_bytes = 0;
   int n_items = 0;
   cudaGraphExec_t gexec = nullptr;
@@ -292,20 +301,25 @@ static size_t elem() { return sizeof(T); }
 
 static size_t dtype_size(const tb_ctx*) { return 4; }
 
-static int max_stream_smem_bytes() {
-  // largest dynamic shared memory a stream tile may ask for (see plan_tile),
-  // or a GEMM tile's staging stages
-  int st = (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4;
-  return st > gemm_smem_bytes_max() ? st : gemm_smem_bytes_max();
+// Dynamic shared memory of the kernels: stream tiles (see plan_tile's
+// limits), GEMM tiles (pipeline stages), or both for the persistent kernel.
+static int stream_smem_bytes() { return (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4; }
+static int smem_bytes(int kinds) {
+  int b = 0;
+  if (kinds & 1) b = std::max(b, stream_smem_bytes());
+  if (kinds & 2) b = std::max(b, gemm_smem_bytes_max());
+  return b;
 }
+static int max_stream_smem_bytes() { return smem_bytes(3); }
 
 template <typename T>
 static tb_status set_kernel_attrs() {
   static bool done = false;
   if (done) return TB_OK;
   int sm = max_stream_smem_bytes();
-  CU(cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-  CU(cudaFuncSetAttribute(k_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CU(cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)));
+  CU(cudaFuncSetAttribute(k_level<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)));
+  CU(cudaFuncSetAttribute(k_level<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2)));
   CU(cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   done = true;
   return TB_OK;
@@ -349,7 +363,7 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
   }
   if (h.n_nodes == 0) {
     const TileDesc& d = h.tiles[0];
-    k_tile<T><<<d.n_tiles, kThreads, stream_smem_words(d) * 4, s>>>(d, arena);
+    k_tile<T><<<d.n_tiles, kThreads, stream_smem_words(d) * 4, s>>>(d, arena);  // within smem_bytes(1)
     CU(cudaGetLastError());
     launches++;
     return TB_OK;
@@ -396,17 +410,18 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     hi[i] = it;
   }
   // groups sorted by (level, item, step)
-  struct GK { int level, item, step; };
+  struct GK { int level, kinds, item, step; };
   std::vector<GK> gk;
   for (int i = 0; i < n; i++) {
     const PlanHost& h = plans[i]->h;
     for (int s = 0; s < (int)h.steps.size(); s++) {
       if (skip_leaves && h.steps[s].kind == STEP_LEAVES) continue;
-      gk.push_back({h.steps[s].level, i, s});
+      gk.push_back({h.steps[s].level, h.steps[s].kind == STEP_GEMM ? 2 : 1, i, s});
     }
   }
   std::stable_sort(gk.begin(), gk.end(), [](const GK& a, const GK& b) {
     if (a.level != b.level) return a.level < b.level;
+    if (a.kinds != b.kinds) return a.kinds < b.kinds;
     if (a.item != b.item) return a.item < b.item;
     return a.step < b.step;
   });
@@ -414,18 +429,19 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   Group* hg = reinterpret_cast<Group*>(c->h_groups.p);
   int64_t tk = 0;
   c->level_ranges.clear();
-  int cur_level = -1;
+  int cur_level = -1, cur_kinds = -1;
   for (size_t g = 0; g < gk.size(); g++) {
     hg[g].item = gk[g].item;
     hg[g].step = gk[g].step;
     hg[g].first = tk;
-    if (gk[g].level != cur_level) {
-      c->level_ranges.push_back({tk, 0});
+    if (gk[g].level != cur_level || gk[g].kinds != cur_kinds) {
+      c->level_ranges.push_back({tk, 0, gk[g].kinds});
       cur_level = gk[g].level;
+      cur_kinds = gk[g].kinds;
     }
     int64_t nt = plans[gk[g].item]->h.steps[gk[g].step].n_tiles;
     tk += nt;
-    c->level_ranges.back().second += nt;
+    c->level_ranges.back().count += nt;
   }
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
@@ -465,11 +481,15 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
     CU(cudaGetLastError());
     launches++;
   } else {
+    int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
     for (auto& lr : c->level_ranges) {
-      if (lr.second > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
-      k_level<T><<<(unsigned)lr.second, kThreads, smem, s>>>(items, groups, c->n_groups, lr.first, out_item, rv,
-                                                             reinterpret_cast<int*>(
-                                                                 reinterpret_cast<char*>(c->misc.p) + 16));
+      if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
+      if (lr.kinds == 2)
+        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), s>>>(items, groups, c->n_groups, lr.first,
+                                                                          out_item, rv, err);
+      else
+        k_level<T, 1><<<(unsigned)lr.count, kThreads, smem_bytes(1), s>>>(items, groups, c->n_groups, lr.first,
+                                                                          out_item, rv, err);
       CU(cudaGetLastError());
       launches++;
     }
@@ -899,11 +919,17 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
     CU(c->out_item.ensure(sizeof(float) * 2));
     CU(cudaMemsetAsync(c->misc.p, 0, 64, c->stream));
     const int smem = max_stream_smem_bytes();
+    int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
+    const ItemDev<T>* items = reinterpret_cast<const ItemDev<T>*>(c->items.p);
+    const Group* groups = reinterpret_cast<const Group*>(c->groups.p);
+    float* oi = reinterpret_cast<float*>(c->out_item.p);
     for (auto& lr : c->level_ranges) {
-      k_level<T><<<(unsigned)lr.second, kThreads, smem, c->stream>>>(
-          reinterpret_cast<const ItemDev<T>*>(c->items.p), reinterpret_cast<const Group*>(c->groups.p), c->n_groups,
-          lr.first, reinterpret_cast<float*>(c->out_item.p), nullptr,
-          reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16));
+      if (lr.kinds == 2)
+        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), c->stream>>>(items, groups, c->n_groups,
+                                                                                  lr.first, oi, nullptr, err);
+      else
+        k_level<T, 1><<<(unsigned)lr.count, kThreads, smem_bytes(1), c->stream>>>(items, groups, c->n_groups,
+                                                                                  lr.first, oi, nullptr, err);
       CU(cudaGetLastError());
     }
   }
@@ -998,7 +1024,7 @@ tb_status tb_gemm_device(tb_ctx* c, int64_t M, int64_t N, int64_t K, int64_t bat
     return fail(TB_ERR_UNSUPPORTED, "K1 takes power-of-two M, N, K >= 16");
   if (M > (1 << 30) || N > (1 << 30) || K > (1 << 30)) return fail(TB_ERR_UNSUPPORTED, "dimension too large");
   CU(cudaSetDevice(c->device));
-  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c->stream;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);  // NULL: the default stream
   if (c->opt.dtype == TB_DTYPE_F32) {
     CU(dispatch_k1<float>((const float*)A, (const float*)B, (float*)C, M, N, K, batch, s));
   } else {

@@ -370,10 +370,18 @@ struct K1Cfg {
 // warp 8 (m) x 4 (n) lanes, each thread a TM x TN register tile split in two
 // halves per dimension.  A warp reads 8 m-groups and 4 n-groups per k pair,
 // which keeps shared-memory traffic near 96 B/clk/SM at full issue rate.
+// Rows of a thread: two halves of H rows; within a half, pairs of rows sit at
+// lm * 2 so the 8 m-lanes of a warp read 8 consecutive 16-byte chunks (one
+// conflict-free wavefront per 128-bit shared load).
 template <int TM, int BM>
 __device__ __forceinline__ int gm_row(int wm, int lm, int i) {
   constexpr int H = TM >= 2 ? TM / 2 : 1;
-  return wm * (BM / 2) + (i / H) * (BM / 4) + lm * H + (i % H);
+  if constexpr (H >= 2) {
+    const int q = i % H;
+    return wm * (BM / 2) + (i / H) * (BM / 4) + (q / 2) * 16 + lm * 2 + (q % 2);
+  } else {
+    return wm * (BM / 2) + (i / H) * (BM / 4) + lm;
+  }
 }
 template <int TN, int BN>
 __device__ __forceinline__ int gm_col(int wn, int ln, int j) {
@@ -381,35 +389,42 @@ __device__ __forceinline__ int gm_col(int wn, int ln, int j) {
   return wn * (BN / 4) + (j / H) * (BN / 8) + ln * H + (j % H);
 }
 
-// One k-pair step of the register tile: shared tiles hold [kp][x][2].
+// One k-pair step of the register tile: shared tiles hold [kp][x][2].  The
+// a-pairs are loaded per half so that at most 64 accumulators + 4 a-pairs +
+// TN b-pairs are live.
 template <typename T, int TM, int TN, int BM, int BN>
 __device__ __forceinline__ void mp_step(const T* __restrict__ as, const T* __restrict__ bs, int kp, int wm,
                                         int wn, int lm, int ln, T (&acc)[TM][TN]) {
-  uint64_t a2[TM], b2[TN];
-#pragma unroll
-  for (int i = 0; i < TM; i++)
-    a2[i] = *reinterpret_cast<const uint64_t*>(as + (kp * BM + gm_row<TM, BM>(wm, lm, i)) * 2);
+  uint64_t b2[TN];
 #pragma unroll
   for (int j = 0; j < TN; j++)
     b2[j] = *reinterpret_cast<const uint64_t*>(bs + (kp * BN + gm_col<TN, BN>(wn, ln, j)) * 2);
-  if constexpr (std::is_same<T, float>::value) {
+  constexpr int HM = TM >= 2 ? TM / 2 : 1;
 #pragma unroll
-    for (int i = 0; i < TM; i++)
+  for (int h = 0; h < TM; h += HM) {
+    uint64_t a2[HM];
 #pragma unroll
-      for (int j = 0; j < TN; j++) {
-        uint64_t s2 = add2(a2[i], b2[j]);
-        acc[i][j] = max3(acc[i][j], lo32(s2), hi32(s2));
-      }
-  } else {
+    for (int i = 0; i < HM; i++)
+      a2[i] = *reinterpret_cast<const uint64_t*>(as + (kp * BM + gm_row<TM, BM>(wm, lm, h + i)) * 2);
+    if constexpr (std::is_same<T, float>::value) {
 #pragma unroll
-    for (int i = 0; i < TM; i++)
+      for (int i = 0; i < HM; i++)
 #pragma unroll
-      for (int j = 0; j < TN; j++) {
-        int32_t x0 = (int32_t)(uint32_t)a2[i], x1 = (int32_t)(uint32_t)(a2[i] >> 32);
-        int32_t y0 = (int32_t)(uint32_t)b2[j], y1 = (int32_t)(uint32_t)(b2[j] >> 32);
-        T v = Trop<T>::mac(acc[i][j], (T)x0, (T)y0);
-        acc[i][j] = Trop<T>::mac(v, (T)x1, (T)y1);
-      }
+        for (int j = 0; j < TN; j++) {
+          uint64_t s2 = add2(a2[i], b2[j]);
+          acc[h + i][j] = max3(acc[h + i][j], lo32(s2), hi32(s2));
+        }
+    } else {
+#pragma unroll
+      for (int i = 0; i < HM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) {
+          int32_t x0 = (int32_t)(uint32_t)a2[i], x1 = (int32_t)(uint32_t)(a2[i] >> 32);
+          int32_t y0 = (int32_t)(uint32_t)b2[j], y1 = (int32_t)(uint32_t)(b2[j] >> 32);
+          T v = Trop<T>::mac(acc[h + i][j], (T)x0, (T)y0);
+          acc[h + i][j] = Trop<T>::mac(v, (T)x1, (T)y1);
+        }
+    }
   }
 }
 
@@ -527,7 +542,7 @@ __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T*
 // fused GEMM tile: k-pair interleaved operands staged by bulk async copies
 // ---------------------------------------------------------------------------
 constexpr int kGemmStages = 3;
-constexpr int kGemmBK = 16;
+constexpr int kGemmBK = 32;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -537,6 +552,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
 }
 __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
   asm volatile("mbarrier.inval.shared.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
@@ -564,22 +582,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-template <int BM, int BN>
+template <int BM, int BN, int S = kGemmStages, int BK = kGemmBK>
 struct GemmSmem {
-  static constexpr int KP = kGemmBK / 2;
-  static constexpr int BAR_BYTES = 128;
+  static constexpr int KP = BK / 2;
+  static constexpr int BAR_BYTES = 128;  // full[S] and empty[S] mbarriers
   static constexpr int A_STAGE = KP * BM * 2;  // elements
   static constexpr int B_STAGE = KP * BN * 2;
-  static constexpr int BYTES = BAR_BYTES + kGemmStages * (A_STAGE + B_STAGE) * 4;
+  static constexpr int BYTES = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;
 };
 
 // One BM x BN output tile of batch point b.  Returns false after a timed-out
 // wait (err is set; copies in flight are drained with a bounded wait).
-template <typename T, int BM, int BN>
+template <typename T, int BM, int BN, int S = kGemmStages, int BK = kGemmBK>
 __device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena, int* __restrict__ smem,
                           int* err) {
-  using SM = GemmSmem<BM, BN>;
-  constexpr int KP = SM::KP, S = kGemmStages;
+  using SM = GemmSmem<BM, BN, S, BK>;
+  constexpr int KP = SM::KP;
   constexpr int TM = BM / 16, TN = BN / 16;
   const int t = threadIdx.x;
   const int M = 1 << d.m_log2, N = 1 << d.n_log2;
@@ -589,29 +607,34 @@ __device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena
   const int m0 = (int)(mn % tiles_m) * BM, n0 = (int)(mn / tiles_m) * BN;
   const T* Ab = arena + d.a_off + b * (int64_t)M * K;
   const T* Bb = arena + d.b_off + b * (int64_t)N * K;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + S;
   T* As = reinterpret_cast<T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES);
   T* Bs = As + S * SM::A_STAGE;
-  const int nk = (int)(K / kGemmBK);
+  const int nk = (int)(K / BK);
+  const int warp = t >> 5, lane = t & 31;
 
   __syncthreads();  // the previous user of this shared memory is done
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (t == 0)
-    for (int i = 0; i < S; i++) mbar_init(&bars[i], 1);
+    for (int i = 0; i < S; i++) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kThreads / 32);
+    }
   __syncthreads();
 
   auto issue = [&](int kc, int slot) {
-    mbar_expect_tx(&bars[slot], (uint32_t)((SM::A_STAGE + SM::B_STAGE) * sizeof(T)));
+    mbar_expect_tx(&full[slot], (uint32_t)((SM::A_STAGE + SM::B_STAGE) * sizeof(T)));
     for (int kp = 0; kp < KP; kp++) {
       const int64_t row = (int64_t)kc * KP + kp;
-      bulk_g2s(As + slot * SM::A_STAGE + kp * BM * 2, Ab + row * 2 * M + 2 * m0, BM * 2 * sizeof(T), &bars[slot]);
-      bulk_g2s(Bs + slot * SM::B_STAGE + kp * BN * 2, Bb + row * 2 * N + 2 * n0, BN * 2 * sizeof(T), &bars[slot]);
+      bulk_g2s(As + slot * SM::A_STAGE + kp * BM * 2, Ab + row * 2 * M + 2 * m0, BM * 2 * sizeof(T), &full[slot]);
+      bulk_g2s(Bs + slot * SM::B_STAGE + kp * BN * 2, Bb + row * 2 * N + 2 * n0, BN * 2 * sizeof(T), &full[slot]);
     }
   };
+  int issued = 0;
   if (t == 0)
-    for (int kc = 0; kc < S - 1 && kc < nk; kc++) issue(kc, kc);
+    for (; issued < S && issued < nk; issued++) issue(issued, issued);
 
-  const int warp = t >> 5, lane = t & 31;
   const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
   T acc[TM][TN];
 #pragma unroll
@@ -619,34 +642,43 @@ __device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena
 #pragma unroll
     for (int j = 0; j < TN; j++) acc[i][j] = Trop<T>::neg();
 
-  int issued = S - 1 < nk ? S - 1 : nk;
+  // S chunks in flight.  A warp that has used a chunk arrives on its empty
+  // barrier; thread 0 refills the slot once all warps have.  No block-wide
+  // barrier in the loop.  A timed-out wait clears ok and the loop runs on
+  // (results are discarded); the failure is collected once after the loop.
   bool ok = true;
   for (int kc = 0; kc < nk; kc++) {
     const int slot = kc % S;
-    if (t == 0 && kc + S - 1 < nk) {
-      issue(kc + S - 1, (kc + S - 1) % S);
-    }
-    if (kc + S - 1 < nk) issued = kc + S;
-    const bool mine = mbar_wait(&bars[slot], (uint32_t)((kc / S) & 1));
-    ok = __syncthreads_and(mine) != 0;
-    if (!ok) break;
+    const uint32_t par = (uint32_t)((kc / S) & 1);
+    if (ok) ok = mbar_wait(&full[slot], par);
     const T* as = As + slot * SM::A_STAGE;
     const T* bs = Bs + slot * SM::B_STAGE;
-#pragma unroll
+#pragma unroll 2
     for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
-    __syncthreads();  // slot free for the next copy
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[slot]);
+    if (t == 0 && kc + S < nk && ok) {
+      ok = mbar_wait(&empty[slot], par);
+      if (ok) {
+        issue(kc + S, slot);
+        issued = kc + S + 1;
+      }
+    }
   }
-  if (!ok) {
+  if (__syncthreads_or(!ok)) {
     if (t == 0) {
       atomicExch(err, 3 /* TB_ERR_TIMEOUT */);
-      // drain what was issued, bounded, before the shared memory is reused
-      for (int kc = 0; kc < issued; kc++) mbar_wait(&bars[kc % S], (uint32_t)((kc / S) & 1));
+      // every issued chunk must land before the shared memory is reused
+      for (int kc = 0; kc < issued; kc++) mbar_wait(&full[kc % S], (uint32_t)((kc / S) & 1));
     }
     __syncthreads();
     return false;
   }
   if (t == 0)
-    for (int i = 0; i < S; i++) mbar_inval(&bars[i]);
+    for (int i = 0; i < S; i++) {
+      mbar_inval(&full[i]);
+      mbar_inval(&empty[i]);
+    }
   // epilogue: scatter the tile into C's layout
   int* scM = reinterpret_cast<int*>(As);
   int* scN = scM + BM;

@@ -67,7 +67,7 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
     while (pa < (int)A.size() && index_of(s, A[pa]) >= 0) pa++;
     while (pb < (int)B.size() && index_of(s, B[pb]) >= 0) pb++;
     while (pc < (int)C.size() && index_of(s, C[pc]) >= 0) pc++;
-    if (tc > 11 || tr > 8 || na > 13 || nb > 13) return false;
+    if (tc > 10 || tr > 8 || na > 13 || nb > 13) return false;
     if (na - pa > 9 || nb - pb > 9 || tc - pc > 9) return false;
     int64_t sm = (int64_t(1) << na) + (Bp ? (int64_t(1) << nb) : 0);
     return sm <= kSmemFloats;
@@ -107,7 +107,7 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
       if (!inS(x)) { next = x; break; }
     if (next < 0) break;
     if (tc >= out_bits_target && grid <= 12) break;
-    if (tc >= 11) break;
+    if (tc >= 10) break;
     auto s2 = with(S, next);
     if (!feasible(s2)) break;
     S = s2;
@@ -184,7 +184,7 @@ bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
     if (j >= B.size() || B[j] != Bt[q]) return false;
   if (j != B.size()) return false;
   if (C.size() != M.size() + N.size() + Bt.size()) return false;
-  if (M.size() < 4 || N.size() < 4 || K.size() < 4) return false;
+  if (M.size() < 4 || N.size() < 4 || K.size() < 5) return false;  // K >= 32: one pipeline stage
   if (M.size() > 30 || N.size() > 30 || K.size() > 30 || Bt.size() > 30) return false;
   std::memset(&g, 0xff, sizeof(g));
   g.a_off = a_off; g.b_off = b_off; g.c_off = c_off;
@@ -466,7 +466,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       else if (!ina) priv = true;
     }
     bool gemm = gmin > 0 && !priv && a >= T && b >= T && (int)M.size() >= gmin && (int)N.size() >= gmin &&
-                (int)K.size() >= gmin;
+                (int)K.size() >= gmin + 1;
     auto by_c = [&](std::vector<int32_t>& v, const std::vector<int32_t>& pref) {
       std::stable_sort(v.begin(), v.end(), [&](int32_t x, int32_t y) {
         bool px = index_of(pref, x) >= 0, py = index_of(pref, y) >= 0;
@@ -483,6 +483,16 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       by_c(M, la);
       by_c(N, lb);
       by_c(Bt, none);
+      // k0 sits at position 0 of both operands: prefer a label each operand's
+      // own node keeps from one side (it is then inside that node's CTA tile)
+      {
+        int best = 0, bscore = -1;
+        for (size_t q = 0; q < K.size(); q++) {
+          int sc = (index_of(la, K[q]) >= 0 ? 2 : 0) + (index_of(lb, K[q]) >= 0 ? 2 : 0);
+          if (sc > bscore) { bscore = sc; best = (int)q; }
+        }
+        std::swap(K[0], K[best]);
+      }
       std::vector<int32_t> fa{K[0]}, fb{K[0]};
       fa.insert(fa.end(), M.begin(), M.end());
       fb.insert(fb.end(), N.begin(), N.end());

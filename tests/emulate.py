@@ -19,7 +19,7 @@ import numpy as np
 KMAXBITS = 48
 KMAXTILE = 16
 KTHREADS = 256
-KMAXOPT = 8
+KMAXOPT = 4
 KSMEM = 8192
 
 
@@ -332,7 +332,7 @@ GEMM_TILES = {(7, 7), (7, 6), (6, 7), (6, 6), (5, 5), (4, 4)}
 def emu_gemm_step(g, arena, written):
     """Fused GEMM tile: k-pair interleaved operands, scatter store to C."""
     assert (g.bm_log2, g.bn_log2) in GEMM_TILES
-    assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 4
+    assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 5
     M, N, K, Bt = 1 << g.m_log2, 1 << g.n_log2, 1 << g.k_log2, 1 << g.bt_log2
     assert g.n_tiles == (M >> g.bm_log2) * (N >> g.bn_log2) * Bt
     rc = tensor_rank([g.m_pc[i] for i in range(g.m_log2)] + [g.n_pc[i] for i in range(g.n_log2)] +

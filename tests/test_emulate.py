@@ -89,7 +89,7 @@ def test_invalid_plans_rejected(tb, lib):
                                                   n_labels=code.n_labels), use_node_iy=True)
 
 
-@pytest.mark.parametrize("shape", [(4, 4, 4, 1), (5, 4, 6, 2), (6, 6, 4, 0), (7, 5, 4, 1)])
+@pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1)])
 def test_gemm_steps(tb, orc, lib, shape):
     from cases import gemm_case
 

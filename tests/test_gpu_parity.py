@@ -111,7 +111,7 @@ def test_contract_generic_tensors(tb, orc, engine):
             assert np.array_equal(got, ref), (it, mode)
 
 
-@pytest.mark.parametrize("shape", [(4, 4, 4, 1), (5, 4, 6, 2), (6, 6, 4, 0), (7, 5, 4, 1), (7, 7, 6, 2),
+@pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (7, 7, 6, 2),
                                    (8, 7, 5, 1)])
 def test_fused_gemm_nodes(tb, orc, engine, shape):
     from cases import gemm_case
