@@ -362,6 +362,8 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       p.labels[me] = needed;
     }
   }
+  for (int i = 0; i < total; i++)
+    if (p.labels[i].size() > 30) return "a tensor of rank > 30 (over 4 GiB) in the contraction tree";
   p.root = in.n_nodes ? total - 1 : 0;
   if (in.n_nodes && !in.node_iy_off) {
     // the root keeps exactly the open labels, in iy order
