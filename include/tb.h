@@ -195,6 +195,27 @@ tb_status tb_last_timing(const tb_ctx* ctx, double* device_ms, int64_t* launches
 tb_status tb_gemm_device(tb_ctx* ctx, int64_t M, int64_t N, int64_t K, int64_t batch,
                          const void* A, const void* B, void* C, void* stream);
 
+/*
+ * tb_solve_static -- has no counterpart in the reference.
+ *
+ * One MIS contraction that allocates no device memory, for callers that
+ * cannot call cudaMalloc (code running inside another runtime's memory pool
+ * or allocator hooks, or handed only a stream).  All device memory it uses
+ * lives in one fixed 64 MiB __device__ array that every GPU loading this
+ * library holds until the process exits; networks whose arena does not fit
+ * are refused with TB_ERR_UNSUPPORTED (tb_last_error(NULL) says why).
+ * Arguments are those of tb_plan_create (no open or sliced labels, labels
+ * derived) plus the vertex weights; the MIS value goes to *out_value (host).
+ * Work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
+ * with the plain per-contraction kernels, and the call returns after the
+ * result is on the host.  The first call on a device looks up the array's
+ * address; make it before any stream capture.  Calls share the array and
+ * race if they overlap on the GPU: serialise them.
+ */
+tb_status tb_solve_static(int32_t n_labels, int32_t n_tensors, const int32_t* ix_off, const int32_t* ix_lab,
+                          int32_t n_nodes, const int32_t* children, const float* weights, float* out_value,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

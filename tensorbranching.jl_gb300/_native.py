@@ -81,6 +81,8 @@ ENGINE_SIGNATURES = {
     "tb_last_timing": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_int64)]),
     "tb_gemm_device": (c_int32, [c_void_p, c_int64, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
+    "tb_solve_static": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                                  c_void_p]),
 }
 
 ORDER_SIGNATURES = {

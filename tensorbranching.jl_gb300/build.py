@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-ENGINE_SOURCES = ["engine.cu", "plan.cpp"]
+ENGINE_SOURCES = ["engine.cu", "static_solve.cu", "plan.cpp"]
 ENGINE_HEADERS = ["kernels.cuh", "plan.h", "tb_internal.h"]
 ORDER_SOURCES = ["order.cpp"]
 

@@ -287,6 +287,11 @@ static tb_status fail(tb_status s, const std::string& msg) {
   return s;
 }
 
+namespace tb {
+// Lets other translation units of the library report through tb_last_error.
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace tb
+
 #define CU(x)                                                                                   \
   do {                                                                                          \
     cudaError_t e_ = (x);                                                                       \
@@ -1112,4 +1117,67 @@ extern "C" int32_t tbi_sizes(int32_t* out, int32_t n) {
                   (int32_t)sizeof(FinalDesc), (int32_t)sizeof(GemmDesc), 0};
   for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Internal: measured SIMT max-plus peak (roofline denominator).  Sixteen
+// loop-carried chains per thread of one packed add (add.f32x2) and one
+// three-input max per two (max,+) pairs -- the inner step of the GEMM tiles
+// -- so that no operand is loop-invariant.  Returns tropical ops/s (max and
+// add counted as two ops).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_peak_f32(float* out, int iters, float seed) {
+  constexpr int NC = 16;
+  float f[NC];
+  uint64_t x[NC];
+#pragma unroll
+  for (int j = 0; j < NC; j++) {
+    f[j] = seed * (float)(j + threadIdx.x);
+    float hi = f[j] + 1.0f;
+    x[j] = ((uint64_t)__float_as_uint(hi) << 32) | __float_as_uint(f[j]);
+  }
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int j = 0; j < NC; j++) {
+      uint64_t s = add2(x[j], x[(j + 5) % NC]);
+      f[j] = max3(f[j], lo32(s), hi32(s));
+      x[j] = s;
+    }
+  }
+  float s = 0;
+#pragma unroll
+  for (int j = 0; j < NC; j++) s += f[j] + lo32(x[j]);
+  if (s == 1.2345f) out[0] = s;
+}
+
+extern "C" int32_t tbi_measure_maxplus_peak(int32_t device, double* ops_per_s) {
+  if (!ops_per_s) return TB_ERR_INVALID;
+  CU(cudaSetDevice(device));
+  int sms = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  float* out = nullptr;
+  CU(cudaMalloc(&out, 64));
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  const int blocks = sms * 8, iters = 4096;
+  k_peak_f32<<<blocks, 256>>>(out, iters, 1e-7f);
+  float best = 1e30f;
+  for (int r = 0; r < 3; r++) {
+    cudaEventRecord(e0);
+    k_peak_f32<<<blocks, 256>>>(out, iters, 1e-7f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return fail(TB_ERR_CUDA, cudaGetErrorString(e));
+  // 16 chains x 2 MAC per iteration per thread, 2 ops per MAC
+  *ops_per_s = (double)blocks * 256 * iters * 16 * 2 * 2 / (best * 1e-3);
+  return TB_OK;
 }
