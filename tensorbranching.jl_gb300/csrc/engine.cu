@@ -36,10 +36,13 @@ __global__ void __launch_bounds__(kThreads) k_leaves(const LeafDesc* leaves, int
   leaves_tile<T>(leaves, n, sv, arena, blockIdx.x);
 }
 
+// A stream-tile node: CTA b runs tiles [b * chunk, (b + 1) * chunk).
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_tile(const TileDesc d, T* arena) {
+__global__ void __launch_bounds__(kThreads, 2) k_tile(const TileDesc d, T* arena, int64_t chunk) {
   extern __shared__ int tb_smem[];
-  stream_tile<T>(d, blockIdx.x, arena, tb_smem);
+  const int64_t t0 = (int64_t)blockIdx.x * chunk;
+  const int64_t t1 = t0 + chunk < d.n_tiles ? t0 + chunk : d.n_tiles;
+  stream_tiles<T>(d, t0, t1, arena, tb_smem);
 }
 
 template <typename T>
@@ -100,17 +103,40 @@ __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int
 // One launch per tree level: block b runs ticket first_ticket + b.  No
 // waiting: the previous launch on the stream finished every dependency.
 template <typename T, int KINDS>
-__global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
-                                                   int64_t first_ticket, float* out_item, const float* r,
-                                                   int* err) {
+__global__ void __launch_bounds__(kThreads, 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
+                                                   int64_t first_ticket, int64_t last_ticket, int64_t chunk,
+                                                   float* out_item, const float* r, int* err) {
   extern __shared__ int tb_smem[];
   __shared__ int s_g;
-  int64_t tk = first_ticket + blockIdx.x;
-  if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
-  __syncthreads();
-  const Group g = groups[s_g];
-  const ItemDev<T>& it = items[g.item];
-  run_step<T, KINDS>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, r, g.item, err);
+  if constexpr (KINDS == 1) {
+    // CTA b runs tickets [b * chunk, (b + 1) * chunk) of this level, a run of
+    // tiles per group so each stream tile builds its tables once
+    int64_t tk = first_ticket + (int64_t)blockIdx.x * chunk;
+    const int64_t end = tk + chunk < last_ticket ? tk + chunk : last_ticket;
+    while (tk < end) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
+      __syncthreads();
+      const int gi = s_g;
+      const Group g = groups[gi];
+      const int64_t g_end = gi + 1 < n_groups && groups[gi + 1].first < end ? groups[gi + 1].first : end;
+      const ItemDev<T>& it = items[g.item];
+      const Step& st = it.steps[g.step];
+      if (st.kind == STEP_TILE) {
+        stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem);
+      } else {
+        for (int64_t x = tk; x < g_end; x++) run_step<T, KINDS>(it, st, x - g.first, tb_smem, out_item, r, g.item, err);
+      }
+      tk = g_end;
+    }
+  } else {
+    int64_t tk = first_ticket + blockIdx.x;
+    if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
+    __syncthreads();
+    const Group g = groups[s_g];
+    const ItemDev<T>& it = items[g.item];
+    run_step<T, KINDS>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, r, g.item, err);
+  }
 }
 
 // Persistent executor.  Tickets are handed out in dependency order, so a
@@ -259,6 +285,7 @@ struct tb_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int sms = 0;
   int persistent_ctas = 0;
+  int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   size_t budget = 0;
   DevBuf arena, items, groups, done, misc, slice_vals, out_item, rvals;
   HostBuf h_items, h_groups, h_in, h_out;
@@ -308,7 +335,7 @@ static size_t dtype_size(const tb_ctx*) { return 4; }
 
 // Dynamic shared memory of the kernels: stream tiles (see plan_tile's
 // limits), GEMM tiles (pipeline stages), or both for the persistent kernel.
-static int stream_smem_bytes() { return (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4; }
+static int stream_smem_bytes() { return stream_smem_words_max() * 4; }
 static int smem_bytes(int kinds) {
   int b = 0;
   if (kinds & 1) b = std::max(b, stream_smem_bytes());
@@ -368,7 +395,8 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
   }
   if (h.n_nodes == 0) {
     const TileDesc& d = h.tiles[0];
-    k_tile<T><<<d.n_tiles, kThreads, stream_smem_words(d) * 4, s>>>(d, arena);  // within smem_bytes(1)
+    int64_t grid = std::min<int64_t>(d.n_tiles, c->stream_ctas);
+    k_tile<T><<<(unsigned)grid, kThreads, stream_smem_words(d) * 4, s>>>(d, arena, (d.n_tiles + grid - 1) / grid);
     CU(cudaGetLastError());
     launches++;
     return TB_OK;
@@ -376,7 +404,9 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
   for (int j = 0; j < h.n_nodes; j++) {
     for (const PlainOp& op : h.plain[j]) {
       if (op.kind == PLAIN_TILE) {
-        k_tile<T><<<op.tile.n_tiles, kThreads, stream_smem_words(op.tile) * 4, s>>>(op.tile, arena);
+        int64_t grid = std::min<int64_t>(op.tile.n_tiles, c->stream_ctas);
+        k_tile<T><<<(unsigned)grid, kThreads, stream_smem_words(op.tile) * 4, s>>>(op.tile, arena,
+                                                                                    (op.tile.n_tiles + grid - 1) / grid);
         CU(cudaGetLastError());
       } else {
         CU(dispatch_k1<T>(arena + op.a_off, arena + op.b_off, arena + op.c_off, op.M, op.N, op.K, op.batch, s));
@@ -489,12 +519,15 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
     int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
     for (auto& lr : c->level_ranges) {
       if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
-      if (lr.kinds == 2)
-        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), s>>>(items, groups, c->n_groups, lr.first,
-                                                                          out_item, rv, err);
-      else
-        k_level<T, 1><<<(unsigned)lr.count, kThreads, smem_bytes(1), s>>>(items, groups, c->n_groups, lr.first,
-                                                                          out_item, rv, err);
+      if (lr.kinds == 2) {
+        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), s>>>(
+            items, groups, c->n_groups, lr.first, lr.first + lr.count, 1, out_item, rv, err);
+      } else {
+        const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
+        k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), s>>>(
+            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv,
+            err);
+      }
       CU(cudaGetLastError());
       launches++;
     }
@@ -725,6 +758,12 @@ tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<int32_t>, kThreads, max_stream_smem_bytes()));
   per_sm = std::max(1, per_sm);
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : per_sm * c->sms;
+  int per_sm_stream = 0;
+  if (c->opt.dtype == TB_DTYPE_F32)
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_stream, k_level<float, 1>, kThreads, smem_bytes(1)));
+  else
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_stream, k_level<int32_t, 1>, kThreads, smem_bytes(1)));
+  c->stream_ctas = std::max(1, per_sm_stream) * c->sms;
   *out = c.release();
   return TB_OK;
 }
@@ -929,12 +968,15 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
     const Group* groups = reinterpret_cast<const Group*>(c->groups.p);
     float* oi = reinterpret_cast<float*>(c->out_item.p);
     for (auto& lr : c->level_ranges) {
-      if (lr.kinds == 2)
-        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), c->stream>>>(items, groups, c->n_groups,
-                                                                                  lr.first, oi, nullptr, err);
-      else
-        k_level<T, 1><<<(unsigned)lr.count, kThreads, smem_bytes(1), c->stream>>>(items, groups, c->n_groups,
-                                                                                  lr.first, oi, nullptr, err);
+      if (lr.kinds == 2) {
+        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), c->stream>>>(
+            items, groups, c->n_groups, lr.first, lr.first + lr.count, 1, oi, nullptr, err);
+      } else {
+        const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
+        k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), c->stream>>>(
+            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr,
+            err);
+      }
       CU(cudaGetLastError());
     }
   }

@@ -63,12 +63,6 @@ struct Vec2<float> { using type = float2; };
 template <>
 struct Vec2<int32_t> { using type = int2; };
 
-// XOR swizzle of a shared-memory index.  Linear over GF(2), so the swizzled
-// index of a bitwise OR of disjoint fields is the XOR of their swizzles.
-// It permutes words inside each 32-word row and spreads power-of-two strides
-// over all 32 banks.
-__device__ __forceinline__ int swz(int j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31); }
-
 __device__ __forceinline__ uint64_t globaltimer() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -117,81 +111,89 @@ __device__ void leaves_tile(const LeafDesc* __restrict__ leaves, int n_leaves,
 // ---------------------------------------------------------------------------
 // stream tile
 // ---------------------------------------------------------------------------
+// XOR swizzle of a shared-memory word index at 16-byte granularity: bits 2..4
+// of the index are XORed with bits 5..7 and 10..12.  It is linear over GF(2)
+// (the swizzle of an OR of disjoint bit fields is the XOR of their swizzles),
+// keeps every aligned 4-word chunk contiguous (so 16-byte async copies land
+// intact) and spreads power-of-two strides over 8 bank groups.
+__host__ __device__ __forceinline__ int swz16(int j) { return j ^ ((((j >> 5) ^ (j >> 10)) & 7) << 2); }
+
+// Operand regions are padded to 4 words so every 16-byte async copy lands on
+// a 16-byte boundary of shared memory.
+__host__ __device__ inline int stream_a_words(const TileDesc& d) { return ((1 << d.na) + 3) & ~3; }
+__host__ __device__ inline int stream_buf_words(const TileDesc& d) {
+  return stream_a_words(d) + (d.b_off >= 0 ? (((1 << d.nb) + 3) & ~3) : 0);
+}
+// shared memory of a stream tile: two operand buffers, then tables
 __host__ __device__ inline int stream_smem_words(const TileDesc& d) {
   const bool hasB = d.b_off >= 0;
-  int w = (1 << d.na) + (hasB ? (1 << d.nb) : 0);
+  int w = 2 * stream_buf_words(d);
   w += 1 << (d.na - d.pa);
   w += hasB ? (1 << (d.nb - d.pb)) : 0;
   w += 1 << (d.n_tc - d.pc);
   w += 2 * (1 << d.n_tr);
   w += kThreads;
+  w += 5 * kMaxBits;  // offset increments
   return w;
 }
+// upper bound of stream_smem_words over every descriptor plan_tile emits
+__host__ __device__ constexpr int stream_smem_words_max() {
+  return 2 * kSmemFloats + 3 * 512 + 2 * 256 + kThreads + 5 * kMaxBits;
+}
 
-// Copy the 2^n-element sub-tensor at src (tile bit b <-> tensor position
-// pos[b]; bits below p are positions 0..p-1) into swizzled shared memory.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Issue async copies of the 2^n-element sub-tensor at src into swizzled
+// shared memory (tile bit b <-> tensor position pos[b]; bits below p are the
+// tensor's positions 0..p-1, the rest go through the table hi).
 template <typename T>
-__device__ __forceinline__ void load_sub(T* __restrict__ dst, const T* __restrict__ src, int n, int p,
-                                         const int* __restrict__ hi) {
+__device__ __forceinline__ void issue_sub(T* __restrict__ dst, const T* __restrict__ src, int n, int p,
+                                          const int* __restrict__ hi) {
   const int N = 1 << n;
   if (p >= 2) {
-    using V = typename Vec4<T>::type;
     const int lowmask = (1 << p) - 1;
-    const int nvec = N >> 2;
-    for (int q0 = threadIdx.x; q0 < nvec; q0 += 4 * kThreads) {
-      V v[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        int q = q0 + u * kThreads;
-        if (q < nvec) {
-          int j = q << 2;
-          v[u] = __ldcg(reinterpret_cast<const V*>(src + ((j & lowmask) + hi[j >> p])));
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        int q = q0 + u * kThreads;
-        if (q < nvec) {
-          int ph = swz(q << 2);
-          dst[ph] = v[u].x;
-          dst[ph ^ 1] = v[u].y;
-          dst[ph ^ 2] = v[u].z;
-          dst[ph ^ 3] = v[u].w;
-        }
-      }
+    for (int q = threadIdx.x; q < (N >> 2); q += kThreads) {
+      const int j = q << 2;
+      cp_async16(dst + swz16(j), src + ((j & lowmask) + hi[j >> p]));
     }
   } else if (p == 1) {
-    using V = typename Vec2<T>::type;
-    const int nvec = N >> 1;
-    for (int q = threadIdx.x; q < nvec; q += kThreads) {
-      int j = q << 1;
-      V v = __ldcg(reinterpret_cast<const V*>(src + ((j & 1) + hi[j >> 1])));
-      int ph = swz(j);
-      dst[ph] = v.x;
-      dst[ph ^ 1] = v.y;
+    for (int q = threadIdx.x; q < (N >> 1); q += kThreads) {
+      const int j = q << 1;
+      cp_async8(dst + swz16(j), src + hi[j >> 1]);
     }
   } else {
-    for (int j = threadIdx.x; j < N; j += kThreads) dst[swz(j)] = __ldcg(src + hi[j]);
+    for (int j = threadIdx.x; j < N; j += kThreads) cp_async4(dst + swz16(j), src + hi[j]);
   }
 }
 
+// Run tiles [t0, t1) of one stream-tile descriptor on this CTA: index tables
+// are built once, and the operand sub-tiles of the next (tile, loop step) are
+// copied asynchronously while the current one is reduced.
 template <typename T>
-__device__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ arena, int* __restrict__ smem) {
+__device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __restrict__ arena,
+                             int* __restrict__ smem) {
   const int t = threadIdx.x;
   const bool hasB = d.b_off >= 0;
-  int64_t oa = d.a_off, ob = d.b_off, oc = d.c_off;
-  for (int i = 0; i < d.n_grid; i++) {
-    if ((tile >> i) & 1) {
-      int a = d.g_pa[i], b = d.g_pb[i];
-      if (a >= 0) oa += int64_t(1) << a;
-      if (b >= 0) ob += int64_t(1) << b;
-      oc += int64_t(1) << d.g_pc[i];
-    }
-  }
-  const int NA = 1 << d.na, NB = hasB ? (1 << d.nb) : 0;
-  T* As = reinterpret_cast<T*>(smem);
-  T* Bs = As + NA;
-  int* ldA = reinterpret_cast<int*>(Bs + NB);
+  const int NA = stream_a_words(d);  // A region (padded), B region follows
+  const int BUF = stream_buf_words(d);
+  T* buf0 = reinterpret_cast<T*>(smem);
+  int* ldA = reinterpret_cast<int*>(buf0 + 2 * BUF);
   const int nAh = 1 << (d.na - d.pa);
   const int nBh = hasB ? (1 << (d.nb - d.pb)) : 0;
   const int nCh = 1 << (d.n_tc - d.pc);
@@ -201,7 +203,15 @@ __device__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ are
   int* IAr = stC + nCh;
   int* IBr = IAr + ntr;
   T* red = reinterpret_cast<T*>(IBr + ntr);
+  // increments of the grid / loop offsets when the index goes from x to x+1
+  // with k trailing ones: +2^pos_k - sum_{i<k} 2^pos_i (pos -1: no term)
+  int* incAg = reinterpret_cast<int*>(red + kThreads);
+  int* incBg = incAg + kMaxBits;
+  int* incCg = incBg + kMaxBits;
+  int* incAl = incCg + kMaxBits;
+  int* incBl = incAl + kMaxBits;
 
+  __syncthreads();  // the previous user of this shared memory is done
   for (int j = t; j < nAh; j += kThreads) {
     int o = 0;
     for (int b = 0; b < d.na - d.pa; b++)
@@ -228,8 +238,20 @@ __device__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ are
         if (d.tr_b[b] >= 0) xb |= 1 << d.tr_b[b];
       }
     }
-    IAr[j] = swz(xa);
-    IBr[j] = swz(xb);
+    IAr[j] = swz16(xa);
+    IBr[j] = swz16(xb);
+  }
+  if (t < 5 * kMaxBits) {
+    const int which = t / kMaxBits, k = t % kMaxBits;
+    const int nbits = which < 3 ? d.n_grid : d.n_loop;
+    const int8_t* pos = which == 0 ? d.g_pa : which == 1 ? d.g_pb : which == 2 ? d.g_pc : which == 3 ? d.l_pa : d.l_pb;
+    int v = 0;
+    if (k < nbits) {
+      if (pos[k] >= 0) v += 1 << pos[k];
+      for (int i = 0; i < k; i++)
+        if (pos[i] >= 0) v -= 1 << pos[i];
+    }
+    incAg[which * kMaxBits + k] = v;
   }
 
   // thread -> (output, reduction split)
@@ -247,10 +269,9 @@ __device__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ are
       if (d.tc_b[b] >= 0) ibt |= 1 << d.tc_b[b];
     }
   }
-  iat = swz(iat);
-  ibt = swz(ibt);
+  iat = swz16(iat);
+  ibt = swz16(ibt);
   int iah[kMaxOpt], ibh[kMaxOpt];
-  T acc[kMaxOpt];
 #pragma unroll
   for (int i = 0; i < kMaxOpt; i++) {
     int xa = 0, xb = 0;
@@ -260,60 +281,150 @@ __device__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ are
         if (d.tc_b[b] >= 0) xb |= 1 << d.tc_b[b];
       }
     }
-    iah[i] = iat ^ swz(xa);
-    ibh[i] = ibt ^ swz(xb);
-    acc[i] = Trop<T>::neg();
+    iah[i] = iat ^ swz16(xa);
+    ibh[i] = ibt ^ swz16(xb);
   }
-  const int64_t nloop = int64_t(1) << d.n_loop;
-  for (int64_t rl = 0; rl < nloop; rl++) {
-    int64_t la = oa, lb = ob;
-    for (int i = 0; i < d.n_loop; i++) {
-      if ((rl >> i) & 1) {
-        if (d.l_pa[i] >= 0) la += int64_t(1) << d.l_pa[i];
-        if (d.l_pb[i] >= 0) lb += int64_t(1) << d.l_pb[i];
-      }
+  // absolute grid offsets of the first tile (32-bit within each tensor)
+  int ga = 0, gb = 0, gc = 0;
+  for (int i = 0; i < d.n_grid; i++) {
+    if ((t0 >> i) & 1) {
+      if (d.g_pa[i] >= 0) ga += 1 << d.g_pa[i];
+      if (d.g_pb[i] >= 0) gb += 1 << d.g_pb[i];
+      gc += 1 << d.g_pc[i];
     }
-    __syncthreads();  // tables ready / previous compute done
-    load_sub<T>(As, arena + la, d.na, d.pa, ldA);
-    if (hasB) load_sub<T>(Bs, arena + lb, d.nb, d.pb, ldB);
-    __syncthreads();
-    if (act) {
-      const int step = 1 << split;
+  }
+  __syncthreads();  // tables ready
+  // reduction tables in registers when they are short (the common case)
+  constexpr int kRr = 4;
+  int iar[kRr], ibr[kRr];
 #pragma unroll
-      for (int i = 0; i < kMaxOpt; i++) {
-        if (i < opt) {
-          T a = acc[i];
-          const int ia = iah[i], ib = ibh[i];
-          if (hasB) {
-            for (int r = s; r < ntr; r += step) a = Trop<T>::mac(a, As[ia ^ IAr[r]], Bs[ib ^ IBr[r]]);
-          } else {
-            for (int r = s; r < ntr; r += step) a = Trop<T>::mx(a, As[ia ^ IAr[r]]);
+  for (int r = 0; r < kRr; r++) {
+    iar[r] = r < ntr ? IAr[r] : 0;
+    ibr[r] = r < ntr ? IBr[r] : 0;
+  }
+  const bool small_r = ntr <= kRr && split == 0;
+
+  const int nloop = 1 << d.n_loop;
+  const int64_t n_items = (t1 - t0) * nloop;
+  const T* A0 = arena + d.a_off;
+  const T* B0 = arena + (hasB ? d.b_off : 0);
+  T* C0 = arena + d.c_off;
+  // prefetch cursor: tile pt, loop step pr, offsets
+  int64_t pt = t0;
+  int pr = 0, pa_g = ga, pb_g = gb, pa_l = 0, pb_l = 0;
+  auto issue = [&](int64_t it) {
+    T* dst = buf0 + (it & 1) * BUF;
+    issue_sub<T>(dst, A0 + (pa_g + pa_l), d.na, d.pa, ldA);
+    if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), d.nb, d.pb, ldB);
+  };
+  auto advance = [&]() {
+    if (pr + 1 < nloop) {
+      const int k = __ffs(~pr) - 1;
+      pa_l += incAl[k];
+      pb_l += incBl[k];
+      pr++;
+    } else {
+      pr = 0;
+      pa_l = pb_l = 0;
+      const int k = __ffsll(~pt) - 1;
+      pa_g += incAg[k];
+      pb_g += incBg[k];
+      pt++;
+    }
+  };
+  int64_t ct = t0;  // tile of the compute / store cursor
+  int oc = gc;
+
+  T acc[kMaxOpt];
+  if (n_items > 0) {
+    issue(0);
+    advance();
+  }
+  cp_async_commit();
+  for (int64_t it = 0; it < n_items; it++) {
+    if (it + 1 < n_items) {
+      issue(it + 1);
+      advance();
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();  // item `it` is in its buffer
+    const int rl = (int)(it % nloop);
+    if (rl == 0) {
+#pragma unroll
+      for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+    }
+    const T* As = buf0 + (it & 1) * BUF;
+    const T* Bs = As + NA;
+    if (act) {
+      if (small_r) {
+#pragma unroll
+        for (int i = 0; i < kMaxOpt; i++) {
+          if (i < opt) {
+            T a = acc[i];
+            const int ia = iah[i], ib = ibh[i];
+#pragma unroll
+            for (int r = 0; r < kRr; r++) {
+              if (r < ntr) {
+                if (hasB) a = Trop<T>::mac(a, As[ia ^ iar[r]], Bs[ib ^ ibr[r]]);
+                else a = Trop<T>::mx(a, As[ia ^ iar[r]]);
+              }
+            }
+            acc[i] = a;
           }
-          acc[i] = a;
+        }
+      } else {
+        const int step = 1 << split;
+#pragma unroll
+        for (int i = 0; i < kMaxOpt; i++) {
+          if (i < opt) {
+            T a = acc[i];
+            const int ia = iah[i], ib = ibh[i];
+            if (hasB) {
+              for (int r = s; r < ntr; r += step) a = Trop<T>::mac(a, As[ia ^ IAr[r]], Bs[ib ^ IBr[r]]);
+            } else {
+              for (int r = s; r < ntr; r += step) a = Trop<T>::mx(a, As[ia ^ IAr[r]]);
+            }
+            acc[i] = a;
+          }
         }
       }
     }
-  }
-  if (split > 0) {
-    __syncthreads();
-    red[t] = acc[0];
-    __syncthreads();
-    if (act && s == 0) {
-      T a = acc[0];
-      for (int s2 = 1; s2 < (1 << split); s2++) a = Trop<T>::mx(a, red[cl + (s2 << lo_bits)]);
-      acc[0] = a;
-    }
-  }
-  if (act && s == 0) {
-    const int cmask = (1 << d.pc) - 1;
-#pragma unroll
-    for (int i = 0; i < kMaxOpt; i++) {
-      if (i < opt) {
-        int c = cl + (i << lo_bits);
-        arena[oc + (c & cmask) + stC[c >> d.pc]] = acc[i];
+    if (rl == nloop - 1) {
+      if (split > 0) {
+        red[t] = acc[0];
+        __syncthreads();
+        if (act && s == 0) {
+          T a = acc[0];
+          for (int s2 = 1; s2 < (1 << split); s2++) a = Trop<T>::mx(a, red[cl + (s2 << lo_bits)]);
+          acc[0] = a;
+        }
       }
+      if (act && s == 0) {
+        const int cmask = (1 << d.pc) - 1;
+        T* Ct = C0 + oc;
+#pragma unroll
+        for (int i = 0; i < kMaxOpt; i++) {
+          if (i < opt) {
+            const int c = cl + (i << lo_bits);
+            Ct[(c & cmask) + stC[c >> d.pc]] = acc[i];
+          }
+        }
+      }
+      const int k = __ffsll(~ct) - 1;
+      oc += incCg[k];
+      ct++;
     }
+    __syncthreads();  // buffer (it & 1) is free for item it + 2
   }
+  cp_async_wait<0>();
+}
+
+// One tile (the launch-per-tile form used by the plain path's kernels).
+template <typename T>
+__device__ __forceinline__ void stream_tile(const TileDesc& d, int64_t tile, T* __restrict__ arena,
+                                            int* __restrict__ smem) {
+  stream_tiles<T>(d, tile, tile + 1, arena, smem);
 }
 
 // ---------------------------------------------------------------------------

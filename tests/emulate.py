@@ -131,12 +131,21 @@ def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4):
 
 
 def swz(j):
-    return j ^ (((j >> 5) ^ (j >> 10)) & 31)
+    """16-byte-granular XOR swizzle of the stream tile (swz16)."""
+    return j ^ ((((j >> 5) ^ (j >> 10)) & 7) << 2)
+
+
+def a_words(d):
+    return ((1 << d.na) + 3) & ~3
+
+
+def buf_words(d):
+    return a_words(d) + ((((1 << d.nb) + 3) & ~3) if d.b_off >= 0 else 0)
 
 
 def smem_words(d):
     hasB = d.b_off >= 0
-    w = (1 << d.na) + ((1 << d.nb) if hasB else 0)
+    w = 2 * buf_words(d)
     w += 1 << (d.na - d.pa)
     w += (1 << (d.nb - d.pb)) if hasB else 0
     w += 1 << (d.n_tc - d.pc)
@@ -146,7 +155,7 @@ def smem_words(d):
 
 
 def max_smem_words():
-    return KSMEM + 3 * 512 + 2 * 256 + KTHREADS
+    return 2 * KSMEM + 3 * 512 + 2 * 256 + KTHREADS
 
 
 def tensor_rank(tile_pos, grid_pos, loop_pos):
@@ -240,22 +249,28 @@ def emu_stream_tile(d, arena, written, expect=None):
                     if d.l_pb[i] >= 0:
                         lb += 1 << d.l_pb[i]
 
-            def load(base, n, p, hi, lo, hi_b):
+            def load(base, n, p, hi, lo, hi_b, region):
                 j = np.arange(1 << n)
                 g = base + (j & ((1 << p) - 1)) + hi[j >> p]
                 assert g.min() >= lo and g.max() < hi_b, "global load out of bounds"
-                if p >= 2:
-                    assert np.all(g[::4] % 4 == 0), "misaligned 16-byte load"
-                elif p == 1:
-                    assert np.all(g[::2] % 2 == 0), "misaligned 8-byte load"
+                # async copies: 16 bytes when p >= 2, 8 when p == 1; both ends aligned
+                for b in (0, 1):  # the two double-buffer slots
+                    dst = b * buf_words(d) + region + swz(j)
+                    if p >= 2:
+                        assert np.all(g[::4] % 4 == 0), "misaligned 16-byte global source"
+                        assert np.all(dst[::4] % 4 == 0), "misaligned 16-byte shared destination"
+                        assert np.all(np.diff(dst.reshape(-1, 4), axis=1) == 1), "16-byte chunk split by swizzle"
+                    elif p == 1:
+                        assert np.all(g[::2] % 2 == 0), "misaligned 8-byte global source"
+                        assert np.all(dst[::2] % 2 == 0), "misaligned 8-byte shared destination"
                 sm = np.empty(1 << n, np.float32)
                 ph = swz(j)
                 assert sorted(ph.tolist()) == list(range(1 << n))
                 sm[ph] = arena[g]
                 return sm
 
-            As = load(la, d.na, d.pa, ldA, a_lo, a_hi)
-            Bs = load(lb, d.nb, d.pb, ldB, b_lo, b_hi) if hasB else None
+            As = load(la, d.na, d.pa, ldA, a_lo, a_hi, 0)
+            Bs = load(lb, d.nb, d.pb, ldB, b_lo, b_hi, a_words(d)) if hasB else None
             act_idx = np.nonzero(act)[0]
             step = 1 << split
             nq = ntr // step
