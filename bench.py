@@ -110,33 +110,50 @@ def load_workload(tb, name):
     return workloads.load(name)
 
 
+OPEN_BITS = 4          # sliced labels kept open per item (2^4 slices per item)
+SLICED_ITEMS_PER_STEP = 64
+
+
 def make_items(engine, wl, tb):
-    """Plans and per-item inputs of one step of the workload."""
+    """Plans and per-item inputs of one step of the workload.  Index-sliced
+    workloads group 2^OPEN_BITS slices per item (those labels stay open in the
+    root tensor) and a step runs SLICED_ITEMS_PER_STEP of the items."""
     plans, svs, rs = [], [], []
     sliced = wl["sliced"]
+    frac = 1.0
     for b in wl["branches"]:
         if b.code is None:
             continue
-        p = engine.plan(b.code, b.p.weight_array(), sliced=sliced)
         if sliced:
-            k = len(sliced)
-            vals = ((np.arange(1 << k)[:, None] >> np.arange(k)[None, :]) & 1).astype(np.int8)
+            opened = sliced[:OPEN_BITS]
+            fixed = sliced[OPEN_BITS:]
+            code = tb.CompressedEinsum(b.code.ixs, list(opened), b.code.children, n_labels=b.code.n_labels)
+            p = engine.plan(code, b.p.weight_array(), sliced=fixed)
+            k = len(fixed)
+            total = 1 << k
+            take = min(total, SLICED_ITEMS_PER_STEP)
+            frac = take / total
+            idx = np.linspace(0, total - 1, take).astype(np.int64)
+            vals = ((idx[:, None] >> np.arange(k)[None, :]) & 1).astype(np.int8)
             for row in vals:
                 plans.append(p)
                 svs.append(row)
                 rs.append(b.r)
         else:
+            p = engine.plan(b.code, b.p.weight_array())
             plans.append(p)
             svs.append(np.zeros(0, np.int8))
             rs.append(b.r)
+    wl["step_fraction"] = frac
     return plans, svs, np.array(rs, np.float32)
 
 
 def expected_answer(wl):
-    """Units a step solves: graphs (MIS values) per step."""
+    """Solves (MIS values) one step completes: graphs per step, or the
+    fraction of one solve a step of a sliced workload covers."""
     if wl["name"] == "rr100_b10":
         return len(wl["graphs"])
-    return 1
+    return wl.get("step_fraction", 1.0)
 
 
 def _node_ops(code):
@@ -220,7 +237,8 @@ def run_cpu_baseline(tb, orc, wl, budget_s: float):
         best = (code.n_nodes - 1, len(nodes), sub[-1], dt)
         rate = sub[-1] / dt
     j, nn, sops, dt = best
-    solves_per_s = (sops / dt) / total_ops * expected_answer(wl)
+    graphs = len(wl["graphs"]) if wl["name"] == "rr100_b10" else 1
+    solves_per_s = (sops / dt) / total_ops * graphs
     sample = (f"subtree of {nn} of {code.n_nodes} contraction nodes of the first network ({sops:.3g} of "
               f"{total_ops:.3g} tropical ops per step) in {dt:.2f}s; solves/s extrapolated by algorithmic ops")
     return {"value": solves_per_s, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
@@ -237,6 +255,8 @@ def main():
     ap.add_argument("--mode", default="batched", choices=["batched", "layered", "plain"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--compare-plain", action="store_true")
+    ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--make", nargs="*")
     args = ap.parse_args()
 
@@ -249,6 +269,13 @@ def main():
         return
 
     ws, rank, local = dist_env()
+    if args.config == "serve":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable":
+                                  "the reference has no serving loop (dynamic_ob_mis solves one request at a time)"}))
+            return
+        return run_serve(tb, args)
     wl = load_workload(tb, args.config)
     units = expected_answer(wl)
 
@@ -364,6 +391,20 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if args.compare_plain and args.mode != "plain":
+        # the drop-in path on the same items: one item at a time, per-node launches
+        t0 = time.perf_counter()
+        n_pl = max(1, min(args.steps, 3))
+        pl_ms = 0.0
+        for _ in range(n_pl):
+            flush.zero_()
+            torch.cuda.synchronize()
+            o, m = eng.solve_batch(plans, slice_vals=svs, r=rs, mode="plain")
+            assert m == mx0
+            pl_ms += eng.last_timing()[0]
+        plain_value = n_pl * units / (pl_ms / 1000.0)
+        res["plain"] = {"value": plain_value, "unit": "solves/s", "ms_per_step": pl_ms / n_pl,
+                        "speedup_vs_plain": value / plain_value}
     if not args.no_cpu_baseline:
         orc = _ge.load_oracle()
         orc.build()
@@ -371,6 +412,49 @@ def main():
     print(json.dumps(res))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_serve(tb, args):
+    """Serving mix: capacity with every request queued at once, then Poisson
+    arrivals at 0.8x that capacity; p50/p99 submit-to-result latency."""
+    from tensorbranching_gb300 import serving
+
+    mix = serving.serving_mix(args.requests, seed=11)
+    eng = tb.Engine()
+    t0 = time.perf_counter()
+    preps = [serving.prepare(eng, g, w, sc_cap=24.0, seed=i, name=nm) for i, (nm, g, w) in enumerate(mix)]
+    prep_s = time.perf_counter() - t0
+    # results served alone (reference values for the mix)
+    alone = []
+    for p in preps:
+        if p.constant is not None:
+            alone.append(p.constant)
+        else:
+            alone.append(eng.solve_batch(p.plans, slice_vals=p.slice_vals, r=np.array(p.r, np.float32),
+                                         mode="batched")[1])
+    with serving.Server(eng, pool_bytes=64 << 30, max_items=1 << 16) as srv:
+        warm = serving.run_poisson(srv, preps[: min(4, len(preps))], rate=0.0)
+        cap = serving.run_poisson(srv, preps, rate=0.0)
+        capacity = len(preps) / cap["wall_s"]
+        rate = 0.8 * capacity
+        with ClockSampler(0) as clk:
+            run = serving.run_poisson(srv, preps, rate=rate, seed=5)
+        st = srv.stats()
+    assert run["values"] == alone and cap["values"] == alone, "served results differ from results alone"
+    lat = np.array(run["latency_ms"])
+    res = {"metric": METRIC, "value": len(preps) / run["wall_s"], "unit": "solves/s", "n_gpus": 1,
+           "steps": len(preps), "warmup": len(warm["values"]), "ms_per_step": 1000.0 * run["wall_s"] / len(preps),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic serving mix (seeded)",
+           "config": {"workload": "serve", "requests": len(preps),
+                      "detail": "Poisson arrivals at 0.8x measured capacity; 3-regular n in [60,400] and KSG L in "
+                                "[10,36] filling 0.8; unit or U{1..10} weights; sc capped at 24 by index slicing",
+                      "arrival_rate_per_s": rate, "capacity_solves_per_s": capacity,
+                      "items": int(sum(p.n_items for p in preps)), "host_prep_s": prep_s},
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "mean": float(lat.mean()), "max": float(lat.max())},
+           "server": st, "same_alone_and_in_mix": True, "clocks": clk.summary()}
+    print(json.dumps(res))
 
 
 def _weights_of(wl, plan):

@@ -196,6 +196,35 @@ tb_status tb_gemm_device(tb_ctx* ctx, int64_t M, int64_t N, int64_t K, int64_t b
                          const void* A, const void* B, void* C, void* stream);
 
 /*
+ * Serving: continuous batching of MIS requests on one context.
+ *
+ * tb_serve_start starts a device-owner thread with a device pool of
+ * pool_bytes (0: half the context budget) and at most max_items items in
+ * flight (0: 4096).  tb_submit queues a request of n items (plans with their
+ * slice values and r, as in tb_solve_batch) and returns at once; any thread
+ * may submit, poll and wait.  The owner thread admits queued requests as pool
+ * memory and item slots free up, and then runs steps: one step executes, for
+ * every admitted item, the contraction steps of its current tree level, so
+ * requests that arrive while others run overlap with them on the device.  A
+ * request's result is the max over its items (as contract_slices + maximum,
+ * src/dynamic_ob.jl:24-27).  Plans must outlive their requests and must not
+ * be re-bound while a request uses them; while a server runs, call
+ * tb_solve_batch on another context.  Has no single counterpart in the
+ * reference (its requests are solved one at a time by dynamic_ob_mis).
+ */
+typedef struct tb_request tb_request;
+tb_status tb_serve_start(tb_ctx* ctx, int64_t pool_bytes, int32_t max_items);
+tb_status tb_serve_stop(tb_ctx* ctx);
+tb_status tb_submit(tb_ctx* ctx, int32_t n, tb_plan* const* plans, const int8_t* slice_vals, const float* r,
+                    tb_request** out);
+tb_status tb_poll(tb_request* req, int32_t* done);
+/* Wait up to timeout_ms (negative: no limit); result and submit-to-done
+ * latency in milliseconds. */
+tb_status tb_wait(tb_request* req, int32_t timeout_ms, float* out_max, double* latency_ms);
+void tb_request_free(tb_request* req);
+tb_status tb_serve_stats(tb_ctx* ctx, int64_t* steps, int64_t* launches, int64_t* completed, int64_t* active);
+
+/*
  * tb_solve_static -- has no counterpart in the reference.
  *
  * One MIS contraction that allocates no device memory, for callers that

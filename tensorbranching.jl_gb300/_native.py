@@ -83,6 +83,13 @@ ENGINE_SIGNATURES = {
                                  c_void_p]),
     "tb_solve_static": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
+    "tb_serve_start": (c_int32, [c_void_p, c_int64, c_int32]),
+    "tb_serve_stop": (c_int32, [c_void_p]),
+    "tb_submit": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, POINTER(c_void_p)]),
+    "tb_poll": (c_int32, [c_void_p, POINTER(c_int32)]),
+    "tb_wait": (c_int32, [c_void_p, c_int32, POINTER(c_float), POINTER(c_double)]),
+    "tb_request_free": (None, [c_void_p]),
+    "tb_serve_stats": (c_int32, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
 }
 
 ORDER_SIGNATURES = {
@@ -94,6 +101,7 @@ ORDER_SIGNATURES = {
                                       c_void_p]),
     "tbo_treesa": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_double, c_double,
                              c_double, c_void_p, c_int32, c_int32, c_int32, c_int32, c_uint64, c_void_p]),
+    "tbo_greedy_tree": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_void_p, c_uint64, c_void_p]),
     "tbo_greedy_slice": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_double,
                                    c_int32, c_void_p, c_void_p, c_void_p]),
 }

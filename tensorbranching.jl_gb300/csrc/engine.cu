@@ -139,25 +139,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_level(const ItemDev<T>* items, 
   }
 }
 
-// Persistent executor.  Tickets are handed out in dependency order, so a
-// ticket only waits on tickets already held by running CTAs; every wait is
+// Persistent executor.  Chunks of tiles are handed out in dependency order,
+// so a chunk only waits on chunks already held by running CTAs; every wait is
 // bounded by timeout_ns and ends with err set instead of hanging.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_persistent(const ItemDev<T>* items, const Group* groups, int n_groups,
-                                                        int64_t n_tickets, int* done, unsigned long long* ticket,
-                                                        int* err, float* out_item, const float* r,
-                                                        int64_t timeout_ns) {
+__global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* items, const Group* groups,
+                                                           const Chunk* chunks, int64_t n_chunks, int* done,
+                                                           unsigned long long* ticket, int* err, float* out_item,
+                                                           const float* r, int64_t timeout_ns) {
   extern __shared__ int tb_smem[];
-  __shared__ long long s_tk;
-  __shared__ int s_g, s_stop;
+  __shared__ long long s_c;
+  __shared__ int s_stop;
   for (;;) {
     if (threadIdx.x == 0) {
-      long long tk = (long long)atomicAdd(ticket, 1ull);
-      int stop = (tk >= n_tickets) || (*(volatile int*)err != 0);
-      int gi = 0;
+      long long c = (long long)atomicAdd(ticket, 1ull);
+      int stop = (c >= n_chunks) || (*(volatile int*)err != 0);
       if (!stop) {
-        gi = find_group(groups, n_groups, tk);
-        const Group g = groups[gi];
+        const Group g = groups[chunks[c].group];
         const ItemDev<T>& it = items[g.item];
         const Step st = it.steps[g.step];
         const int deps[2] = {st.dep0, st.dep1};
@@ -177,18 +175,23 @@ __global__ void __launch_bounds__(kThreads) k_persistent(const ItemDev<T>* items
           }
         }
       }
-      s_tk = tk;
-      s_g = gi;
+      s_c = c;
       s_stop = stop;
     }
     __syncthreads();
     if (s_stop) break;
-    const Group g = groups[s_g];
+    const Chunk ch = chunks[s_c];
+    const Group g = groups[ch.group];
     const ItemDev<T>& it = items[g.item];
-    run_step<T>(it, it.steps[g.step], s_tk - g.first, tb_smem, out_item, r, g.item, err);
+    const Step& st = it.steps[g.step];
+    if (st.kind == STEP_TILE) {
+      stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem);
+    } else {
+      for (int64_t x = ch.t0; x < ch.t1; x++) run_step<T>(it, st, x, tb_smem, out_item, r, g.item, err);
+    }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(done + it.done_base + g.step, 1);
+    if (threadIdx.x == 0) atomicAdd(done + it.done_base + g.step, (int)(ch.t1 - ch.t0));
   }
 }
 
@@ -287,13 +290,14 @@ struct tb_ctx {
   int persistent_ctas = 0;
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   size_t budget = 0;
-  DevBuf arena, items, groups, done, misc, slice_vals, out_item, rvals;
-  HostBuf h_items, h_groups, h_in, h_out;
+  DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals;
+  HostBuf h_items, h_groups, h_chunks, h_in, h_out;
   // batch state of the last upload (reused when the same plans come again)
   GraphKey key;
   bool have_key = false;
   int64_t n_tickets = 0;
   int n_groups = 0;
+  int64_t n_chunks = 0;
   struct LevelRange {
     int64_t first, count;
     int kinds;  // 1 stream-like, 2 GEMM
@@ -480,6 +484,28 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   }
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
+  // chunks for the persistent executor: runs of stream tiles (tables are
+  // built once per chunk), single GEMM tiles, whole leaf / final steps
+  std::vector<Chunk> chs;
+  for (size_t g = 0; g < gk.size(); g++) {
+    const Step& st = plans[gk[g].item]->h.steps[gk[g].step];
+    const int64_t nt = st.n_tiles;
+    int64_t cs = 1;
+    if (st.kind == STEP_TILE) cs = std::max<int64_t>(1, std::min<int64_t>(256, (nt + c->persistent_ctas - 1) / c->persistent_ctas));
+    else if (st.kind == STEP_LEAVES) cs = nt;
+    for (int64_t t0 = 0; t0 < nt; t0 += cs) {
+      Chunk ch;
+      ch.group = (int32_t)g;
+      ch.pad_ = 0;
+      ch.t0 = t0;
+      ch.t1 = std::min(nt, t0 + cs);
+      chs.push_back(ch);
+    }
+  }
+  c->n_chunks = (int64_t)chs.size();
+  CU(c->chunks.ensure(sizeof(Chunk) * std::max<size_t>(chs.size(), 1)));
+  CU(cudaMemcpyAsync(c->chunks.p, chs.data(), sizeof(Chunk) * chs.size(), cudaMemcpyHostToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
   CU(c->items.ensure(sizeof(ItemDev<T>) * n));
   CU(c->groups.ensure(sizeof(Group) * std::max<size_t>(gk.size(), 1)));
   CU(c->done.ensure(sizeof(int) * std::max(done_base, 1) + 64));
@@ -510,9 +536,10 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
     int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
     int64_t timeout_ns = (int64_t)c->opt.timeout_ms * 1000000LL;
-    k_persistent<T><<<c->persistent_ctas, kThreads, smem, s>>>(items, groups, c->n_groups, c->n_tickets,
-                                                               reinterpret_cast<int*>(c->done.p), ticket, err,
-                                                               out_item, rv, timeout_ns);
+    k_persistent<T><<<c->persistent_ctas, kThreads, smem, s>>>(items, groups,
+                                                               reinterpret_cast<const Chunk*>(c->chunks.p),
+                                                               c->n_chunks, reinterpret_cast<int*>(c->done.p),
+                                                               ticket, err, out_item, rv, timeout_ns);
     CU(cudaGetLastError());
     launches++;
   } else {
@@ -1223,3 +1250,437 @@ extern "C" int32_t tbi_measure_maxplus_peak(int32_t device, double* ops_per_s) {
   *ops_per_s = (double)blocks * 256 * iters * 16 * 2 * 2 / (best * 1e-3);
   return TB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Serving: continuous batching at tree-level granularity.
+//
+// A device-owner thread admits submitted requests while their arenas fit in
+// a device pool and the active-item limit allows, then repeats steps: one
+// step runs, for every active item, the steps of its current tree level --
+// stream-like tiles in one launch, GEMM tiles in another -- so an item that
+// arrived a moment ago runs its leaves while older items run deeper levels.
+// Finished items release their arena at once and their request completes
+// when its last item does.
+// ---------------------------------------------------------------------------
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+
+struct tb_request {
+  struct Item {
+    tb_plan* plan;
+    std::vector<int8_t> sv;
+    float r;
+  };
+  std::vector<Item> items;
+  int items_left = 0;
+  float result = -INFINITY;
+  tb_status status = TB_OK;
+  std::string err;
+  int state = 0;  // 0 queued, 1 running, 2 done
+  double t_submit = 0, t_start = 0, t_done = 0;
+  std::mutex m;
+  std::condition_variable cv;
+};
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// first-fit allocator over [0, size) in elements
+struct PoolAlloc {
+  std::map<int64_t, int64_t> free_;  // offset -> length
+  void reset(int64_t size) {
+    free_.clear();
+    free_[0] = size;
+  }
+  int64_t alloc(int64_t n) {
+    n = (n + 63) / 64 * 64;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        int64_t off = it->first, len = it->second;
+        free_.erase(it);
+        if (len > n) free_[off + n] = len - n;
+        return off;
+      }
+    }
+    return -1;
+  }
+  void release(int64_t off, int64_t n) {
+    n = (n + 63) / 64 * 64;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+};
+
+}  // namespace
+
+struct Server {
+  tb_ctx* ctx = nullptr;
+  std::thread th;
+  std::atomic<bool> stop{false};
+  std::mutex qm;
+  std::condition_variable qcv;
+  std::deque<tb_request*> pending;
+  cudaStream_t stream = nullptr;
+  DevBuf pool, items, groups, sv, rv, out, err;
+  HostBuf h_items, h_groups, h_sv, h_rv, h_out;
+  PoolAlloc palloc;
+  int64_t pool_elems = 0;
+  int max_items = 0;
+  struct Active {
+    tb_request* req;
+    int idx;
+    tb_plan* plan;
+    int64_t off, elems;
+    int level;
+  };
+  std::vector<Active> active;
+  std::atomic<int64_t> steps{0}, launches{0}, completed{0};
+  std::string fatal;
+};
+
+template <typename T>
+static void serve_finish(Server* S, tb_request* q) {
+  std::lock_guard<std::mutex> lk(q->m);
+  q->t_done = now_s();
+  q->state = 2;
+  q->cv.notify_all();
+}
+
+template <typename T>
+static tb_status serve_step(Server* S) {
+  tb_ctx* c = S->ctx;
+  const int n = (int)S->active.size();
+  // item table
+  CU(S->h_items.ensure(sizeof(ItemDev<T>) * n));
+  CU(S->items.ensure(sizeof(ItemDev<T>) * n));
+  size_t svn = 0;
+  for (auto& a : S->active) svn += a.req->items[a.idx].sv.size();
+  CU(S->h_sv.ensure(std::max<size_t>(svn, 16)));
+  CU(S->sv.ensure(std::max<size_t>(svn, 16)));
+  CU(S->h_rv.ensure(sizeof(float) * n));
+  CU(S->rv.ensure(sizeof(float) * n));
+  CU(S->h_out.ensure(sizeof(float) * n));
+  CU(S->out.ensure(sizeof(float) * n));
+  ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(S->h_items.p);
+  int8_t* hsv = reinterpret_cast<int8_t*>(S->h_sv.p);
+  float* hr = reinterpret_cast<float*>(S->h_rv.p);
+  size_t so = 0;
+  for (int i = 0; i < n; i++) {
+    const auto& a = S->active[i];
+    const auto& qi = a.req->items[a.idx];
+    tb_plan* p = a.plan;
+    ItemDev<T> it{};
+    it.arena = reinterpret_cast<T*>(S->pool.p) + a.off;
+    it.steps = reinterpret_cast<const Step*>(p->d_steps.p);
+    it.tiles = reinterpret_cast<const TileDesc*>(p->d_tiles.p);
+    it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
+    it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
+    it.slice_vals = reinterpret_cast<const int8_t*>(S->sv.p) + so;
+    it.r = 0.0f;
+    it.n_leaves = p->h.n_tensors;
+    it.done_base = 0;
+    it.n_steps = (int)p->h.steps.size();
+    it.fin = p->h.fin;
+    hi[i] = it;
+    if (!qi.sv.empty()) std::memcpy(hsv + so, qi.sv.data(), qi.sv.size());
+    so += qi.sv.size();
+    hr[i] = qi.r;
+  }
+  // groups of this step: kind 1 first, then kind 2
+  std::vector<Group> g1, g2;
+  int64_t t1 = 0, t2 = 0;
+  for (int i = 0; i < n; i++) {
+    const auto& a = S->active[i];
+    const PlanHost& h = a.plan->h;
+    for (int32_t si : h.levels[a.level]) {
+      const Step& st = h.steps[si];
+      if (st.kind == STEP_GEMM) {
+        g2.push_back({i, si, t2});
+        t2 += st.n_tiles;
+      } else {
+        g1.push_back({i, si, t1});
+        t1 += st.n_tiles;
+      }
+    }
+  }
+  const size_t ng = g1.size() + g2.size();
+  CU(S->h_groups.ensure(sizeof(Group) * std::max<size_t>(ng, 1)));
+  CU(S->groups.ensure(sizeof(Group) * std::max<size_t>(ng, 1)));
+  Group* hg = reinterpret_cast<Group*>(S->h_groups.p);
+  std::copy(g1.begin(), g1.end(), hg);
+  std::copy(g2.begin(), g2.end(), hg + g1.size());
+  cudaStream_t s = S->stream;
+  CU(cudaMemcpyAsync(S->items.p, hi, sizeof(ItemDev<T>) * n, cudaMemcpyHostToDevice, s));
+  if (svn) CU(cudaMemcpyAsync(S->sv.p, hsv, svn, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(S->rv.p, hr, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(S->groups.p, hg, sizeof(Group) * ng, cudaMemcpyHostToDevice, s));
+  CU(cudaMemsetAsync(S->err.p, 0, 16, s));
+  const ItemDev<T>* di = reinterpret_cast<const ItemDev<T>*>(S->items.p);
+  const Group* dg = reinterpret_cast<const Group*>(S->groups.p);
+  float* dout = reinterpret_cast<float*>(S->out.p);
+  const float* drv = reinterpret_cast<const float*>(S->rv.p);
+  int* derr = reinterpret_cast<int*>(S->err.p);
+  if (t1 > 0) {
+    const int64_t grid = std::min<int64_t>(t1, c->stream_ctas);
+    k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), s>>>(di, dg, (int)g1.size(), 0, t1, (t1 + grid - 1) / grid,
+                                                                   dout, drv, derr);
+    CU(cudaGetLastError());
+    S->launches++;
+  }
+  if (t2 > 0) {
+    if (t2 > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "step too large for one launch");
+    k_level<T, 2><<<(unsigned)t2, kThreads, smem_bytes(2), s>>>(di, dg + g1.size(), (int)g2.size(), 0, t2, 1, dout,
+                                                                drv, derr);
+    CU(cudaGetLastError());
+    S->launches++;
+  }
+  CU(cudaMemcpyAsync(S->h_out.p, dout, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  int herr = 0;
+  CU(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  S->steps++;
+  if (herr) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
+  // advance every item; collect finished ones
+  const float* ho = reinterpret_cast<const float*>(S->h_out.p);
+  std::vector<Server::Active> keep;
+  for (int i = 0; i < n; i++) {
+    Server::Active a = S->active[i];
+    a.level++;
+    if (a.level >= (int)a.plan->h.levels.size()) {
+      tb_request* q = a.req;
+      q->result = std::max(q->result, ho[i]);
+      S->palloc.release(a.off, a.elems);
+      if (--q->items_left == 0) {
+        serve_finish<T>(S, q);
+        S->completed++;
+      }
+    } else {
+      keep.push_back(a);
+    }
+  }
+  S->active.swap(keep);
+  return TB_OK;
+}
+
+template <typename T>
+static void serve_loop(Server* S) {
+  cudaSetDevice(S->ctx->device);
+  while (true) {
+    {
+      std::unique_lock<std::mutex> lk(S->qm);
+      // admit while slots and memory allow
+      while (!S->pending.empty()) {
+        tb_request* q = S->pending.front();
+        if ((int)(S->active.size() + q->items.size()) > S->max_items && !S->active.empty()) break;
+        std::vector<Server::Active> adm;
+        bool ok = true;
+        for (int k = 0; k < (int)q->items.size(); k++) {
+          tb_plan* p = q->items[k].plan;
+          int64_t off = S->palloc.alloc(p->h.arena_elems);
+          if (off < 0) {
+            ok = false;
+            break;
+          }
+          adm.push_back({q, k, p, off, p->h.arena_elems, 0});
+        }
+        if (!ok) {
+          for (auto& a : adm) S->palloc.release(a.off, a.elems);
+          if (S->active.empty()) {
+            // cannot fit even alone: fail the request
+            S->pending.pop_front();
+            std::lock_guard<std::mutex> lq(q->m);
+            q->status = TB_ERR_OOM;
+            q->err = "request needs more device memory than the serving pool";
+            q->state = 2;
+            q->t_done = now_s();
+            q->cv.notify_all();
+            continue;
+          }
+          break;
+        }
+        S->pending.pop_front();
+        {
+          std::lock_guard<std::mutex> lq(q->m);
+          q->state = 1;
+          q->t_start = now_s();
+        }
+        for (auto& a : adm) S->active.push_back(a);
+      }
+      if (S->active.empty()) {
+        if (S->stop) break;
+        S->qcv.wait_for(lk, std::chrono::milliseconds(2));
+        continue;
+      }
+    }
+    tb_status st = serve_step<T>(S);
+    if (st != TB_OK) {
+      // fail every active request; the server keeps running
+      std::string msg = g_err;
+      for (auto& a : S->active) {
+        S->palloc.release(a.off, a.elems);
+        tb_request* q = a.req;
+        std::lock_guard<std::mutex> lq(q->m);
+        if (q->state != 2) {
+          q->status = st;
+          q->err = msg;
+          q->state = 2;
+          q->t_done = now_s();
+          q->cv.notify_all();
+        }
+      }
+      S->active.clear();
+    }
+  }
+}
+
+static std::map<tb_ctx*, Server*> g_servers;
+static std::mutex g_servers_mu;
+
+extern "C" {
+
+tb_status tb_serve_start(tb_ctx* c, int64_t pool_bytes, int32_t max_items) {
+  if (!c) return fail(TB_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lk(g_servers_mu);
+  if (g_servers.count(c)) return fail(TB_ERR_INVALID, "server already running on this context");
+  CU(cudaSetDevice(c->device));
+  tb_status st = c->opt.dtype == TB_DTYPE_F32 ? set_kernel_attrs<float>() : set_kernel_attrs<int32_t>();
+  if (st) return st;
+  std::unique_ptr<Server> S(new Server());
+  S->ctx = c;
+  if (pool_bytes <= 0) pool_bytes = (int64_t)(c->budget / 2);
+  S->pool_elems = pool_bytes / 4;
+  S->max_items = max_items > 0 ? max_items : 4096;
+  CU(S->pool.ensure((size_t)S->pool_elems * 4));
+  CU(S->err.ensure(64));
+  S->palloc.reset(S->pool_elems);
+  CU(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  Server* raw = S.release();
+  raw->th = c->opt.dtype == TB_DTYPE_F32 ? std::thread(serve_loop<float>, raw) : std::thread(serve_loop<int32_t>, raw);
+  g_servers[c] = raw;
+  return TB_OK;
+}
+
+tb_status tb_serve_stop(tb_ctx* c) {
+  Server* S = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_servers_mu);
+    auto it = g_servers.find(c);
+    if (it == g_servers.end()) return fail(TB_ERR_INVALID, "no server on this context");
+    S = it->second;
+    g_servers.erase(it);
+  }
+  {
+    std::lock_guard<std::mutex> lk(S->qm);
+    S->stop = true;
+  }
+  S->qcv.notify_all();
+  S->th.join();  // drains admitted work; requests still queued are failed below
+  for (tb_request* q : S->pending) {
+    std::lock_guard<std::mutex> lq(q->m);
+    q->status = TB_ERR_INVALID;
+    q->err = "server stopped";
+    q->state = 2;
+    q->cv.notify_all();
+  }
+  cudaStreamDestroy(S->stream);
+  delete S;
+  return TB_OK;
+}
+
+tb_status tb_submit(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8_t* slice_vals, const float* r,
+                    tb_request** out) {
+  if (!c || !out || n <= 0 || !plans) return fail(TB_ERR_INVALID, "bad arguments");
+  *out = nullptr;
+  Server* S = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_servers_mu);
+    auto it = g_servers.find(c);
+    if (it == g_servers.end()) return fail(TB_ERR_INVALID, "no server on this context (tb_serve_start)");
+    S = it->second;
+  }
+  std::unique_ptr<tb_request> q(new tb_request());
+  size_t so = 0;
+  for (int i = 0; i < n; i++) {
+    tb_plan* p = plans[i];
+    if (!p || p->ctx != c) return fail(TB_ERR_INVALID, "plan of another context");
+    if (!p->h.has_weights) return fail(TB_ERR_INVALID, "plan has no bound weights");
+    tb_request::Item it;
+    it.plan = p;
+    size_t k = p->h.sliced.size();
+    if (k && !slice_vals) return fail(TB_ERR_INVALID, "slice_vals required");
+    if (k) it.sv.assign(slice_vals + so, slice_vals + so + k);
+    for (int8_t v : it.sv)
+      if (v != 0 && v != 1) return fail(TB_ERR_INVALID, "slice values must be 0 or 1");
+    so += k;
+    it.r = r ? r[i] : 0.0f;
+    q->items.push_back(std::move(it));
+  }
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    tb_status st = TB_OK;
+    for (auto& it : q->items)
+      if ((st = upload_plan(it.plan))) return st;
+  }
+  q->items_left = n;
+  q->t_submit = now_s();
+  tb_request* raw = q.release();
+  {
+    std::lock_guard<std::mutex> lk(S->qm);
+    S->pending.push_back(raw);
+  }
+  S->qcv.notify_all();
+  *out = raw;
+  return TB_OK;
+}
+
+tb_status tb_poll(tb_request* q, int32_t* done) {
+  if (!q || !done) return fail(TB_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(q->m);
+  *done = q->state == 2;
+  return TB_OK;
+}
+
+tb_status tb_wait(tb_request* q, int32_t timeout_ms, float* out_max, double* latency_ms) {
+  if (!q) return fail(TB_ERR_INVALID, "null request");
+  std::unique_lock<std::mutex> lk(q->m);
+  if (!q->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms < 0 ? 1 << 30 : timeout_ms),
+                      [&] { return q->state == 2; }))
+    return fail(TB_ERR_TIMEOUT, "request not finished within the timeout");
+  if (q->status != TB_OK) return fail(q->status, q->err);
+  if (out_max) *out_max = q->result;
+  if (latency_ms) *latency_ms = (q->t_done - q->t_submit) * 1000.0;
+  return TB_OK;
+}
+
+void tb_request_free(tb_request* q) { delete q; }
+
+tb_status tb_serve_stats(tb_ctx* c, int64_t* steps, int64_t* launches, int64_t* completed, int64_t* active) {
+  std::lock_guard<std::mutex> lk(g_servers_mu);
+  auto it = g_servers.find(c);
+  if (it == g_servers.end()) return fail(TB_ERR_INVALID, "no server on this context");
+  Server* S = it->second;
+  if (steps) *steps = S->steps;
+  if (launches) *launches = S->launches;
+  if (completed) *completed = S->completed;
+  if (active) *active = (int64_t)S->active.size();
+  return TB_OK;
+}
+
+}  // extern "C"

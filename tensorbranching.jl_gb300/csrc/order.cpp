@@ -447,9 +447,117 @@ std::vector<std::vector<char>> label_graph(const Tree& t) {
   return adj;
 }
 
+// ---------------------------------------------------------------------------
+// greedy pairwise contraction (the GreedyMethod of OMEinsumContractionOrders):
+// repeatedly contract the pair of tensors sharing a label whose result grows
+// the least, size(out) - size(a) - size(b), ties broken at random
+// ---------------------------------------------------------------------------
+bool greedy_tree(Tree& t, uint64_t seed) {
+  const int T = t.T, w = t.S.w, L = t.L;
+  std::mt19937_64 rng(seed);
+  std::vector<int> cnt(L, 0);
+  std::vector<char> alive(2 * T - 1, 0);
+  for (int i = 0; i < T; i++) {
+    alive[i] = 1;
+    for (int l = 0; l < L; l++)
+      if (get_bit(t.S.at(i), l)) cnt[l]++;
+  }
+  const uint64_t* fiy = t.final_iy.at(0);
+  // label -> live tensors holding it
+  std::vector<std::vector<int>> holders(L);
+  for (int i = 0; i < T; i++)
+    for (int l = 0; l < L; l++)
+      if (get_bit(t.S.at(i), l)) holders[l].push_back(i);
+  int next = T;
+  std::vector<uint64_t> tmp(w);
+  auto out_set = [&](int a, int b, uint64_t* o) {
+    const uint64_t* sa = t.S.at(a);
+    const uint64_t* sb = t.S.at(b);
+    int sz = 0;
+    for (int k = 0; k < w; k++) {
+      uint64_t u = sa[k] | sb[k], keep = 0;
+      while (u) {
+        int bit = __builtin_ctzll(u);
+        u &= u - 1;
+        int l = k * 64 + bit;
+        int c = cnt[l] - (int)get_bit(sa, l) - (int)get_bit(sb, l);
+        if (c > 0 || get_bit(fiy, l)) keep |= 1ull << bit;
+      }
+      o[k] = keep;
+      sz += __builtin_popcountll(keep);
+    }
+    return sz;
+  };
+  int live = T;
+  while (live > 1) {
+    double best = INFINITY;
+    int ba = -1, bb = -1;
+    uint64_t bkey = 0;
+    for (int l = 0; l < L; l++) {
+      auto& hs = holders[l];
+      for (size_t x = 0; x < hs.size(); x++)
+        for (size_t y = x + 1; y < hs.size(); y++) {
+          int a = hs[x], b = hs[y];
+          int so = out_set(a, b, tmp.data());
+          double cost = std::exp2((double)so) - std::exp2((double)t.sc(a)) - std::exp2((double)t.sc(b));
+          uint64_t key = rng();
+          if (cost < best || (cost == best && key < bkey)) {
+            best = cost;
+            ba = a;
+            bb = b;
+            bkey = key;
+          }
+        }
+    }
+    if (ba < 0) {
+      // no shared label left: merge the two smallest live tensors
+      std::vector<int> ls;
+      for (int i = 0; i < next; i++)
+        if (alive[i]) ls.push_back(i);
+      std::sort(ls.begin(), ls.end(), [&](int x, int y) { return t.sc(x) < t.sc(y); });
+      ba = ls[0];
+      bb = ls[1];
+    }
+    int n = next++;
+    t.left[n] = ba;
+    t.right[n] = bb;
+    t.parent[ba] = n;
+    t.parent[bb] = n;
+    out_set(ba, bb, t.S.at(n));
+    for (int l = 0; l < L; l++) {
+      bool ina = get_bit(t.S.at(ba), l), inb = get_bit(t.S.at(bb), l);
+      if (!ina && !inb) continue;
+      cnt[l] -= (int)ina + (int)inb;
+      auto& hs = holders[l];
+      hs.erase(std::remove_if(hs.begin(), hs.end(), [&](int x) { return x == ba || x == bb; }), hs.end());
+      if (get_bit(t.S.at(n), l)) {
+        cnt[l]++;
+        hs.push_back(n);
+      }
+    }
+    alive[ba] = alive[bb] = 0;
+    alive[n] = 1;
+    live--;
+  }
+  t.root = next - 1;
+  return next == 2 * T - 1;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Greedy pairwise contraction tree (size-increase greedy, random ties).
+int tbo_greedy_tree(int n_tensors, const int* ix_off, const int* ix_lab, int n_labels, int n_iy, const int* iy,
+                    uint64_t seed, int* children) {
+  if (n_tensors < 1) return 1;
+  Tree t;
+  if (!load_leaves(t, n_tensors, ix_off, ix_lab, n_labels, n_iy, iy)) return 1;
+  if (n_tensors == 1) return 0;
+  if (!greedy_tree(t, seed)) return 1;
+  emit(t, children);
+  return 0;
+}
 
 // Contraction complexity of a tree: tc = log2 sum_n 2^{|labels(n)|},
 // sc = max log2 tensor size, rw = log2 of total read+write elements.

@@ -565,6 +565,8 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
   }
   Step fin{STEP_FINAL, 0, (int32_t)p.steps.size() - 1, -1, 1, p.steps.back().level + 1};
   p.steps.push_back(fin);
+  p.levels.assign(fin.level + 1, {});
+  for (size_t si = 0; si < p.steps.size(); si++) p.levels[p.steps[si].level].push_back((int32_t)si);
   p.total_tiles += 1;
   p.fin.root_off = root_off;
   p.fin.root_log2 = root_rank;

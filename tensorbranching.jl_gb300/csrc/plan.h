@@ -51,6 +51,7 @@ struct PlanHost {
   bool has_weights = false;
 
   std::vector<Step> steps;
+  std::vector<std::vector<int32_t>> levels;    // step indices of each level
   std::vector<TileDesc> tiles;
   std::vector<GemmDesc> gemms;
   std::vector<LeafDesc> leaves;

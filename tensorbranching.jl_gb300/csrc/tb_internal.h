@@ -109,4 +109,11 @@ struct Group {
   int64_t first;  // first ticket of this group
 };
 
+// A unit of work of the persistent executor: tiles [t0, t1) of one group.
+// Chunks are listed in dependency order.
+struct Chunk {
+  int32_t group, pad_;
+  int64_t t0, t1;
+};
+
 }  // namespace tb

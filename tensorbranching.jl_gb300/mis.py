@@ -36,11 +36,18 @@ class KernelResult:
     vmap: list[int]  # kernel vertex -> input vertex
 
 
-def kernelize(g: Graph, weights=None, verbose: int = 0) -> KernelResult:
+REDUCTIONS_ALL = ("isolated", "pendant", "domination")
+REDUCTIONS_BASIC = ("isolated", "pendant")
+
+
+def kernelize(g: Graph, weights=None, verbose: int = 0, rules=REDUCTIONS_ALL) -> KernelResult:
     """Apply exact MIS reductions until none applies:
     isolated vertex (take it if its weight is positive), pendant vertex v with
     neighbour u and w(v) >= w(u) (take v), and neighbourhood domination
-    N[u] within N[v] with w(u) >= w(v) (drop v)."""
+    N[u] within N[v] with w(u) >= w(v) (drop v).  ``rules`` selects a subset
+    (domination alone empties most King's subgraphs with unit weights)."""
+    use_dom = "domination" in rules
+    use_pend = "pendant" in rules
     w = weights_array(weights, g.n).astype(np.float64)
     adj = g.adjacency()
     for u, v in g.edges:
@@ -71,14 +78,14 @@ def kernelize(g: Graph, weights=None, verbose: int = 0) -> KernelResult:
                     r += w[v]
                 remove(v)
                 changed = True
-            elif len(nb) == 1:
+            elif len(nb) == 1 and use_pend:
                 u = next(iter(nb))
                 if w[v] >= w[u]:
                     r += w[v]
                     remove(u)
                     remove(v)
                     changed = True
-            else:
+            elif use_dom and len(nb) > 1:
                 closed_v = nb | {v}
                 for u in sorted(nb):
                     if w[u] >= w[v] and (adj[u] | {u}) <= closed_v:
@@ -103,6 +110,7 @@ class ContractionTreeSlicer:
     refiner: _order.TreeSA = field(default_factory=lambda: _order.TreeSA(
         betas=np.arange(1.0, 16.0, 1.0), ntrials=2, niters=30, nthreads=1))
     max_branches: int = 1 << 16
+    reductions: tuple = REDUCTIONS_ALL
 
 
 def eincode2order(code: CompressedEinsum) -> list[int]:
@@ -120,12 +128,17 @@ def eincode2order(code: CompressedEinsum) -> list[int]:
     return list(dict.fromkeys(eo))
 
 
+def update_order(code_old: CompressedEinsum, vmap: list[int]) -> list[int]:
+    """The old tree's elimination order mapped onto an induced subgraph
+    (update_order, src/decompose.jl:49-56)."""
+    inv = {old: new for new, old in enumerate(vmap)}
+    return [inv[v] for v in eincode2order(code_old) if v in inv]
+
+
 def update_code(g_new: Graph, code_old: CompressedEinsum, vmap: list[int]) -> CompressedEinsum:
     """Map the old tree's elimination order onto an induced subgraph and
     rebuild the tree (update_code, src/decompose.jl:96-100)."""
-    inv = {old: new for new, old in enumerate(vmap)}
-    eo = [inv[v] for v in eincode2order(code_old) if v in inv]
-    return _order.order2eincode(g_new, eo)
+    return _order.order2eincode(g_new, update_order(code_old, vmap))
 
 
 def _branch_vertex(code: CompressedEinsum, sc_target: float) -> int:
@@ -148,18 +161,20 @@ def _make_branch(g: Graph, w: np.ndarray, code: CompressedEinsum, r: float, remo
                  slicer: ContractionTreeSlicer) -> SlicedBranch:
     keep = [v for v in range(g.n) if v not in removed]
     sub, vmap = g.induced_subgraph(keep)
-    kr = kernelize(sub, w[vmap] if keep else np.zeros(0, np.float32))
+    kr = kernelize(sub, w[vmap] if keep else np.zeros(0, np.float32), rules=slicer.reductions)
     vmap2 = [vmap[i] for i in kr.vmap]
     r2 = r + kr.r
     if kr.g.n == 0:
-        return SlicedBranch(MISProblem(kr.g, kr.weights), None, r2)
-    new_code = update_code(kr.g, code, vmap2)
+        return SlicedBranch(MISProblem(kr.g, kr.weights), None, r2, vmap=vmap2)
+    eo = update_order(code, vmap2)
+    new_code = _order.order2eincode(kr.g, eo)
     if slicer.refine and new_code.complexity()[1] > slicer.sc_target:
         ref = slicer.refiner
         new_code = _order.treesa(new_code, _order.TreeSA(sc_target=slicer.sc_target, betas=ref.betas,
                                                          ntrials=ref.ntrials, niters=ref.niters,
                                                          seed=ref.seed, nthreads=ref.nthreads))
-    return SlicedBranch(MISProblem(kr.g, kr.weights), new_code, r2)
+        eo = None
+    return SlicedBranch(MISProblem(kr.g, kr.weights), new_code, r2, order=eo, vmap=vmap2)
 
 
 def slice(p: MISProblem, code: CompressedEinsum, r: float, slicer: ContractionTreeSlicer,
@@ -182,8 +197,11 @@ def slice(p: MISProblem, code: CompressedEinsum, r: float, slicer: ContractionTr
         w = b.p.weight_array()
         v = _branch_vertex(b.code, slicer.sc_target)
         nbv = set(g.neighbors(v))
-        todo.append(_make_branch(g, w, b.code, b.r, {v}, slicer))
-        todo.append(_make_branch(g, w, b.code, b.r + float(w[v]), nbv | {v}, slicer))
+        base = b.vmap if b.vmap is not None else list(range(g.n))
+        for child in (_make_branch(g, w, b.code, b.r, {v}, slicer),
+                      _make_branch(g, w, b.code, b.r + float(w[v]), nbv | {v}, slicer)):
+            child.vmap = [base[x] for x in child.vmap]  # relative to the graph slice() was given
+            todo.append(child)
     if verbose:
         scs = [x.sc() for x in done]
         print(f"branches: {len(done)}, max sc: {max(scs) if scs else 0}")

@@ -207,6 +207,8 @@ class SlicedBranch:
     r: float = 0.0
     sliced: list[int] = field(default_factory=list)      # labels fixed per item
     slice_values: np.ndarray | None = None               # (n_items, len(sliced)) int8
+    order: list[int] | None = None                       # elimination order the tree was built from
+    vmap: list[int] | None = None                        # branch vertex -> vertex of the sliced graph
 
     def complexity(self) -> tuple[float, float, float]:
         if self.code is None:
@@ -222,4 +224,5 @@ class SlicedBranch:
 
 def add_r(branch: SlicedBranch, r: float) -> SlicedBranch:
     """add_r (src/types.jl:113)."""
-    return SlicedBranch(branch.p, branch.code, branch.r + r, branch.sliced, branch.slice_values)
+    return SlicedBranch(branch.p, branch.code, branch.r + r, branch.sliced, branch.slice_values, branch.order,
+                        branch.vmap)

@@ -105,6 +105,21 @@ def order2eincode(g: Graph, eo) -> CompressedEinsum:
     return tree_from_order(ixs, iy, g.n, [v for v in eo if 0 <= v < g.n])
 
 
+def greedy_tree(ixs, iy, n_labels: int, seed: int = 0) -> CompressedEinsum:
+    """Greedy pairwise contraction tree (contract the pair whose result grows
+    the least first; OMEinsumContractionOrders GreedyMethod)."""
+    lib = _native.order_lib()
+    T = len(ixs)
+    tmp = CompressedEinsum(ixs, iy, np.zeros((max(T - 1, 0), 2), np.int32), n_labels=n_labels)
+    off, lab, iya = _args(tmp)
+    ch = np.zeros((max(T - 1, 1), 2), np.int32)
+    rc = lib.tbo_greedy_tree(T, off.ctypes.data, lab.ctypes.data, n_labels, len(iy), iya.ctypes.data, seed,
+                             ch.ctypes.data)
+    if rc:
+        raise ValueError("greedy_tree failed")
+    return CompressedEinsum(ixs, iy, ch[: max(T - 1, 0)], n_labels=n_labels)
+
+
 def treesa(code: CompressedEinsum, opt: TreeSA) -> CompressedEinsum:
     """Refine a tree with simulated annealing; returns a new plan."""
     if code.n_tensors <= 2:

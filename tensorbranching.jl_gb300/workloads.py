@@ -38,7 +38,8 @@ WORKLOADS = {
     "rr100_b10": "32 random 3-regular graphs n=100 (seeds 1..32), unit weights, branched to sc<=10",
     "rr220": "random 3-regular n=220 (seed 1), unit weights, one contraction, no slicing",
     "rr300_s22": "random 3-regular n=300 (seed 3), weights U{1..10}, index-sliced to sc<=22",
-    "ksg32_b20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, branched to sc<=20",
+    "ksg32_b20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, isolated/pendant reductions, "
+                 "branched to sc<=20",
 }
 
 
@@ -96,55 +97,107 @@ def build_rr300_s22() -> dict:
             "sliced": sliced, "sliced_cc": list(cc)}
 
 
-def _branched(g: Graph, w, sc_target: int, seed: int) -> list[SlicedBranch]:
-    kr = _mis.kernelize(g, w)
+def _pack_branches(brs: list[SlicedBranch]) -> dict:
+    """Branches of one graph as flat int arrays: the kept vertices of the
+    kernel graph (vmap), the elimination order each tree was built from, and
+    r.  Trees are rebuilt by order2eincode (integer-deterministic)."""
+    vm, vo, eo, eoo, rs, has = [], [0], [], [0], [], []
+    for b in brs:
+        vm.extend(b.vmap if b.vmap is not None else [])
+        vo.append(len(vm))
+        if b.code is not None and b.order is None:
+            raise ValueError("branch tree was re-annealed: its elimination order is not stored")
+        eo.extend(b.order if b.order is not None else [])
+        eoo.append(len(eo))
+        rs.append(b.r)
+        has.append(b.code is not None)
+    return {"vmap": np.array(vm, np.int32), "vmap_off": np.array(vo, np.int64), "order": np.array(eo, np.int32),
+            "order_off": np.array(eoo, np.int64), "r": np.array(rs, np.float64), "has_code": np.array(has, bool)}
+
+
+def _unpack_branches(kernel_g: Graph, kernel_w: np.ndarray, d) -> list[SlicedBranch]:
+    out = []
+    for i in range(len(d["r"])):
+        vm = d["vmap"][d["vmap_off"][i]:d["vmap_off"][i + 1]].tolist()
+        g, _ = kernel_g.induced_subgraph(vm)
+        w = kernel_w[vm] if vm else np.zeros(0, np.float32)
+        code = None
+        if d["has_code"][i]:
+            eo = d["order"][d["order_off"][i]:d["order_off"][i + 1]].tolist()
+            code = _order.order2eincode(g, eo)
+        out.append(SlicedBranch(MISProblem(g, w.astype(np.float32)), code, float(d["r"][i]), order=None, vmap=vm))
+    return out
+
+
+def _branch_set(g: Graph, w, sc_target: int, seed: int, init_niters: int, reductions):
+    """Kernelize, anneal briefly, branch without re-annealing (so every tree
+    is determined by its elimination order)."""
+    kr = _mis.kernelize(g, w, rules=reductions)
     if kr.g.n == 0:
-        return [SlicedBranch(MISProblem(kr.g, kr.weights), None, kr.r)]
+        return kr, [SlicedBranch(MISProblem(kr.g, kr.weights), None, kr.r, vmap=[])]
     code = _order.initialize_code(kr.g, _order.GreedyMethod(seed))
-    code = _order.treesa(code, _order.TreeSA(sc_target=sc_target, betas=np.arange(0.5, 20, 0.25), ntrials=4,
-                                             niters=60, seed=seed))
-    slicer = _mis.ContractionTreeSlicer(sc_target=sc_target)
-    return _mis.slice(MISProblem(kr.g, kr.weights), code, kr.r, slicer)
+    code = _order.treesa(code, _order.TreeSA(sc_target=sc_target, betas=np.arange(1.0, 15.0, 1.0), ntrials=2,
+                                             niters=init_niters, seed=seed))
+    slicer = _mis.ContractionTreeSlicer(sc_target=sc_target, refine=False, reductions=reductions)
+    brs = _mis.slice(MISProblem(kr.g, kr.weights), code, kr.r, slicer)
+    if len(brs) == 1 and brs[0].vmap is None:
+        # no branching needed: the root tree is the annealed one; store its order
+        b = brs[0]
+        eo = _mis.eincode2order(code)
+        b.order, b.vmap = eo, list(range(kr.g.n))
+        b.code = _order.order2eincode(kr.g, eo)
+    return kr, brs
 
 
 def build_rr100_b10() -> dict:
-    graphs = []
+    graphs = {}
     for s in range(1, 33):
         g = random_regular_graph(100, 3, s)
-        brs = _branched(g, np.ones(100, np.float32), 10, s)
-        graphs.append({"seed": s, "edges": [list(e) for e in g.edges], "branches": [_branch_json(b) for b in brs]})
-    return {"name": "rr100_b10", "graphs": graphs}
+        kr, brs = _branch_set(g, np.ones(100, np.float32), 10, s, 20, _mis.REDUCTIONS_ALL)
+        for k, v in _pack_branches(brs).items():
+            graphs[f"g{s}_{k}"] = v
+    return graphs
 
 
 def build_ksg32_b20() -> dict:
+    # the reductions without domination (which alone empties King's subgraphs
+    # with unit weights), a short annealing of the initial tree, and branching
+    # without re-annealing each branch: an uneven batch of subnetworks
     g = random_ksg(32, 0.8, 1)
-    brs = _branched(g, np.ones(g.n, np.float32), 20, 1)
-    return {"name": "ksg32_b20", "graph": {"n": g.n, "edges": [list(e) for e in g.edges]}, "seed": 1,
-            "branches": [_branch_json(b) for b in brs]}
+    kr, brs = _branch_set(g, np.ones(g.n, np.float32), 20, 1, 20, _mis.REDUCTIONS_BASIC)
+    return _pack_branches(brs)
 
 
 BUILDERS = {"rr220": build_rr220, "rr300_s22": build_rr300_s22, "rr100_b10": build_rr100_b10,
             "ksg32_b20": build_ksg32_b20}
 
 
+NPZ = {"rr100_b10", "ksg32_b20"}
+
+
 def path(name: str) -> str:
-    return os.path.join(DATA, name + ".json")
+    return os.path.join(DATA, name + (".npz" if name in NPZ else ".json"))
 
 
-def make(name: str) -> dict:
+def make(name: str):
     t = time.time()
     d = BUILDERS[name]()
     os.makedirs(DATA, exist_ok=True)
-    with open(path(name), "w") as f:
-        json.dump(d, f, separators=(",", ":"))
+    if name in NPZ:
+        np.savez_compressed(path(name), **d)
+    else:
+        with open(path(name), "w") as f:
+            json.dump(d, f, separators=(",", ":"))
     print(f"{name}: built in {time.time() - t:.0f}s", file=sys.stderr)
     return d
 
 
-def load_raw(name: str) -> dict:
+def load_raw(name: str):
     p = path(name)
     if not os.path.exists(p):
         raise FileNotFoundError(f"workload {name} not built; run: python bench.py --make {name}")
+    if name in NPZ:
+        return dict(np.load(p))
     with open(p) as f:
         return json.load(f)
 
@@ -175,16 +228,17 @@ def load(name: str) -> dict:
         return {"name": name, "graph": g, "branches": [b], "sliced": list(d["sliced"]), "slice_values": None}
     if name == "rr100_b10":
         brs, gs = [], []
-        for gd in d["graphs"]:
-            g = random_regular_graph(100, 3, gd["seed"])
-            assert [list(e) for e in g.edges] == gd["edges"], "graph generator changed"
+        for s in range(1, 33):
+            g = random_regular_graph(100, 3, s)
+            kr = _mis.kernelize(g, np.ones(100, np.float32), rules=_mis.REDUCTIONS_ALL)
+            sub = {k[len(f"g{s}_"):]: v for k, v in d.items() if k.startswith(f"g{s}_")}
             gs.append(g)
-            brs.append([_branch_from(x) for x in gd["branches"]])
+            brs.append(_unpack_branches(kr.g, kr.weights, sub))
         return {"name": name, "graphs": gs, "branch_sets": brs, "branches": [b for bs in brs for b in bs],
                 "sliced": [], "slice_values": None}
     if name == "ksg32_b20":
-        g = random_ksg(32, 0.8, d["seed"])
-        assert [list(e) for e in g.edges] == d["graph"]["edges"], "graph generator changed"
-        brs = [_branch_from(x) for x in d["branches"]]
+        g = random_ksg(32, 0.8, 1)
+        kr = _mis.kernelize(g, np.ones(g.n, np.float32), rules=_mis.REDUCTIONS_BASIC)
+        brs = _unpack_branches(kr.g, kr.weights, d)
         return {"name": name, "graph": g, "branches": brs, "sliced": [], "slice_values": None}
     raise KeyError(name)
