@@ -485,14 +485,31 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
   // chunks for the persistent executor: runs of stream tiles (tables are
-  // built once per chunk), single GEMM tiles, whole leaf / final steps
+  // built once per chunk and the copy pipeline stays full along the run),
+  // single GEMM tiles, whole leaf / final steps.  A stream step is cut into
+  // runs of at least 1/ctas of its tiles and at least 1/(4 ctas) of the
+  // stream tiles of its whole level, so many small steps of many items do
+  // not turn into as many tiny runs.
+  std::vector<int64_t> level_tiles;
+  for (const GK& x : gk) {
+    const Step& st = plans[x.item]->h.steps[x.step];
+    if (st.kind != STEP_TILE) continue;
+    if ((int)level_tiles.size() <= x.level) level_tiles.resize(x.level + 1, 0);
+    level_tiles[x.level] += st.n_tiles;
+  }
+  const int64_t ctas = std::max(1, c->persistent_ctas);
   std::vector<Chunk> chs;
   for (size_t g = 0; g < gk.size(); g++) {
     const Step& st = plans[gk[g].item]->h.steps[gk[g].step];
     const int64_t nt = st.n_tiles;
     int64_t cs = 1;
-    if (st.kind == STEP_TILE) cs = std::max<int64_t>(1, std::min<int64_t>(256, (nt + c->persistent_ctas - 1) / c->persistent_ctas));
-    else if (st.kind == STEP_LEAVES) cs = nt;
+    if (st.kind == STEP_TILE) {
+      const int64_t lt = level_tiles[gk[g].level];
+      cs = std::max((nt + ctas - 1) / ctas, (lt + 4 * ctas - 1) / (4 * ctas));
+      cs = std::max<int64_t>(1, std::min<int64_t>(cs, 256));
+    } else if (st.kind == STEP_LEAVES) {
+      cs = nt;
+    }
     for (int64_t t0 = 0; t0 < nt; t0 += cs) {
       Chunk ch;
       ch.group = (int32_t)g;

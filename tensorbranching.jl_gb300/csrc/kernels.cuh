@@ -124,10 +124,18 @@ __host__ __device__ inline int stream_a_words(const TileDesc& d) { return ((1 <<
 __host__ __device__ inline int stream_buf_words(const TileDesc& d) {
   return stream_a_words(d) + (d.b_off >= 0 ? (((1 << d.nb) + 3) & ~3) : 0);
 }
-// shared memory of a stream tile: two operand buffers, then tables
+// Pipeline depth: as many operand buffers as fit in the staging area of two
+// full-size buffers, from 2 (operand tiles of 2^13 words) up to kMaxStages
+// (short tiles, where the bytes in flight would otherwise be too few to cover
+// the memory latency).
+__host__ __device__ inline int stream_stages(const TileDesc& d) {
+  const int s = (2 * kSmemFloats) / stream_buf_words(d);
+  return s < 2 ? 2 : s > kMaxStages ? kMaxStages : s;
+}
+// shared memory of a stream tile: the operand buffers, then tables
 __host__ __device__ inline int stream_smem_words(const TileDesc& d) {
   const bool hasB = d.b_off >= 0;
-  int w = 2 * stream_buf_words(d);
+  int w = stream_stages(d) * stream_buf_words(d);
   w += 1 << (d.na - d.pa);
   w += hasB ? (1 << (d.nb - d.pb)) : 0;
   w += 1 << (d.n_tc - d.pc);
@@ -158,6 +166,19 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
+// wait until at most n (0..7) committed groups are pending
+__device__ __forceinline__ void cp_async_wait_n(int n) {
+  switch (n) {
+    case 7: cp_async_wait<7>(); break;
+    case 6: cp_async_wait<6>(); break;
+    case 5: cp_async_wait<5>(); break;
+    case 4: cp_async_wait<4>(); break;
+    case 3: cp_async_wait<3>(); break;
+    case 2: cp_async_wait<2>(); break;
+    case 1: cp_async_wait<1>(); break;
+    default: cp_async_wait<0>(); break;
+  }
+}
 
 // Issue async copies of the 2^n-element sub-tensor at src into swizzled
 // shared memory (tile bit b <-> tensor position pos[b]; bits below p are the
@@ -183,8 +204,9 @@ __device__ __forceinline__ void issue_sub(T* __restrict__ dst, const T* __restri
 }
 
 // Run tiles [t0, t1) of one stream-tile descriptor on this CTA: index tables
-// are built once, and the operand sub-tiles of the next (tile, loop step) are
-// copied asynchronously while the current one is reduced.
+// are built once, and the operand sub-tiles of the next stream_stages(d) - 1
+// (tile, loop step) items are copied asynchronously while the current one is
+// reduced.
 template <typename T>
 __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __restrict__ arena,
                              int* __restrict__ smem) {
@@ -192,8 +214,9 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
   const bool hasB = d.b_off >= 0;
   const int NA = stream_a_words(d);  // A region (padded), B region follows
   const int BUF = stream_buf_words(d);
+  const int S = stream_stages(d);
   T* buf0 = reinterpret_cast<T*>(smem);
-  int* ldA = reinterpret_cast<int*>(buf0 + 2 * BUF);
+  int* ldA = reinterpret_cast<int*>(buf0 + S * BUF);
   const int nAh = 1 << (d.na - d.pa);
   const int nBh = hasB ? (1 << (d.nb - d.pb)) : 0;
   const int nCh = 1 << (d.n_tc - d.pc);
@@ -312,10 +335,12 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
   // prefetch cursor: tile pt, loop step pr, offsets
   int64_t pt = t0;
   int pr = 0, pa_g = ga, pb_g = gb, pa_l = 0, pb_l = 0;
-  auto issue = [&](int64_t it) {
-    T* dst = buf0 + (it & 1) * BUF;
+  int ib = 0;  // buffer of the next issue
+  auto issue = [&]() {
+    T* dst = buf0 + ib * BUF;
     issue_sub<T>(dst, A0 + (pa_g + pa_l), d.na, d.pa, ldA);
     if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), d.nb, d.pb, ldB);
+    ib = ib + 1 == S ? 0 : ib + 1;
   };
   auto advance = [&]() {
     if (pr + 1 < nloop) {
@@ -336,26 +361,36 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
   int oc = gc;
 
   T acc[kMaxOpt];
-  if (n_items > 0) {
-    issue(0);
-    advance();
-  }
-  cp_async_commit();
-  for (int64_t it = 0; it < n_items; it++) {
-    if (it + 1 < n_items) {
-      issue(it + 1);
+  // prologue: items 0 .. S-2, one commit group each (empty past the end)
+  int64_t issued = 0;
+  for (int k = 0; k < S - 1; k++) {
+    if (issued < n_items) {
+      issue();
       advance();
+      issued++;
     }
     cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();  // item `it` is in its buffer
+  }
+  int cb = 0;  // buffer of the item being reduced
+  for (int64_t it = 0; it < n_items; it++) {
+    // item it + S - 1 goes to the buffer item it - 1 used (released by the
+    // barrier that closed the previous iteration)
+    if (issued < n_items) {
+      issue();
+      advance();
+      issued++;
+    }
+    cp_async_commit();
+    cp_async_wait_n(S - 1);  // groups 0..it are complete
+    __syncthreads();         // item `it` is in its buffer for every thread
     const int rl = (int)(it % nloop);
     if (rl == 0) {
 #pragma unroll
       for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
     }
-    const T* As = buf0 + (it & 1) * BUF;
+    const T* As = buf0 + cb * BUF;
     const T* Bs = As + NA;
+    cb = cb + 1 == S ? 0 : cb + 1;
     if (act) {
       if (small_r) {
 #pragma unroll
@@ -415,7 +450,7 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
       oc += incCg[k];
       ct++;
     }
-    __syncthreads();  // buffer (it & 1) is free for item it + 2
+    __syncthreads();  // this item's buffer is free for item it + S
   }
   cp_async_wait<0>();
 }

@@ -10,6 +10,7 @@ constexpr int kMaxBits = 48;      // labels of one tensor / grid / loop
 constexpr int kThreads = 256;     // threads of every tile kernel
 constexpr int kMaxOpt = 4;        // outputs per thread in the stream tile
 constexpr int kSmemFloats = 8192; // stream tile staging (As + Bs), floats
+constexpr int kMaxStages = 8;     // stream tile pipeline depth (short operand tiles)
 
 enum StepKind : int32_t {
   STEP_LEAVES = 1,  // build the item's leaf tensors

@@ -165,6 +165,19 @@ class Engine:
 _default: Engine | None = None
 
 
+def measure_maxplus_peak(device: int = 0) -> float:
+    """Measured f32 SIMT max-plus rate of this GPU in ops/s (max and add
+    counted as two ops): a loop-carried add.f32x2 + 3-input max.f32 probe
+    over every SM (tbi_measure_maxplus_peak, an internal engine symbol)."""
+    lib = _native.engine_lib()
+    f = lib.tbi_measure_maxplus_peak
+    f.restype = c_int32
+    f.argtypes = [c_int32, POINTER(c_double)]
+    v = c_double()
+    _native.check(f(int(device), ctypes.byref(v)))
+    return float(v.value)
+
+
 def default_engine() -> Engine:
     global _default
     if _default is None:

@@ -7,8 +7,10 @@ Each workload follows one configuration of the benchmark plan:
               test/dynamic_ob.jl:10-26); 32 graphs (seeds 1..32), every branch
               of every graph in one batch
   rr220       random 3-regular n=220, unit weights, one contraction, no slicing
-  rr300_s22   random 3-regular n=300, integer weights U{1..10}; index slicing
-              until every slice has sc <= 22; 2^k slices
+  rr220w_s22  the rr220 graph and tree with integer weights U{1..10}; index
+              slicing until every slice has sc <= 22; 2^k slices (the sliced
+              batch configuration at n=220: at n=300 the host order search
+              reaches sc 42-45, which needs 2^20 slices and ~4.5e15 ops)
   ksg32_b20   King's subgraph L=32, filling 0.8, unit weights; kernelize +
               branch until sc <= 20
 
@@ -37,7 +39,7 @@ DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 WORKLOADS = {
     "rr100_b10": "32 random 3-regular graphs n=100 (seeds 1..32), unit weights, branched to sc<=10",
     "rr220": "random 3-regular n=220 (seed 1), unit weights, one contraction, no slicing",
-    "rr300_s22": "random 3-regular n=300 (seed 3), weights U{1..10}, index-sliced to sc<=22",
+    "rr220w_s22": "random 3-regular n=220 (seed 1), weights U{1..10} (seed 1), rr220's tree index-sliced to sc<=22",
     "ksg32_b20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, isolated/pendant reductions, "
                  "branched to sc<=20",
 }
@@ -86,15 +88,16 @@ def build_rr220() -> dict:
             "weights": "unit", "code": _code_json(code), "cc": list(code.complexity())}
 
 
-def build_rr300_s22() -> dict:
-    g = random_regular_graph(300, 3, 3)
-    w = random_weights(300, 3)
-    code = _order.initialize_code(g, _order.GreedyMethod(3))
-    code = _anneal(code, 30, rounds=2, niters=400, seed=3)
+def build_rr220w_s22() -> dict:
+    base = load_raw("rr220")
+    g = random_regular_graph(220, 3, base["seed"])
+    ixs, iy = rawcode(g)
+    code = CompressedEinsum(ixs, iy, np.array(base["code"]["children"], np.int32).reshape(-1, 2), n_labels=g.n)
+    w = random_weights(220, 1)
     sliced, cc = _order.greedy_slice(code, 22, 40)
-    return {"name": "rr300_s22", "graph": {"n": g.n, "edges": [list(e) for e in g.edges]}, "seed": 3,
-            "weights": w.tolist(), "code": _code_json(code), "cc": list(code.complexity()),
-            "sliced": sliced, "sliced_cc": list(cc)}
+    return {"name": "rr220w_s22", "graph": {"n": g.n, "edges": [list(e) for e in g.edges]}, "seed": base["seed"],
+            "weights": w.tolist(), "code": base["code"], "cc": list(code.complexity()), "sliced": sliced,
+            "sliced_cc": list(cc)}
 
 
 def _pack_branches(brs: list[SlicedBranch]) -> dict:
@@ -168,7 +171,7 @@ def build_ksg32_b20() -> dict:
     return _pack_branches(brs)
 
 
-BUILDERS = {"rr220": build_rr220, "rr300_s22": build_rr300_s22, "rr100_b10": build_rr100_b10,
+BUILDERS = {"rr220": build_rr220, "rr220w_s22": build_rr220w_s22, "rr100_b10": build_rr100_b10,
             "ksg32_b20": build_ksg32_b20}
 
 
@@ -218,14 +221,15 @@ def load(name: str) -> dict:
         code = CompressedEinsum(ixs, iy, np.array(d["code"]["children"], np.int32).reshape(-1, 2), n_labels=g.n)
         b = SlicedBranch(MISProblem(g, np.ones(g.n, np.float32)), code, 0.0)
         return {"name": name, "graph": g, "branches": [b], "sliced": [], "slice_values": None}
-    if name == "rr300_s22":
-        g = random_regular_graph(300, 3, d["seed"])
+    if name == "rr220w_s22":
+        g = random_regular_graph(220, 3, d["seed"])
         assert [list(e) for e in g.edges] == d["graph"]["edges"], "graph generator changed"
         w = np.array(d["weights"], np.float32)
         ixs, iy = rawcode(g)
         code = CompressedEinsum(ixs, iy, np.array(d["code"]["children"], np.int32).reshape(-1, 2), n_labels=g.n)
         b = SlicedBranch(MISProblem(g, w), code, 0.0)
-        return {"name": name, "graph": g, "branches": [b], "sliced": list(d["sliced"]), "slice_values": None}
+        return {"name": name, "graph": g, "branches": [b], "sliced": list(d["sliced"]), "slice_values": None,
+                "open_bits": 0}
     if name == "rr100_b10":
         brs, gs = [], []
         for s in range(1, 33):

@@ -143,9 +143,14 @@ def buf_words(d):
     return a_words(d) + ((((1 << d.nb) + 3) & ~3) if d.b_off >= 0 else 0)
 
 
+def stages(d):
+    """Pipeline depth of the stream tile (stream_stages)."""
+    return max(2, min(8, (2 * KSMEM) // buf_words(d)))
+
+
 def smem_words(d):
     hasB = d.b_off >= 0
-    w = 2 * buf_words(d)
+    w = stages(d) * buf_words(d)
     w += 1 << (d.na - d.pa)
     w += (1 << (d.nb - d.pb)) if hasB else 0
     w += 1 << (d.n_tc - d.pc)
@@ -254,7 +259,7 @@ def emu_stream_tile(d, arena, written, expect=None):
                 g = base + (j & ((1 << p) - 1)) + hi[j >> p]
                 assert g.min() >= lo and g.max() < hi_b, "global load out of bounds"
                 # async copies: 16 bytes when p >= 2, 8 when p == 1; both ends aligned
-                for b in (0, 1):  # the two double-buffer slots
+                for b in range(stages(d)):  # every pipeline buffer
                     dst = b * buf_words(d) + region + swz(j)
                     if p >= 2:
                         assert np.all(g[::4] % 4 == 0), "misaligned 16-byte global source"
