@@ -147,7 +147,7 @@ OPEN_BITS = 4          # sliced labels kept open per item (2^4 slices per item)
 SLICED_ITEMS_PER_STEP = 64
 
 
-def make_items(engine, wl, tb):
+def make_items(engine, wl, tb, max_items=0):
     """Plans and per-item inputs of one step of the workload.  Index-sliced
     workloads group 2^OPEN_BITS slices per item (those labels stay open in the
     root tensor) and a step runs SLICED_ITEMS_PER_STEP of the items."""
@@ -167,7 +167,7 @@ def make_items(engine, wl, tb):
             wmap[id(p)] = b.p.weight_array()
             k = len(fixed)
             total = 1 << k
-            take = min(total, SLICED_ITEMS_PER_STEP)
+            take = min(total, max_items or SLICED_ITEMS_PER_STEP)
             frac = take / total
             idx = np.linspace(0, total - 1, take).astype(np.int64)
             vals = ((idx[:, None] >> np.arange(k)[None, :]) & 1).astype(np.int8)
@@ -189,8 +189,8 @@ def expected_answer(wl):
     """Solves (MIS values) one step completes: graphs per step, or the
     fraction of one solve a step of a sliced workload covers."""
     if wl["name"] == "rr100_b10":
-        return len(wl["graphs"])
-    return wl.get("step_fraction", 1.0)
+        return len(wl["graphs"]) if not wl.get("truncated") else 0.0
+    return wl.get("step_fraction", 1.0) if not wl.get("truncated") else 0.0
 
 
 def _node_ops(code):
@@ -289,12 +289,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="rr220")
-    ap.add_argument("--mode", default="batched", choices=["batched", "layered", "plain"])
+    ap.add_argument("--mode", default="auto", choices=["auto", "batched", "layered", "plain"],
+                    help="auto: tb_autotune picks tile size and schedule before the warm-up (untimed)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--compare-plain", action="store_true")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--make", nargs="*")
+    ap.add_argument("--max-items", type=int, default=0,
+                    help="run only the first N branches / sliced items (small cases for ncu captures)")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch kernels directly instead of replaying a CUDA graph")
     args = ap.parse_args()
 
     tb = _ge.load_package()
@@ -314,6 +319,8 @@ def main():
             return
         return run_serve(tb, args)
     wl = load_workload(tb, args.config)
+    if args.max_items and not wl["sliced"]:
+        wl["truncated"] = True  # a subset of the branches answers no whole solve
     units = expected_answer(wl)
 
     if args.impl == "reference":
@@ -347,12 +354,18 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
-    eng = tb.Engine(device=dev)
-    plans, svs, rs = make_items(eng, wl, tb)
+    eng = tb.Engine(device=dev, use_graphs=not args.no_graphs)
+    if args.max_items:
+        wl["branches"] = [b for b in wl["branches"] if b.code is not None][: args.max_items]
+    plans, svs, rs = make_items(eng, wl, tb, args.max_items)
+    units = expected_answer(wl)
     st = plans[0].stats()
     uniq = {id(p): p for p in plans}
     ops = sum(uniq[k].stats()["ops"] for k in uniq) if not wl["sliced"] else st["ops"] * len(plans)
     byts = sum(uniq[k].stats()["bytes"] for k in uniq) if not wl["sliced"] else st["bytes"] * len(plans)
+    tuned = None
+    if args.mode == "auto":
+        tuned = eng.autotune(plans, slice_vals=svs, r=rs)
     # check the answer once
     out0, mx0 = eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
     from tensorbranching_gb300.engine import measure_maxplus_peak
@@ -431,7 +444,7 @@ def main():
         "config": {"workload": args.config, "detail": _desc(args.config), "mode": args.mode,
                    "items_per_step": len(plans), "graphs_per_step": units, "tc": st["tc"], "sc": st["sc"],
                    "rwc": st["rwc"], "l2": "flushed between steps (256 MiB write)",
-                   "answer": mx0, "parallelism": f"replicas x{ws}"},
+                   "answer": mx0, "parallelism": f"replicas x{ws}", "autotune": tuned},
         "tropical_gops": ops / (ms_per_step / 1000.0) / 1e9,
         "roofline": roof,
         "e2e": {"value": ws * args.steps * units / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,

@@ -68,6 +68,9 @@ typedef int32_t tb_status;
                              work queue, replayed from a captured CUDA graph */
 #define TB_MODE_LAYERED 2 /* fused per-contraction launches over all items,
                              captured in a CUDA graph */
+#define TB_MODE_AUTO 3    /* the schedule tb_autotune chose for this context
+                             (tuned on first use when tb_options.autotune is 1;
+                             TB_MODE_BATCHED before any tuning) */
 
 typedef struct tb_ctx tb_ctx;
 typedef struct tb_plan tb_plan;
@@ -77,7 +80,7 @@ typedef struct tb_options {
   int32_t use_graphs;       /* 1: capture batched launches in CUDA graphs */
   int64_t max_device_bytes; /* arena budget; 0 = 80% of free memory at create */
   int32_t timeout_ms;       /* bound on every device-side wait (default 20000) */
-  int32_t autotune;         /* 1: choose tile shapes by timing (cached per shape) */
+  int32_t autotune;         /* 1: the first TB_MODE_AUTO solve runs tb_autotune */
   int32_t persistent_ctas;  /* CTAs of the persistent executor; 0 = 2 per SM */
   int32_t reserved[9];
 } tb_options;
@@ -97,7 +100,19 @@ typedef struct tb_plan_stats {
   int32_t reserved[7];
 } tb_plan_stats;
 
-/* Fill *opt with defaults (f32, graphs on, autotune on). */
+/* Result of tb_autotune: the chosen tile size and schedule. */
+typedef struct tb_tune_result {
+  int32_t mode;        /* TB_MODE_BATCHED or TB_MODE_LAYERED */
+  int32_t tile_bits;   /* stream tiles of up to 2^tile_bits outputs (8..10) */
+  int32_t ctas_per_sm; /* resident CTAs per SM of the persistent executor */
+  int32_t chunk_div;   /* runs of stream tiles hold >= 1/(chunk_div CTAs) of a level */
+  double ms;           /* device time of the batch with the chosen settings */
+  double ms_default;   /* device time with the defaults */
+  int32_t n_tried;     /* configurations timed */
+  int32_t reserved[7];
+} tb_tune_result;
+
+/* Fill *opt with defaults (f32, graphs on, autotune on for TB_MODE_AUTO). */
 void tb_options_default(tb_options* opt);
 
 /* Create / destroy a context bound to CUDA device `device`. */
@@ -158,6 +173,18 @@ tb_status tb_plan_bind_mis(tb_plan* plan, const float* weights);
  */
 tb_status tb_solve_batch(tb_ctx* ctx, int32_t n, tb_plan* const* plans, const int8_t* slice_vals,
                          const float* r, float* out_item, float* out_max, int32_t mode);
+
+/*
+ * Choose the stream tile size (tile_bits 8..10) and the executor schedule
+ * (persistent launch with 1..2 CTAs per SM and three run lengths, or
+ * per-level launches) for this batch by running it with each setting and
+ * keeping the fastest; the chosen tiles stay in the plans and the schedule in
+ * the context for TB_MODE_AUTO.  Arguments as tb_solve_batch.  Runs the batch
+ * about 40 times.  No counterpart in the reference (its contraction has no
+ * tunable schedule).
+ */
+tb_status tb_autotune(tb_ctx* ctx, int32_t n, tb_plan* const* plans, const int8_t* slice_vals,
+                      const float* r, tb_tune_result* out);
 
 /*
  * Contract one plan with explicit leaf tensors (host arrays, leaf i holding

@@ -23,8 +23,9 @@ TB_DTYPE_I32 = 1
 TB_MODE_PLAIN = 0
 TB_MODE_BATCHED = 1
 TB_MODE_LAYERED = 2
+TB_MODE_AUTO = 3
 
-MODES = {"plain": TB_MODE_PLAIN, "batched": TB_MODE_BATCHED, "layered": TB_MODE_LAYERED}
+MODES = {"plain": TB_MODE_PLAIN, "batched": TB_MODE_BATCHED, "layered": TB_MODE_LAYERED, "auto": TB_MODE_AUTO}
 
 
 class TbOptions(ctypes.Structure):
@@ -56,6 +57,19 @@ class TbPlanStats(ctypes.Structure):
     ]
 
 
+class TbTuneResult(ctypes.Structure):
+    _fields_ = [
+        ("mode", c_int32),
+        ("tile_bits", c_int32),
+        ("ctas_per_sm", c_int32),
+        ("chunk_div", c_int32),
+        ("ms", c_double),
+        ("ms_default", c_double),
+        ("n_tried", c_int32),
+        ("reserved", c_int32 * 7),
+    ]
+
+
 class TbError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"tb status {status}: {msg}")
@@ -83,6 +97,7 @@ ENGINE_SIGNATURES = {
                                  c_void_p]),
     "tb_solve_static": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
+    "tb_autotune": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, POINTER(TbTuneResult)]),
     "tb_serve_start": (c_int32, [c_void_p, c_int64, c_int32]),
     "tb_serve_stop": (c_int32, [c_void_p]),
     "tb_submit": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, POINTER(c_void_p)]),

@@ -278,7 +278,10 @@ struct GraphKey {
   std::vector<const tb_plan*> plans;
   std::vector<uint64_t> versions;
   int mode = 0;
-  bool operator==(const GraphKey& o) const { return plans == o.plans && versions == o.versions && mode == o.mode; }
+  int sched = 0;  // persistent CTAs and chunk divisor the chunk list was built for
+  bool operator==(const GraphKey& o) const {
+    return plans == o.plans && versions == o.versions && mode == o.mode && sched == o.sched;
+  }
 };
 
 struct tb_ctx {
@@ -311,6 +314,11 @@ struct tb_ctx {
   int64_t launches_graph = 0;
   uint64_t plan_counter = 0;
   std::mutex mu;
+  // schedule knobs of the batched executor (tb_autotune sets them)
+  int ctas_per_sm_max = 2;  // resident k_persistent CTAs per SM
+  int chunk_div = 4;        // a stream step's runs hold >= 1/(chunk_div ctas) of its level
+  bool tuned = false;
+  tb_tune_result tune{};
 };
 
 static tb_status fail(tb_status s, const std::string& msg) {
@@ -505,7 +513,8 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     int64_t cs = 1;
     if (st.kind == STEP_TILE) {
       const int64_t lt = level_tiles[gk[g].level];
-      cs = std::max((nt + ctas - 1) / ctas, (lt + 4 * ctas - 1) / (4 * ctas));
+      const int64_t div = std::max(1, c->chunk_div) * ctas;
+      cs = std::max((nt + ctas - 1) / ctas, (lt + div - 1) / div);
       cs = std::max<int64_t>(1, std::min<int64_t>(cs, 256));
     } else if (st.kind == STEP_LEAVES) {
       cs = nt;
@@ -683,6 +692,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     CU(c->arena.ensure(bytes));
     GraphKey key;
     key.mode = mode;
+    key.sched = c->persistent_ctas * 64 + c->chunk_div;
     for (int i = 0; i < n; i++) {
       key.plans.push_back(plans[i]);
       key.versions.push_back(plans[i]->version);
@@ -755,9 +765,123 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
 }
 
 // ---------------------------------------------------------------------------
+// Autotuner: tile shapes, then the executor's schedule, by timing the batch.
+// ---------------------------------------------------------------------------
+static void retile_all(tb_ctx* c, const std::vector<tb_plan*>& uniq, int bits, std::string& err) {
+  for (tb_plan* p : uniq) {
+    if (p->h.tile_bits == bits) continue;
+    std::string e = retile_plan(p->h, bits);
+    if (!e.empty()) {
+      err = e;
+      return;
+    }
+    p->structure_uploaded = false;
+    p->uploaded = false;
+    p->version = ++c->plan_counter;
+  }
+}
+
+static tb_status time_batch(tb_ctx* c, int n, tb_plan* const* plans, const int8_t* sv, const float* r, int mode,
+                            double& best_ms) {
+  tb_status st = TB_OK;
+  best_ms = 1e30;
+  for (int rep = 0; rep < 3; rep++) {  // first run builds the batch and its graph
+    st = c->opt.dtype == TB_DTYPE_F32 ? solve_batch_t<float>(c, n, plans, sv, r, nullptr, nullptr, mode)
+                                      : solve_batch_t<int32_t>(c, n, plans, sv, r, nullptr, nullptr, mode);
+    if (st) return st;
+    if (rep > 0) best_ms = std::min(best_ms, c->last_ms);
+  }
+  return TB_OK;
+}
+
+static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const int8_t* sv, const float* r,
+                                 tb_tune_result* out) {
+  std::vector<tb_plan*> uniq;
+  for (int i = 0; i < n; i++)
+    if (std::find(uniq.begin(), uniq.end(), plans[i]) == uniq.end()) uniq.push_back(plans[i]);
+  tb_tune_result res{};
+  res.n_tried = 0;
+  std::string err;
+  tb_status st;
+  // the defaults first, as the reference point
+  const int base_bits = uniq.empty() ? 9 : uniq[0]->h.tile_bits;
+  c->chunk_div = 4;
+  c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : c->ctas_per_sm_max * c->sms;
+  double ms;
+  if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
+  res.ms_default = ms;
+  res.n_tried++;
+  // 1. stream tile size
+  int best_bits = base_bits;
+  double best = ms;
+  for (int bits = 8; bits <= 10; bits++) {
+    if (bits == base_bits) continue;
+    retile_all(c, uniq, bits, err);
+    if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
+    if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
+    res.n_tried++;
+    if (ms < best) {
+      best = ms;
+      best_bits = bits;
+    }
+  }
+  retile_all(c, uniq, best_bits, err);
+  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
+  // 2. schedule: per-level launches, or the persistent executor with 1..max
+  // CTAs per SM and coarser or finer runs of stream tiles
+  int best_mode = TB_MODE_BATCHED, best_cps = c->ctas_per_sm_max, best_div = 4;
+  if ((st = time_batch(c, n, plans, sv, r, TB_MODE_LAYERED, ms))) return st;
+  res.n_tried++;
+  if (ms < best) {
+    best = ms;
+    best_mode = TB_MODE_LAYERED;
+  }
+  if (c->opt.persistent_ctas <= 0) {
+    for (int cps = 1; cps <= c->ctas_per_sm_max; cps++) {
+      for (int div : {1, 4, 16}) {
+        if (cps == c->ctas_per_sm_max && div == 4) continue;  // timed above
+        c->persistent_ctas = cps * c->sms;
+        c->chunk_div = div;
+        if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
+        res.n_tried++;
+        if (ms < best) {
+          best = ms;
+          best_mode = TB_MODE_BATCHED;
+          best_cps = cps;
+          best_div = div;
+        }
+      }
+    }
+  }
+  c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : best_cps * c->sms;
+  c->chunk_div = best_div;
+  res.mode = best_mode;
+  res.tile_bits = best_bits;
+  res.ctas_per_sm = c->persistent_ctas / std::max(1, c->sms);
+  res.chunk_div = best_div;
+  res.ms = best;
+  c->tune = res;
+  c->tuned = true;
+  if (out) *out = res;
+  return TB_OK;
+}
+
+// ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
+
+tb_status tb_autotune(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8_t* slice_vals, const float* r,
+                      tb_tune_result* out) {
+  if (!c) return fail(TB_ERR_INVALID, "null context");
+  if (n <= 0 || !plans) return fail(TB_ERR_INVALID, "empty batch");
+  std::lock_guard<std::mutex> lk(c->mu);
+  try {
+    return autotune_locked(c, n, plans, slice_vals, r, out);
+  } catch (const std::exception& ex) {
+    return fail(TB_ERR_INVALID, std::string("internal: ") + ex.what());
+  }
+}
 
 void tb_options_default(tb_options* o) {
   if (!o) return;
@@ -766,7 +890,7 @@ void tb_options_default(tb_options* o) {
   o->use_graphs = 1;
   o->max_device_bytes = 0;
   o->timeout_ms = 20000;
-  o->autotune = 0;
+  o->autotune = 1;
   o->persistent_ctas = 0;
 }
 
@@ -801,6 +925,7 @@ tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
   else
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<int32_t>, kThreads, max_stream_smem_bytes()));
   per_sm = std::max(1, per_sm);
+  c->ctas_per_sm_max = per_sm;
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : per_sm * c->sms;
   int per_sm_stream = 0;
   if (c->opt.dtype == TB_DTYPE_F32)
@@ -932,10 +1057,17 @@ tb_status tb_solve_batch(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8
                          float* out_item, float* out_max, int32_t mode) {
   if (!c) return fail(TB_ERR_INVALID, "null context");
   if (n <= 0 || !plans) return fail(TB_ERR_INVALID, "empty batch");
-  if (mode != TB_MODE_PLAIN && mode != TB_MODE_BATCHED && mode != TB_MODE_LAYERED)
+  if (mode != TB_MODE_PLAIN && mode != TB_MODE_BATCHED && mode != TB_MODE_LAYERED && mode != TB_MODE_AUTO)
     return fail(TB_ERR_INVALID, "unknown mode");
   std::lock_guard<std::mutex> lk(c->mu);
   try {
+    if (mode == TB_MODE_AUTO) {
+      if (!c->tuned && c->opt.autotune) {
+        tb_status st = autotune_locked(c, n, plans, slice_vals, r, nullptr);
+        if (st) return st;
+      }
+      mode = c->tuned ? c->tune.mode : TB_MODE_BATCHED;
+    }
     if (c->opt.dtype == TB_DTYPE_F32) return solve_batch_t<float>(c, n, plans, slice_vals, r, out_item, out_max, mode);
     return solve_batch_t<int32_t>(c, n, plans, slice_vals, r, out_item, out_max, mode);
   } catch (const std::exception& ex) {
@@ -1140,14 +1272,15 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
                                      const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
                                      const int32_t* children, const int32_t* node_iy_off,
                                      const int32_t* node_iy_lab, int32_t n_sliced, const int32_t* sliced,
-                                     int32_t gemm_min, void** blob, int64_t* blob_bytes, char* err,
-                                     int32_t err_cap) {
+                                     int32_t gemm_min, int32_t tile_bits, void** blob, int64_t* blob_bytes,
+                                     char* err, int32_t err_cap) {
   PlanInput in;
   in.n_labels = n_labels; in.n_tensors = n_tensors; in.ix_off = ix_off; in.ix_lab = ix_lab;
   in.n_iy = n_iy; in.iy = iy; in.n_nodes = n_nodes; in.children = children;
   in.node_iy_off = node_iy_off; in.node_iy_lab = node_iy_lab; in.n_sliced = n_sliced; in.sliced = sliced;
   PlanHost h;
   std::string e = compile_plan(in, h, gemm_min);
+  if (e.empty() && tile_bits != h.tile_bits) e = retile_plan(h, tile_bits);
   if (!e.empty()) {
     if (err && err_cap > 0) {
       std::strncpy(err, e.c_str(), err_cap - 1);

@@ -132,10 +132,11 @@ __host__ __device__ inline int stream_stages(const TileDesc& d) {
   const int s = (2 * kSmemFloats) / stream_buf_words(d);
   return s < 2 ? 2 : s > kMaxStages ? kMaxStages : s;
 }
-// shared memory of a stream tile: the operand buffers, then tables
+// shared memory of a stream tile: the descriptor, the operand buffers, then
+// tables
 __host__ __device__ inline int stream_smem_words(const TileDesc& d) {
   const bool hasB = d.b_off >= 0;
-  int w = stream_stages(d) * stream_buf_words(d);
+  int w = kDescWords + stream_stages(d) * stream_buf_words(d);
   w += 1 << (d.na - d.pa);
   w += hasB ? (1 << (d.nb - d.pb)) : 0;
   w += 1 << (d.n_tc - d.pc);
@@ -146,7 +147,7 @@ __host__ __device__ inline int stream_smem_words(const TileDesc& d) {
 }
 // upper bound of stream_smem_words over every descriptor plan_tile emits
 __host__ __device__ constexpr int stream_smem_words_max() {
-  return 2 * kSmemFloats + 3 * 512 + 2 * 256 + kThreads + 5 * kMaxBits;
+  return kDescWords + 2 * kSmemFloats + 3 * 512 + 2 * 256 + kThreads + 5 * kMaxBits;
 }
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
@@ -203,22 +204,210 @@ __device__ __forceinline__ void issue_sub(T* __restrict__ dst, const T* __restri
   }
 }
 
-// Run tiles [t0, t1) of one stream-tile descriptor on this CTA: index tables
-// are built once, and the operand sub-tiles of the next stream_stages(d) - 1
-// (tile, loop step) items are copied asynchronously while the current one is
+// Per-CTA state of a run of stream tiles: shared-memory tables, the
+// thread's fixed indices and the copy / compute / store cursors.
+template <typename T>
+struct StreamRun {
+  T* buf0;
+  const int* ldA;
+  const int* ldB;
+  const int* stC;
+  const int* IAr;
+  const int* IBr;
+  T* red;
+  const int* incAg;
+  const int* incBg;
+  const int* incCg;
+  const int* incAl;
+  const int* incBl;
+  const T* A0;
+  const T* B0;
+  T* C0;
+  int NA, BUF, S;
+  int na, pa, nb, pb, pc;
+  int nloop, ntr, lo_bits, split, opt;
+  bool hasB, act;
+  int cl, s;
+  int iah[kMaxOpt], ibh[kMaxOpt];
+  int64_t n_items;
+  // prefetch cursor (tile pt, loop step pr) and its operand offsets
+  int64_t pt, issued;
+  int pr, pa_g, pb_g, pa_l, pb_l, ib;
+  // compute / store cursor
+  int64_t ct;
+  int oc, cb, rl;
+
+  __device__ __forceinline__ void issue() {
+    T* dst = buf0 + ib * BUF;
+    issue_sub<T>(dst, A0 + (pa_g + pa_l), na, pa, ldA);
+    if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), nb, pb, ldB);
+    ib = ib + 1 == S ? 0 : ib + 1;
+    if (pr + 1 < nloop) {
+      const int k = __ffs(~pr) - 1;
+      pa_l += incAl[k];
+      pb_l += incBl[k];
+      pr++;
+    } else {
+      pr = 0;
+      pa_l = pb_l = 0;
+      const int k = __ffsll(~pt) - 1;
+      pa_g += incAg[k];
+      pb_g += incBg[k];
+      pt++;
+    }
+    issued++;
+  }
+  // item `issued` into the buffer freed by the item before the current one
+  __device__ __forceinline__ void refill() {
+    if (issued < n_items) issue();
+    cp_async_commit();
+  }
+  __device__ __forceinline__ void store(const T* acc) {
+    const int cmask = (1 << pc) - 1;
+    T* Ct = C0 + oc;
+#pragma unroll
+    for (int i = 0; i < kMaxOpt; i++) {
+      if (i < opt) {
+        const int c = cl + (i << lo_bits);
+        Ct[(c & cmask) + stC[c >> pc]] = acc[i];
+      }
+    }
+  }
+  __device__ __forceinline__ void next_tile() {
+    const int k = __ffsll(~ct) - 1;
+    oc += incCg[k];
+    ct++;
+  }
+};
+
+// The loop for the common shape: two operands, no reduction split, OPT
+// outputs per thread and NTR in-tile reduction terms, all compile-time.
+// One barrier per item: after it, item `it` is visible to every thread and
+// every thread is done with item it - 1, whose buffer the refill reuses.
+template <typename T, int OPT, int NTR>
+__device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
+  int iar[NTR], ibr[NTR];
+#pragma unroll
+  for (int r = 0; r < NTR; r++) {
+    iar[r] = R.IAr[r];
+    ibr[r] = R.IBr[r];
+  }
+  T acc[kMaxOpt];
+#pragma unroll
+  for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+  const int last = R.nloop - 1;
+  for (int64_t it = 0; it < R.n_items; it++) {
+    cp_async_wait_n(R.S - 2);
+    __syncthreads();
+    R.refill();
+    const T* As = R.buf0 + R.cb * R.BUF;
+    const T* Bs = As + R.NA;
+    R.cb = R.cb + 1 == R.S ? 0 : R.cb + 1;
+    if (R.act) {
+#pragma unroll
+      for (int i = 0; i < OPT; i++) {
+        T a = acc[i];
+#pragma unroll
+        for (int r = 0; r < NTR; r++) a = Trop<T>::mac(a, As[R.iah[i] ^ iar[r]], Bs[R.ibh[i] ^ ibr[r]]);
+        acc[i] = a;
+      }
+    }
+    if (R.rl == last) {
+      if (R.act) R.store(acc);
+#pragma unroll
+      for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+      R.next_tile();
+      R.rl = 0;
+    } else {
+      R.rl++;
+    }
+  }
+}
+
+// Any shape: unary nodes, reduction splits, longer in-tile reductions.
+template <typename T>
+__device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
+  const int t = threadIdx.x;
+  T acc[kMaxOpt];
+#pragma unroll
+  for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+  const int step = 1 << R.split;
+  const int last = R.nloop - 1;
+  for (int64_t it = 0; it < R.n_items; it++) {
+    cp_async_wait_n(R.S - 2);
+    __syncthreads();
+    R.refill();
+    const T* As = R.buf0 + R.cb * R.BUF;
+    const T* Bs = As + R.NA;
+    R.cb = R.cb + 1 == R.S ? 0 : R.cb + 1;
+    if (R.act) {
+#pragma unroll
+      for (int i = 0; i < kMaxOpt; i++) {
+        if (i < R.opt) {
+          T a = acc[i];
+          const int ia = R.iah[i], ib = R.ibh[i];
+          if (R.hasB) {
+            for (int r = R.s; r < R.ntr; r += step) a = Trop<T>::mac(a, As[ia ^ R.IAr[r]], Bs[ib ^ R.IBr[r]]);
+          } else {
+            for (int r = R.s; r < R.ntr; r += step) a = Trop<T>::mx(a, As[ia ^ R.IAr[r]]);
+          }
+          acc[i] = a;
+        }
+      }
+    }
+    if (R.rl == last) {
+      if (R.split > 0) {
+        // red[] of the previous tile was read before this item's barrier
+        R.red[t] = acc[0];
+        __syncthreads();
+        if (R.act && R.s == 0) {
+          T a = acc[0];
+          for (int s2 = 1; s2 < step; s2++) a = Trop<T>::mx(a, R.red[R.cl + (s2 << R.lo_bits)]);
+          acc[0] = a;
+        }
+      }
+      if (R.act && R.s == 0) R.store(acc);
+#pragma unroll
+      for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+      R.next_tile();
+      R.rl = 0;
+    } else {
+      R.rl++;
+    }
+  }
+}
+
+// Run tiles [t0, t1) of one stream-tile descriptor on this CTA: the
+// descriptor is copied to shared memory and the index tables built from it
+// once, and the operand sub-tiles of the next stream_stages(d) - 1 (tile,
+// loop step) items are copied asynchronously while the current one is
 // reduced.
 template <typename T>
-__device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __restrict__ arena,
+__device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __restrict__ arena,
                              int* __restrict__ smem) {
   const int t = threadIdx.x;
-  const bool hasB = d.b_off >= 0;
-  const int NA = stream_a_words(d);  // A region (padded), B region follows
-  const int BUF = stream_buf_words(d);
-  const int S = stream_stages(d);
-  T* buf0 = reinterpret_cast<T*>(smem);
-  int* ldA = reinterpret_cast<int*>(buf0 + S * BUF);
+  __syncthreads();  // the previous user of this shared memory is done
+  {
+    const int* src = reinterpret_cast<const int*>(&dg);
+    for (int j = t; j < (int)(sizeof(TileDesc) / 4); j += kThreads) smem[j] = src[j];
+  }
+  __syncthreads();
+  const TileDesc& d = *reinterpret_cast<const TileDesc*>(smem);
+  StreamRun<T> R;
+  R.hasB = d.b_off >= 0;
+  R.NA = stream_a_words(d);  // A region (padded), B region follows
+  R.BUF = stream_buf_words(d);
+  R.S = stream_stages(d);
+  R.na = d.na;
+  R.pa = d.pa;
+  R.nb = d.nb;
+  R.pb = d.pb;
+  R.pc = d.pc;
+  T* buf0 = reinterpret_cast<T*>(smem + kDescWords);
+  R.buf0 = buf0;
+  int* ldA = reinterpret_cast<int*>(buf0 + R.S * R.BUF);
   const int nAh = 1 << (d.na - d.pa);
-  const int nBh = hasB ? (1 << (d.nb - d.pb)) : 0;
+  const int nBh = R.hasB ? (1 << (d.nb - d.pb)) : 0;
   const int nCh = 1 << (d.n_tc - d.pc);
   const int ntr = 1 << d.n_tr;
   int* ldB = ldA + nAh;
@@ -229,12 +418,6 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
   // increments of the grid / loop offsets when the index goes from x to x+1
   // with k trailing ones: +2^pos_k - sum_{i<k} 2^pos_i (pos -1: no term)
   int* incAg = reinterpret_cast<int*>(red + kThreads);
-  int* incBg = incAg + kMaxBits;
-  int* incCg = incBg + kMaxBits;
-  int* incAl = incCg + kMaxBits;
-  int* incBl = incAl + kMaxBits;
-
-  __syncthreads();  // the previous user of this shared memory is done
   for (int j = t; j < nAh; j += kThreads) {
     int o = 0;
     for (int b = 0; b < d.na - d.pa; b++)
@@ -276,36 +459,47 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
     }
     incAg[which * kMaxBits + k] = v;
   }
+  R.ldA = ldA;
+  R.ldB = ldB;
+  R.stC = stC;
+  R.IAr = IAr;
+  R.IBr = IBr;
+  R.red = red;
+  R.incAg = incAg;
+  R.incBg = incAg + kMaxBits;
+  R.incCg = incAg + 2 * kMaxBits;
+  R.incAl = incAg + 3 * kMaxBits;
+  R.incBl = incAg + 4 * kMaxBits;
 
   // thread -> (output, reduction split)
-  const int lo_bits = d.n_tc < 8 ? d.n_tc : 8;
-  const int split = d.split_log2;
-  const int active = 1 << (lo_bits + split);
-  const int opt = 1 << (d.n_tc - lo_bits);
-  const bool act = t < active;
-  const int cl = t & ((1 << lo_bits) - 1);
-  const int s = t >> lo_bits;
+  R.lo_bits = d.n_tc < 8 ? d.n_tc : 8;
+  R.split = d.split_log2;
+  const int active = 1 << (R.lo_bits + R.split);
+  R.opt = 1 << (d.n_tc - R.lo_bits);
+  R.act = t < active;
+  R.cl = t & ((1 << R.lo_bits) - 1);
+  R.s = t >> R.lo_bits;
+  R.ntr = ntr;
   int iat = 0, ibt = 0;
-  for (int b = 0; b < lo_bits; b++) {
-    if ((cl >> b) & 1) {
+  for (int b = 0; b < R.lo_bits; b++) {
+    if ((R.cl >> b) & 1) {
       if (d.tc_a[b] >= 0) iat |= 1 << d.tc_a[b];
       if (d.tc_b[b] >= 0) ibt |= 1 << d.tc_b[b];
     }
   }
   iat = swz16(iat);
   ibt = swz16(ibt);
-  int iah[kMaxOpt], ibh[kMaxOpt];
 #pragma unroll
   for (int i = 0; i < kMaxOpt; i++) {
     int xa = 0, xb = 0;
-    for (int b = lo_bits; b < d.n_tc; b++) {
-      if (((i << lo_bits) >> b) & 1) {
+    for (int b = R.lo_bits; b < d.n_tc; b++) {
+      if (((i << R.lo_bits) >> b) & 1) {
         if (d.tc_a[b] >= 0) xa |= 1 << d.tc_a[b];
         if (d.tc_b[b] >= 0) xb |= 1 << d.tc_b[b];
       }
     }
-    iah[i] = iat ^ swz16(xa);
-    ibh[i] = ibt ^ swz16(xb);
+    R.iah[i] = iat ^ swz16(xa);
+    R.ibh[i] = ibt ^ swz16(xb);
   }
   // absolute grid offsets of the first tile (32-bit within each tensor)
   int ga = 0, gb = 0, gc = 0;
@@ -316,141 +510,42 @@ __device__ void stream_tiles(const TileDesc& d, int64_t t0, int64_t t1, T* __res
       gc += 1 << d.g_pc[i];
     }
   }
+  R.nloop = 1 << d.n_loop;
+  R.n_items = (t1 - t0) * R.nloop;
+  R.A0 = arena + d.a_off;
+  R.B0 = arena + (R.hasB ? d.b_off : 0);
+  R.C0 = arena + d.c_off;
+  R.pt = t0;
+  R.issued = 0;
+  R.pr = 0;
+  R.pa_g = ga;
+  R.pb_g = gb;
+  R.pa_l = R.pb_l = 0;
+  R.ib = 0;
+  R.ct = t0;
+  R.oc = gc;
+  R.cb = 0;
+  R.rl = 0;
+  const bool fixed = R.hasB && R.split == 0 && ntr <= 4;
+  const int shape = R.opt * 8 + ntr;
   __syncthreads();  // tables ready
-  // reduction tables in registers when they are short (the common case)
-  constexpr int kRr = 4;
-  int iar[kRr], ibr[kRr];
-#pragma unroll
-  for (int r = 0; r < kRr; r++) {
-    iar[r] = r < ntr ? IAr[r] : 0;
-    ibr[r] = r < ntr ? IBr[r] : 0;
-  }
-  const bool small_r = ntr <= kRr && split == 0;
-
-  const int nloop = 1 << d.n_loop;
-  const int64_t n_items = (t1 - t0) * nloop;
-  const T* A0 = arena + d.a_off;
-  const T* B0 = arena + (hasB ? d.b_off : 0);
-  T* C0 = arena + d.c_off;
-  // prefetch cursor: tile pt, loop step pr, offsets
-  int64_t pt = t0;
-  int pr = 0, pa_g = ga, pb_g = gb, pa_l = 0, pb_l = 0;
-  int ib = 0;  // buffer of the next issue
-  auto issue = [&]() {
-    T* dst = buf0 + ib * BUF;
-    issue_sub<T>(dst, A0 + (pa_g + pa_l), d.na, d.pa, ldA);
-    if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), d.nb, d.pb, ldB);
-    ib = ib + 1 == S ? 0 : ib + 1;
-  };
-  auto advance = [&]() {
-    if (pr + 1 < nloop) {
-      const int k = __ffs(~pr) - 1;
-      pa_l += incAl[k];
-      pb_l += incBl[k];
-      pr++;
-    } else {
-      pr = 0;
-      pa_l = pb_l = 0;
-      const int k = __ffsll(~pt) - 1;
-      pa_g += incAg[k];
-      pb_g += incBg[k];
-      pt++;
-    }
-  };
-  int64_t ct = t0;  // tile of the compute / store cursor
-  int oc = gc;
-
-  T acc[kMaxOpt];
   // prologue: items 0 .. S-2, one commit group each (empty past the end)
-  int64_t issued = 0;
-  for (int k = 0; k < S - 1; k++) {
-    if (issued < n_items) {
-      issue();
-      advance();
-      issued++;
+  for (int k = 0; k < R.S - 1; k++) R.refill();
+  if (fixed) {
+    switch (shape) {
+      case 1 * 8 + 1: stream_loop_fixed<T, 1, 1>(R); break;
+      case 1 * 8 + 2: stream_loop_fixed<T, 1, 2>(R); break;
+      case 1 * 8 + 4: stream_loop_fixed<T, 1, 4>(R); break;
+      case 2 * 8 + 1: stream_loop_fixed<T, 2, 1>(R); break;
+      case 2 * 8 + 2: stream_loop_fixed<T, 2, 2>(R); break;
+      case 2 * 8 + 4: stream_loop_fixed<T, 2, 4>(R); break;
+      case 4 * 8 + 1: stream_loop_fixed<T, 4, 1>(R); break;
+      case 4 * 8 + 2: stream_loop_fixed<T, 4, 2>(R); break;
+      case 4 * 8 + 4: stream_loop_fixed<T, 4, 4>(R); break;
+      default: stream_loop_any<T>(R); break;
     }
-    cp_async_commit();
-  }
-  int cb = 0;  // buffer of the item being reduced
-  for (int64_t it = 0; it < n_items; it++) {
-    // item it + S - 1 goes to the buffer item it - 1 used (released by the
-    // barrier that closed the previous iteration)
-    if (issued < n_items) {
-      issue();
-      advance();
-      issued++;
-    }
-    cp_async_commit();
-    cp_async_wait_n(S - 1);  // groups 0..it are complete
-    __syncthreads();         // item `it` is in its buffer for every thread
-    const int rl = (int)(it % nloop);
-    if (rl == 0) {
-#pragma unroll
-      for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
-    }
-    const T* As = buf0 + cb * BUF;
-    const T* Bs = As + NA;
-    cb = cb + 1 == S ? 0 : cb + 1;
-    if (act) {
-      if (small_r) {
-#pragma unroll
-        for (int i = 0; i < kMaxOpt; i++) {
-          if (i < opt) {
-            T a = acc[i];
-            const int ia = iah[i], ib = ibh[i];
-#pragma unroll
-            for (int r = 0; r < kRr; r++) {
-              if (r < ntr) {
-                if (hasB) a = Trop<T>::mac(a, As[ia ^ iar[r]], Bs[ib ^ ibr[r]]);
-                else a = Trop<T>::mx(a, As[ia ^ iar[r]]);
-              }
-            }
-            acc[i] = a;
-          }
-        }
-      } else {
-        const int step = 1 << split;
-#pragma unroll
-        for (int i = 0; i < kMaxOpt; i++) {
-          if (i < opt) {
-            T a = acc[i];
-            const int ia = iah[i], ib = ibh[i];
-            if (hasB) {
-              for (int r = s; r < ntr; r += step) a = Trop<T>::mac(a, As[ia ^ IAr[r]], Bs[ib ^ IBr[r]]);
-            } else {
-              for (int r = s; r < ntr; r += step) a = Trop<T>::mx(a, As[ia ^ IAr[r]]);
-            }
-            acc[i] = a;
-          }
-        }
-      }
-    }
-    if (rl == nloop - 1) {
-      if (split > 0) {
-        red[t] = acc[0];
-        __syncthreads();
-        if (act && s == 0) {
-          T a = acc[0];
-          for (int s2 = 1; s2 < (1 << split); s2++) a = Trop<T>::mx(a, red[cl + (s2 << lo_bits)]);
-          acc[0] = a;
-        }
-      }
-      if (act && s == 0) {
-        const int cmask = (1 << d.pc) - 1;
-        T* Ct = C0 + oc;
-#pragma unroll
-        for (int i = 0; i < kMaxOpt; i++) {
-          if (i < opt) {
-            const int c = cl + (i << lo_bits);
-            Ct[(c & cmask) + stC[c >> d.pc]] = acc[i];
-          }
-        }
-      }
-      const int k = __ffsll(~ct) - 1;
-      oc += incCg[k];
-      ct++;
-    }
-    __syncthreads();  // this item's buffer is free for item it + S
+  } else {
+    stream_loop_any<T>(R);
   }
   cp_async_wait<0>();
 }

@@ -534,7 +534,9 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       p.gemms.push_back(g);
     } else {
       TileDesc d;
-      if (!(e = plan_tile(p.flabels[a], &p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], d)).empty())
+      if (!(e = plan_tile(p.flabels[a], &p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], d,
+                          p.tile_bits))
+               .empty())
         return "node " + std::to_string(j) + ": " + e;
       st.kind = STEP_TILE;
       st.desc = (int32_t)p.tiles.size();
@@ -582,6 +584,36 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       return "plain lowering of node " + std::to_string(j) + ": " + e;
   }
   p.plain_elems = fused_end + scratch;
+  return "";
+}
+
+std::string retile_plan(PlanHost& p, int bits) {
+  if (bits < 8 || bits > 10) return "tile bits outside 8..10";
+  const int T = p.n_tensors;
+  if (p.n_nodes == 0) {
+    p.tile_bits = bits;
+    return "";
+  }
+  std::vector<TileDesc> tiles = p.tiles;
+  std::vector<Step> steps = p.steps;
+  int64_t total = 0;
+  for (size_t si = 0; si < steps.size(); si++) {
+    Step& st = steps[si];
+    if (st.kind == STEP_TILE) {
+      const int j = (int)si - 1;  // step 1 + j runs node j
+      const int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+      TileDesc d;
+      std::string e = plan_tile(p.flabels[a], &p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], d, bits);
+      if (!e.empty()) return "node " + std::to_string(j) + ": " + e;
+      tiles[st.desc] = d;
+      st.n_tiles = d.n_tiles;
+    }
+    total += st.n_tiles;
+  }
+  p.tiles.swap(tiles);
+  p.steps.swap(steps);
+  p.total_tiles = total;
+  p.tile_bits = bits;
   return "";
 }
 

@@ -60,10 +60,15 @@ struct PlanHost {
 
   double tc = 0, sc = 0, rwc = 0, ops = 0, bytes = 0;
   int64_t total_tiles = 0;
+  int32_t tile_bits = 9;                       // stream tiles grow to 2^tile_bits outputs
 };
 
 // Compile; returns "" on success or an error message.
 std::string compile_plan(const PlanInput& in, PlanHost& out, int gemm_min_log2);
+
+// Re-plan every stream-tile step of the fused form with tiles of up to
+// 2^bits outputs (8..10); GEMM steps and the arena layout are unchanged.
+std::string retile_plan(PlanHost& p, int bits);
 
 // Plan one stream tile for C = max_{R} A (+ B).  A, C (and B if non-null)
 // are label lists in their memory order.  Returns "" or an error.

@@ -43,6 +43,10 @@ struct TileDesc {
   int8_t tc_a[kMaxTileBits], tc_b[kMaxTileBits];          // Tc bit -> A / B tile bit (-1)
   int8_t tr_a[kMaxTileBits], tr_b[kMaxTileBits];          // Tr bit -> A / B tile bit (-1)
 };
+// a TileDesc copied to the front of a stream tile's shared memory, padded
+// so the operand buffers after it start on a 16-byte boundary
+constexpr int kDescWords = 108;
+static_assert(sizeof(TileDesc) <= kDescWords * 4 && kDescWords % 4 == 0, "descriptor copy");
 
 // Register-blocked GEMM for a contraction node with large M, N and K label
 // groups.  The plan compiler lays the operands out "k-pair interleaved":

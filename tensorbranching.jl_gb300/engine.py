@@ -96,8 +96,8 @@ class Engine:
             p.bind_mis(weights)
         return p
 
-    def solve_batch(self, plans, slice_vals=None, r=None, mode: str = "batched"):
-        """Per-item results (max root + r) and their max."""
+    @staticmethod
+    def _batch_args(plans, slice_vals, r):
         n = len(plans)
         arr = (c_void_p * n)(*[p.handle for p in plans])
         sv = None
@@ -108,6 +108,23 @@ class Engine:
             if sv.size == 0:
                 sv = None
         rr = None if r is None else np.ascontiguousarray(r, dtype=np.float32)
+        return n, arr, sv, rr
+
+    def autotune(self, plans, slice_vals=None, r=None) -> dict:
+        """tb_autotune on this batch: tile size and schedule by timing; the
+        choice serves later mode="auto" solves."""
+        n, arr, sv, rr = self._batch_args(plans, slice_vals, r)
+        res = _native.TbTuneResult()
+        st = self.lib.tb_autotune(self.ctx, n, ctypes.cast(arr, c_void_p), None if sv is None else sv.ctypes.data,
+                                  None if rr is None else rr.ctypes.data, ctypes.byref(res))
+        _native.check(st, self.ctx)
+        names = {v: k for k, v in _native.MODES.items()}
+        return {"mode": names[res.mode], "tile_bits": res.tile_bits, "ctas_per_sm": res.ctas_per_sm,
+                "chunk_div": res.chunk_div, "ms": res.ms, "ms_default": res.ms_default, "n_tried": res.n_tried}
+
+    def solve_batch(self, plans, slice_vals=None, r=None, mode: str = "batched"):
+        """Per-item results (max root + r) and their max."""
+        n, arr, sv, rr = self._batch_args(plans, slice_vals, r)
         out = np.zeros(n, np.float32)
         mx = np.zeros(1, np.float32)
         st = self.lib.tb_solve_batch(self.ctx, n, ctypes.cast(arr, c_void_p),

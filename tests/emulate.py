@@ -21,6 +21,7 @@ KMAXTILE = 16
 KTHREADS = 256
 KMAXOPT = 4
 KSMEM = 8192
+KDESCWORDS = 108  # descriptor copy in front of the operand buffers
 
 
 class TileDesc(ctypes.Structure):
@@ -73,10 +74,10 @@ def check_layout(lib):
     assert list(out)[:5] == want, (list(out), want)
 
 
-def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4):
+def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4, tile_bits=9):
     lib.tbi_plan_describe.restype = c_int32
     lib.tbi_plan_describe.argtypes = [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p,
-                                      c_void_p, c_void_p, c_int32, c_void_p, c_int32, ctypes.POINTER(c_void_p),
+                                      c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_int32, ctypes.POINTER(c_void_p),
                                       ctypes.POINTER(c_int64), ctypes.c_char_p, c_int32]
     lib.tbi_free.argtypes = [c_void_p]
     lib.tbi_sizes.argtypes = [c_void_p, c_int32]
@@ -93,7 +94,7 @@ def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4):
                                iy.ctypes.data, code.n_nodes, ch.ctypes.data,
                                None if noff is None else noff.ctypes.data,
                                None if nlab is None else nlab.ctypes.data, len(sliced), sl.ctypes.data,
-                               gemm_min, ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
+                               gemm_min, tile_bits, ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
     if rc:
         raise ValueError(err.value.decode())
     raw = ctypes.string_at(blob, nbytes.value)
@@ -150,7 +151,7 @@ def stages(d):
 
 def smem_words(d):
     hasB = d.b_off >= 0
-    w = stages(d) * buf_words(d)
+    w = KDESCWORDS + stages(d) * buf_words(d)
     w += 1 << (d.na - d.pa)
     w += (1 << (d.nb - d.pb)) if hasB else 0
     w += 1 << (d.n_tc - d.pc)
@@ -160,7 +161,7 @@ def smem_words(d):
 
 
 def max_smem_words():
-    return 2 * KSMEM + 3 * 512 + 2 * 256 + KTHREADS
+    return KDESCWORDS + 2 * KSMEM + 3 * 512 + 2 * 256 + KTHREADS
 
 
 def tensor_rank(tile_pos, grid_pos, loop_pos):
@@ -260,7 +261,7 @@ def emu_stream_tile(d, arena, written, expect=None):
                 assert g.min() >= lo and g.max() < hi_b, "global load out of bounds"
                 # async copies: 16 bytes when p >= 2, 8 when p == 1; both ends aligned
                 for b in range(stages(d)):  # every pipeline buffer
-                    dst = b * buf_words(d) + region + swz(j)
+                    dst = KDESCWORDS + b * buf_words(d) + region + swz(j)
                     if p >= 2:
                         assert np.all(g[::4] % 4 == 0), "misaligned 16-byte global source"
                         assert np.all(dst[::4] % 4 == 0), "misaligned 16-byte shared destination"

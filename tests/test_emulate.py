@@ -101,3 +101,21 @@ def test_gemm_steps(tb, orc, lib, shape):
     assert np.array_equal(root, ref)
     for a, b in zip(nodes, dumps):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("bits", [8, 10])
+def test_tile_sizes_of_the_autotuner(tb, orc, lib, bits):
+    """Every stream tile size tb_autotune may pick (tile_bits 8..10) keeps
+    every access in bounds and every intermediate equal to the oracle's."""
+    for g, w, code in (rr_case(tb, 60, 3), ksg_case(tb, 8, 2)):
+        D = emulate.describe(lib, code, tile_bits=bits)
+        root, nodes = emulate.run_fused(D, w, ())
+        ref, dumps = orc.execute(code, w, dump=True)
+        assert np.array_equal(root, ref)
+        for a, c in zip(nodes, dumps or []):
+            assert np.array_equal(a, c)
+    # the knob changes the tiling
+    g, w, code = rr_case(tb, 60, 3)
+    n8 = sum(s.n_tiles for s in emulate.describe(lib, code, tile_bits=8)["steps"])
+    n10 = sum(s.n_tiles for s in emulate.describe(lib, code, tile_bits=10)["steps"])
+    assert n8 > n10
