@@ -274,10 +274,20 @@ def run_cpu_baseline(tb, orc, wl, budget_s: float):
         best = (code.n_nodes - 1, len(nodes), sub[-1], dt)
         rate = sub[-1] / dt
     j, nn, sops, dt = best
+    reps = 1
+    if dt < budget_s / 3:
+        # a short sample: repeat it to about a third of the budget
+        s_code, _ = _subtree(tb, code, labs, j)
+        reps = max(1, int(budget_s / 3 / max(dt, 1e-3)))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            orc.execute(s_code, w, mode="gemm")
+        dt = (time.perf_counter() - t0) / reps
     graphs = len(wl["graphs"]) if wl["name"] == "rr100_b10" else 1
     solves_per_s = (sops / dt) / total_ops * graphs
     sample = (f"subtree of {nn} of {code.n_nodes} contraction nodes of the first network ({sops:.3g} of "
-              f"{total_ops:.3g} tropical ops per step) in {dt:.2f}s; solves/s extrapolated by algorithmic ops")
+              f"{total_ops:.3g} tropical ops per step) in {dt:.2f}s (mean of {reps}); solves/s extrapolated by "
+              f"algorithmic ops")
     return {"value": solves_per_s, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
             "ops_per_s": sops / dt}
 
@@ -508,8 +518,8 @@ def run_serve(tb, args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic serving mix (seeded)",
            "config": {"workload": "serve", "requests": len(preps),
-                      "detail": "Poisson arrivals at 0.8x measured capacity; 3-regular n in [60,400] and KSG L in "
-                                "[10,36] filling 0.8; unit or U{1..10} weights; sc capped at 24 by index slicing",
+                      "detail": "Poisson arrivals at 0.8x measured capacity; 3-regular n in [60,200] and KSG L in "
+                                "[10,24] filling 0.8; unit or U{1..10} weights; sc capped at 24 by index slicing",
                       "arrival_rate_per_s": rate, "capacity_solves_per_s": capacity,
                       "items": int(sum(p.n_items for p in preps)), "host_prep_s": prep_s},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),

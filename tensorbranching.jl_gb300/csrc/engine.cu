@@ -1369,6 +1369,52 @@ __global__ void __launch_bounds__(256) k_peak_f32(float* out, int iters, float s
   if (s == 1.2345f) out[0] = s;
 }
 
+// Test hook for the bounded waits of the persistent executor: one item whose
+// chunk list keeps only the final step, so the wait on the root's done
+// counter is never satisfied.  The wait gives up after timeout_ms, the kernel
+// sets the error word and returns, and the hook returns TB_ERR_TIMEOUT; the
+// context stays usable (the next batch is uploaded afresh).
+extern "C" int32_t tbi_timeout_probe(tb_ctx* c, tb_plan* p, int32_t timeout_ms) {
+  if (!c || !p || p->ctx != c || timeout_ms <= 0) return fail(TB_ERR_INVALID, "bad probe arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (c->opt.dtype != TB_DTYPE_F32) return fail(TB_ERR_UNSUPPORTED, "the probe runs f32 contexts");
+  if (!p->h.has_weights) return fail(TB_ERR_INVALID, "plan has no bound weights");
+  CU(cudaSetDevice(c->device));
+  tb_status st = set_kernel_attrs<float>();
+  if (st) return st;
+  if ((st = upload_plan(p))) return st;
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  c->have_key = false;
+  std::vector<int64_t> aoff(1, 0), svoff(1, 0);
+  CU(c->arena.ensure((size_t)p->h.arena_elems * sizeof(float) + 256));
+  CU(c->slice_vals.ensure(16));
+  CU(c->out_item.ensure(sizeof(float) * 2));
+  CU(c->rvals.ensure(16));
+  if ((st = upload_batch<float>(c, 1, &p, aoff, svoff, false))) return st;
+  Chunk* ch = reinterpret_cast<Chunk*>(c->chunks.p);
+  // the final step comes last (highest level): make it the only chunk
+  CU(cudaMemcpyAsync(ch, ch + (c->n_chunks - 1), sizeof(Chunk), cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaMemsetAsync(c->misc.p, 0, 64, c->stream));
+  CU(cudaMemsetAsync(c->done.p, 0, sizeof(int) * p->h.steps.size(), c->stream));
+  CU(cudaMemsetAsync(c->rvals.p, 0, 16, c->stream));
+  unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
+  int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
+  k_persistent<float><<<c->persistent_ctas, kThreads, max_stream_smem_bytes(), c->stream>>>(
+      reinterpret_cast<const ItemDev<float>*>(c->items.p), reinterpret_cast<const Group*>(c->groups.p), ch, 1,
+      reinterpret_cast<int*>(c->done.p), ticket, err, reinterpret_cast<float*>(c->out_item.p),
+      reinterpret_cast<const float*>(c->rvals.p), (int64_t)timeout_ms * 1000000LL);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(c->stream));
+  int e = 0;
+  CU(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+  c->have_key = false;
+  if (e == TB_ERR_TIMEOUT) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
+  return e ? fail(TB_ERR_CUDA, "unexpected device error word") : TB_OK;
+}
+
 extern "C" int32_t tbi_measure_maxplus_peak(int32_t device, double* ops_per_s) {
   if (!ops_per_s) return TB_ERR_INVALID;
   CU(cudaSetDevice(device));

@@ -1,0 +1,35 @@
+"""The reference's entry point end to end on the GPU: dynamic_ob_mis with
+ContractionTreeSlicer(sc_target=10) on 3-regular graphs equals the exact MIS
+(test/dynamic_ob.jl:10-52), and every known-answer case of
+tests/golden/mis_known.json solves to its stored value in one batch."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.parametrize("seed", range(3))
+@pytest.mark.parametrize("mode", ["batched", "plain"])
+def test_dynamic_ob_mis(tb, exact, engine, seed, mode):
+    g = tb.random_regular_graph(80, 3, seed)
+    w = tb.random_weights(g.n, seed) if seed % 2 else np.ones(g.n, np.float32)
+    slicer = tb.ContractionTreeSlicer(sc_target=10)
+    got = tb.dynamic_ob_mis(g, w, slicer=slicer, engine=engine, mode=mode)
+    assert got == pytest.approx(exact.branch_and_bound(g.n, g.edges, w))
+
+
+def test_golden_cases_in_one_batch(tb, engine):
+    cases = json.load(open(os.path.join(HERE, "golden", "mis_known.json")))["cases"]
+    plans, want = [], []
+    for c in cases:
+        g = tb.Graph(c["n"], [tuple(e) for e in c["edges"]])
+        w = np.ones(c["n"], np.float32) if c["weights"] is None else np.array(c["weights"], np.float32)
+        plans.append(engine.plan(tb.initialize_code(g, tb.GreedyMethod(1)), w))
+        want.append(c["mis"])
+    for mode in ("batched", "layered"):
+        out, mx = engine.solve_batch(plans, mode=mode)
+        assert np.array_equal(out, np.array(want, np.float32)), mode
