@@ -108,9 +108,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_level(const ItemDev<T>* items, 
                                                    float* out_item, const float* r, int* err) {
   extern __shared__ int tb_smem[];
   __shared__ int s_g;
-  if constexpr (KINDS == 1) {
+  {
     // CTA b runs tickets [b * chunk, (b + 1) * chunk) of this level, a run of
-    // tiles per group so each stream tile builds its tables once
+    // tiles per group: each stream tile builds its tables once, each GEMM run
+    // keeps one copy pipeline across its tiles
     int64_t tk = first_ticket + (int64_t)blockIdx.x * chunk;
     const int64_t end = tk + chunk < last_ticket ? tk + chunk : last_ticket;
     while (tk < end) {
@@ -122,20 +123,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_level(const ItemDev<T>* items, 
       const int64_t g_end = gi + 1 < n_groups && groups[gi + 1].first < end ? groups[gi + 1].first : end;
       const ItemDev<T>& it = items[g.item];
       const Step& st = it.steps[g.step];
-      if (st.kind == STEP_TILE) {
+      if ((KINDS & 1) && st.kind == STEP_TILE) {
         stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem);
+      } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
+        gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err);
       } else {
         for (int64_t x = tk; x < g_end; x++) run_step<T, KINDS>(it, st, x - g.first, tb_smem, out_item, r, g.item, err);
       }
       tk = g_end;
     }
-  } else {
-    int64_t tk = first_ticket + blockIdx.x;
-    if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
-    __syncthreads();
-    const Group g = groups[s_g];
-    const ItemDev<T>& it = items[g.item];
-    run_step<T, KINDS>(it, it.steps[g.step], tk - g.first, tb_smem, out_item, r, g.item, err);
   }
 }
 
@@ -186,6 +182,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
     const Step& st = it.steps[g.step];
     if (st.kind == STEP_TILE) {
       stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem);
+    } else if (st.kind == STEP_GEMM) {
+      gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
     } else {
       for (int64_t x = ch.t0; x < ch.t1; x++) run_step<T>(it, st, x, tb_smem, out_item, r, g.item, err);
     }
@@ -292,6 +290,7 @@ struct tb_ctx {
   int sms = 0;
   int persistent_ctas = 0;
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
+  int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   size_t budget = 0;
   DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals;
   HostBuf h_items, h_groups, h_chunks, h_in, h_out;
@@ -516,6 +515,9 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
       const int64_t div = std::max(1, c->chunk_div) * ctas;
       cs = std::max((nt + ctas - 1) / ctas, (lt + div - 1) / div);
       cs = std::max<int64_t>(1, std::min<int64_t>(cs, 256));
+    } else if (st.kind == STEP_GEMM) {
+      // runs of GEMM units share one copy pipeline; keep >= 1 run per CTA
+      cs = std::max<int64_t>(1, std::min<int64_t>(nt / ctas, 64));
     } else if (st.kind == STEP_LEAVES) {
       cs = nt;
     }
@@ -573,8 +575,10 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
     for (auto& lr : c->level_ranges) {
       if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
       if (lr.kinds == 2) {
-        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), s>>>(
-            items, groups, c->n_groups, lr.first, lr.first + lr.count, 1, out_item, rv, err);
+        const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
+        k_level<T, 2><<<(unsigned)grid, kThreads, smem_bytes(2), s>>>(
+            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv,
+            err);
       } else {
         const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
         k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), s>>>(
@@ -933,6 +937,12 @@ tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
   else
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_stream, k_level<int32_t, 1>, kThreads, smem_bytes(1)));
   c->stream_ctas = std::max(1, per_sm_stream) * c->sms;
+  int per_sm_gemm = 0;
+  if (c->opt.dtype == TB_DTYPE_F32)
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_gemm, k_level<float, 2>, kThreads, smem_bytes(2)));
+  else
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_gemm, k_level<int32_t, 2>, kThreads, smem_bytes(2)));
+  c->gemm_ctas = std::max(1, per_sm_gemm) * c->sms;
   *out = c.release();
   return TB_OK;
 }
@@ -974,6 +984,7 @@ tb_status tb_plan_create(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const
   in.sliced = sliced;
   std::unique_ptr<tb_plan> p(new tb_plan());
   p->ctx = ctx;
+  p->h.gemm_ctas = ctx->gemm_ctas;
   std::string e;
   try {
     e = compile_plan(in, p->h, 4);
@@ -1145,8 +1156,10 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
     float* oi = reinterpret_cast<float*>(c->out_item.p);
     for (auto& lr : c->level_ranges) {
       if (lr.kinds == 2) {
-        k_level<T, 2><<<(unsigned)lr.count, kThreads, smem_bytes(2), c->stream>>>(
-            items, groups, c->n_groups, lr.first, lr.first + lr.count, 1, oi, nullptr, err);
+        const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
+        k_level<T, 2><<<(unsigned)grid, kThreads, smem_bytes(2), c->stream>>>(
+            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr,
+            err);
       } else {
         const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
         k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), c->stream>>>(
@@ -1642,8 +1655,9 @@ static tb_status serve_step(Server* S) {
   }
   if (t2 > 0) {
     if (t2 > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "step too large for one launch");
-    k_level<T, 2><<<(unsigned)t2, kThreads, smem_bytes(2), s>>>(di, dg + g1.size(), (int)g2.size(), 0, t2, 1, dout,
-                                                                drv, derr);
+    const int64_t grid2 = std::min<int64_t>(t2, c->gemm_ctas);
+    k_level<T, 2><<<(unsigned)grid2, kThreads, smem_bytes(2), s>>>(di, dg + g1.size(), (int)g2.size(), 0, t2,
+                                                                   (t2 + grid2 - 1) / grid2, dout, drv, derr);
     CU(cudaGetLastError());
     S->launches++;
   }

@@ -829,31 +829,70 @@ struct GemmSmem {
   static constexpr int BAR_BYTES = 128;  // full[S] and empty[S] mbarriers
   static constexpr int A_STAGE = KP * BM * 2;  // elements
   static constexpr int B_STAGE = KP * BN * 2;
-  static constexpr int BYTES = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;
+  static constexpr int SCAT_OFF = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;  // epilogue tables
+  static constexpr int BYTES = SCAT_OFF + (BM + BN) * 4;
 };
 
-// One BM x BN output tile of batch point b.  Returns false after a timed-out
+// Work units [u0, u1) of one GEMM descriptor on this CTA: unit u is output
+// tile mn = u mod tiles_mn of batch point b and K part p (u / tiles_mn =
+// p 2^bt + b).  The copies of every (unit, K chunk) of the run go through one
+// ring of S stages, so the next unit's operands load while this unit's last
+// chunks are reduced and its tile is stored.  Returns false after a timed-out
+// wait (err is set; copies in flight are drained with a bounded wait).
+// Copies of chunk q of a run (unit u0 + q / nkp, K chunk p nkp + q mod nkp)
+// into stage `slot`; thread 0 only.  Everything is recomputed from the
+// descriptor so none of it stays live in the consumers' registers.
+template <typename T, int BM, int BN, int S, int BK>
+__device__ __forceinline__ void gemm_issue(const GemmDesc& d, int64_t u0, int q, int slot, const T* arena,
+                                           int* smem) {
+  using SM = GemmSmem<BM, BN, S, BK>;
+  constexpr int KP = SM::KP;
+  constexpr int BK_LOG2 = BK == 32 ? 5 : 4;
+  const int nkp_log2 = d.k_log2 - BK_LOG2 - d.ks_log2;
+  const int tm_log2 = d.m_log2 - d.bm_log2, tmn_log2 = tm_log2 + d.n_log2 - d.bn_log2;
+  const int64_t u = u0 + (q >> nkp_log2);
+  const int64_t mn = u & ((int64_t(1) << tmn_log2) - 1), rest = u >> tmn_log2;
+  const int64_t b = rest & ((int64_t(1) << d.bt_log2) - 1), part = rest >> d.bt_log2;
+  const int m0 = (int)(mn & ((int64_t(1) << tm_log2) - 1)) * BM, n0 = (int)(mn >> tm_log2) * BN;
+  const int64_t kc = (part << nkp_log2) + (q & ((1 << nkp_log2) - 1));
+  const int64_t M = int64_t(1) << d.m_log2, N = int64_t(1) << d.n_log2, K = int64_t(1) << d.k_log2;
+  const T* Ab = arena + d.a_off + b * M * K + 2 * m0;
+  const T* Bb = arena + d.b_off + b * N * K + 2 * n0;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  T* As = reinterpret_cast<T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES) + slot * SM::A_STAGE;
+  T* Bs = reinterpret_cast<T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES) + S * SM::A_STAGE + slot * SM::B_STAGE;
+  mbar_expect_tx(&full[slot], (uint32_t)((SM::A_STAGE + SM::B_STAGE) * sizeof(T)));
+  for (int kp = 0; kp < KP; kp++) {
+    const int64_t row = kc * KP + kp;
+    bulk_g2s(As + kp * BM * 2, Ab + row * 2 * M, BM * 2 * sizeof(T), &full[slot]);
+    bulk_g2s(Bs + kp * BN * 2, Bb + row * 2 * N, BN * 2 * sizeof(T), &full[slot]);
+  }
+}
+
+// Work units [u0, u1) of one GEMM descriptor on this CTA: unit u is output
+// tile mn = u mod tiles_mn of batch point b and K part p (u / tiles_mn =
+// p 2^bt + b).  The copies of every (unit, K chunk) of the run go through one
+// ring of S stages, so the next unit's operands load while this unit's last
+// chunks are reduced and its tile is stored.  Returns false after a timed-out
 // wait (err is set; copies in flight are drained with a bounded wait).
 template <typename T, int BM, int BN, int S = kGemmStages, int BK = kGemmBK>
-__device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena, int* __restrict__ smem,
-                          int* err) {
+__device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restrict__ arena, int* __restrict__ smem,
+                           int* err) {
   using SM = GemmSmem<BM, BN, S, BK>;
   constexpr int KP = SM::KP;
   constexpr int TM = BM / 16, TN = BN / 16;
+  constexpr int BK_LOG2 = BK == 32 ? 5 : 4;
+  static_assert(BK == 32 || BK == 16, "BK");
   const int t = threadIdx.x;
-  const int M = 1 << d.m_log2, N = 1 << d.n_log2;
-  const int64_t K = int64_t(1) << d.k_log2;
-  const int64_t tiles_m = M / BM, tiles_mn = tiles_m * (N / BN);
-  const int64_t b = tile / tiles_mn, mn = tile % tiles_mn;
-  const int m0 = (int)(mn % tiles_m) * BM, n0 = (int)(mn / tiles_m) * BN;
-  const T* Ab = arena + d.a_off + b * (int64_t)M * K;
-  const T* Bb = arena + d.b_off + b * (int64_t)N * K;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + S;
-  T* As = reinterpret_cast<T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES);
-  T* Bs = As + S * SM::A_STAGE;
-  const int nk = (int)(K / BK);
-  const int warp = t >> 5, lane = t & 31;
+  const T* As = reinterpret_cast<const T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES);
+  const T* Bs = As + S * SM::A_STAGE;
+  int* scM = reinterpret_cast<int*>(reinterpret_cast<char*>(smem) + SM::SCAT_OFF);
+  int* scN = scM + BM;
+  const int nkp_log2 = d.k_log2 - BK_LOG2 - d.ks_log2;  // chunks of one unit
+  const int n_units = (int)(u1 - u0);
+  const int total_q = n_units << nkp_log2;
 
   __syncthreads();  // the previous user of this shared memory is done
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -862,55 +901,106 @@ __device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], kThreads / 32);
     }
+  // C offsets of the tile's rows / columns from their low bits: the scatter
+  // is linear over disjoint bits, so a unit adds only its (m0, n0, b) base
+  for (int i = t; i < BM; i += kThreads) {
+    int o = 0;
+    for (int x = 0; x < d.bm_log2; x++)
+      if ((i >> x) & 1) o += 1 << d.m_pc[x];
+    scM[i] = o;
+  }
+  for (int j = t; j < BN; j += kThreads) {
+    int o = 0;
+    for (int x = 0; x < d.bn_log2; x++)
+      if ((j >> x) & 1) o += 1 << d.n_pc[x];
+    scN[j] = o;
+  }
   __syncthreads();
-
-  auto issue = [&](int kc, int slot) {
-    mbar_expect_tx(&full[slot], (uint32_t)((SM::A_STAGE + SM::B_STAGE) * sizeof(T)));
-    for (int kp = 0; kp < KP; kp++) {
-      const int64_t row = (int64_t)kc * KP + kp;
-      bulk_g2s(As + slot * SM::A_STAGE + kp * BM * 2, Ab + row * 2 * M + 2 * m0, BM * 2 * sizeof(T), &full[slot]);
-      bulk_g2s(Bs + slot * SM::B_STAGE + kp * BN * 2, Bb + row * 2 * N + 2 * n0, BN * 2 * sizeof(T), &full[slot]);
-    }
-  };
   int issued = 0;
   if (t == 0)
-    for (; issued < S && issued < nk; issued++) issue(issued, issued);
+    for (; issued < S && issued < total_q; issued++) gemm_issue<T, BM, BN, S, BK>(d, u0, issued, issued, arena, smem);
 
-  const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
-  T acc[TM][TN];
-#pragma unroll
-  for (int i = 0; i < TM; i++)
-#pragma unroll
-    for (int j = 0; j < TN; j++) acc[i][j] = Trop<T>::neg();
-
-  // S chunks in flight.  A warp that has used a chunk arrives on its empty
-  // barrier; thread 0 refills the slot once all warps have.  No block-wide
-  // barrier in the loop.  A timed-out wait clears ok and the loop runs on
-  // (results are discarded); the failure is collected once after the loop.
+  // A warp that has used a chunk arrives on its empty barrier; thread 0
+  // refills the slot once all warps have.  A timed-out wait clears ok and the
+  // loops run on (results are discarded); the failure is collected at the end.
   bool ok = true;
-  for (int kc = 0; kc < nk; kc++) {
-    const int slot = kc % S;
-    const uint32_t par = (uint32_t)((kc / S) & 1);
-    if (ok) ok = mbar_wait(&full[slot], par);
-    const T* as = As + slot * SM::A_STAGE;
-    const T* bs = Bs + slot * SM::B_STAGE;
-#pragma unroll 2
-    for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[slot]);
-    if (t == 0 && kc + S < nk && ok) {
-      ok = mbar_wait(&empty[slot], par);
-      if (ok) {
-        issue(kc + S, slot);
-        issued = kc + S + 1;
+  int slot = 0;
+  uint32_t par = 0;
+  int q = 0;
+  for (int ui = 0; ui < n_units; ui++) {
+    const int warp = t >> 5, lane = t & 31;
+    const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+      for (int j = 0; j < TN; j++) acc[i][j] = Trop<T>::neg();
+    for (int kl = 0; kl < (1 << nkp_log2); kl++, q++) {
+      if (ok) ok = mbar_wait(&full[slot], par);
+      const T* as = As + slot * SM::A_STAGE;
+      const T* bs = Bs + slot * SM::B_STAGE;
+#pragma unroll 1
+      for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[slot]);
+      if (t == 0 && q + S < total_q && ok) {
+        ok = mbar_wait(&empty[slot], par);
+        if (ok) {
+          gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
+          issued = q + S + 1;
+        }
+      }
+      if (++slot == S) {
+        slot = 0;
+        par ^= 1u;
+      }
+    }
+    // epilogue: scatter the tile into C's layout (part p of a split K at
+    // c_off + p 2^(m+n+bt))
+    {
+      const int tm_log2 = d.m_log2 - d.bm_log2, tmn_log2 = tm_log2 + d.n_log2 - d.bn_log2;
+      const int64_t u = u0 + ui;
+      const int64_t mn = u & ((int64_t(1) << tmn_log2) - 1), rest = u >> tmn_log2;
+      const int64_t b = rest & ((int64_t(1) << d.bt_log2) - 1), part = rest >> d.bt_log2;
+      const int mt = (int)(mn & ((int64_t(1) << tm_log2) - 1)), nt = (int)(mn >> tm_log2);
+      int64_t cb = d.c_off + (part << (d.m_log2 + d.n_log2 + d.bt_log2));
+      for (int x = 0; x < d.bt_log2; x++)
+        if ((b >> x) & 1) cb += int64_t(1) << d.b_pc[x];
+      for (int x = d.bm_log2; x < d.m_log2; x++)
+        if ((mt >> (x - d.bm_log2)) & 1) cb += int64_t(1) << d.m_pc[x];
+      for (int x = d.bn_log2; x < d.n_log2; x++)
+        if ((nt >> (x - d.bn_log2)) & 1) cb += int64_t(1) << d.n_pc[x];
+      T* Cb = arena + cb;
+      // rows i, i + 1 (i even) of a thread differ in m bit 0 when BM >= 64:
+      // adjacent in C when m bit 0 sits at C position 0
+      if (TM >= 4 && d.m_pc[0] == 0) {
+#pragma unroll
+        for (int i = 0; i < TM; i += 2) {
+          T* ro = Cb + scM[gm_row<TM, BM>(wm, lm, i)];
+#pragma unroll
+          for (int j = 0; j < TN; j++) {
+            typename Vec2<T>::type v;
+            v.x = acc[i][j];
+            v.y = acc[i + 1][j];
+            *reinterpret_cast<typename Vec2<T>::type*>(ro + scN[gm_col<TN, BN>(wn, ln, j)]) = v;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < TM; i++) {
+          T* ro = Cb + scM[gm_row<TM, BM>(wm, lm, i)];
+#pragma unroll
+          for (int j = 0; j < TN; j++) ro[scN[gm_col<TN, BN>(wn, ln, j)]] = acc[i][j];
+        }
       }
     }
   }
   if (__syncthreads_or(!ok)) {
     if (t == 0) {
       atomicExch(err, 3 /* TB_ERR_TIMEOUT */);
-      // every issued chunk must land before the shared memory is reused
-      for (int kc = 0; kc < issued; kc++) mbar_wait(&full[kc % S], (uint32_t)((kc / S) & 1));
+      // a chunk before issued - S had its slot refilled only after thread 0
+      // saw it land; the last S may still be in flight
+      for (int j = issued > S ? issued - S : 0; j < issued; j++) mbar_wait(&full[j % S], (uint32_t)((j / S) & 1));
     }
     __syncthreads();
     return false;
@@ -920,46 +1010,39 @@ __device__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* __restrict__ arena
       mbar_inval(&full[i]);
       mbar_inval(&empty[i]);
     }
-  // epilogue: scatter the tile into C's layout
-  int* scM = reinterpret_cast<int*>(As);
-  int* scN = scM + BM;
-  for (int i = t; i < BM; i += kThreads) {
-    int m = m0 + i, o = 0;
-    for (int q = 0; q < d.m_log2; q++)
-      if ((m >> q) & 1) o += 1 << d.m_pc[q];
-    scM[i] = o;
-  }
-  for (int j = t; j < BN; j += kThreads) {
-    int n = n0 + j, o = 0;
-    for (int q = 0; q < d.n_log2; q++)
-      if ((n >> q) & 1) o += 1 << d.n_pc[q];
-    scN[j] = o;
-  }
-  int64_t cb = d.c_off;
-  for (int q = 0; q < d.bt_log2; q++)
-    if ((b >> q) & 1) cb += int64_t(1) << d.b_pc[q];
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < TM; i++) {
-    const int64_t ro = cb + scM[gm_row<TM, BM>(wm, lm, i)];
-#pragma unroll
-    for (int j = 0; j < TN; j++) arena[ro + scN[gm_col<TN, BN>(wn, ln, j)]] = acc[i][j];
-  }
   return true;
+}
+
+template <typename T, int BM, int BN>
+__device__ __forceinline__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* arena, int* smem, int* err) {
+  return gemm_tiles<T, BM, BN>(d, tile, tile + 1, arena, smem, err);
 }
 
 // Dispatch on the CTA tile shape chosen by the plan compiler.
 template <typename T>
-__device__ __forceinline__ bool gemm_tile_any(const GemmDesc& d, int64_t tile, T* arena, int* smem, int* err) {
+__device__ __forceinline__ bool gemm_tiles_any(const GemmDesc& d, int64_t u0, int64_t u1, T* arena, int* smem,
+                                               int* err) {
+  // copy stages: as many as fit the shared memory of the 128 x 128 form
   const int bm = d.bm_log2, bn = d.bn_log2;
-  if (bm == 7 && bn == 7) return gemm_tile<T, 128, 128>(d, tile, arena, smem, err);
-  if (bm == 7 && bn == 6) return gemm_tile<T, 128, 64>(d, tile, arena, smem, err);
-  if (bm == 6 && bn == 7) return gemm_tile<T, 64, 128>(d, tile, arena, smem, err);
-  if (bm == 6 && bn == 6) return gemm_tile<T, 64, 64>(d, tile, arena, smem, err);
-  if (bm >= 5 && bn >= 5) return gemm_tile<T, 32, 32>(d, tile, arena, smem, err);
-  return gemm_tile<T, 16, 16>(d, tile, arena, smem, err);
+  if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 3>(d, u0, u1, arena, smem, err);
+  if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 4>(d, u0, u1, arena, smem, err);
+  if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 4>(d, u0, u1, arena, smem, err);
+  if (bm == 6 && bn == 6) return gemm_tiles<T, 64, 64, 6>(d, u0, u1, arena, smem, err);
+  if (bm >= 5 && bn >= 5) return gemm_tiles<T, 32, 32, 8>(d, u0, u1, arena, smem, err);
+  return gemm_tiles<T, 16, 16, 8>(d, u0, u1, arena, smem, err);
+}
+template <typename T>
+__device__ __forceinline__ bool gemm_tile_any(const GemmDesc& d, int64_t tile, T* arena, int* smem, int* err) {
+  return gemm_tiles_any<T>(d, tile, tile + 1, arena, smem, err);
 }
 
-__host__ __device__ constexpr int gemm_smem_bytes_max() { return GemmSmem<128, 128>::BYTES; }
+__host__ __device__ constexpr int gemm_smem_bytes_max() { return GemmSmem<128, 128, 3>::BYTES; }
+static_assert(GemmSmem<128, 64, 4>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<64, 128, 4>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<64, 64, 6>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<32, 32, 8>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<16, 16, 8>::BYTES <= gemm_smem_bytes_max(),
+              "GEMM stages exceed the shared memory of the 128 x 128 form");
+static_assert(2 * 8 * 8 <= 128, "mbarriers of 8 stages");
 
 }  // namespace tb

@@ -198,7 +198,7 @@ bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
                (int64_t(1) << g.bt_log2);
   if (nt > 0x7fffffffLL) return false;
   g.n_tiles = (int32_t)nt;
-  g.pad_ = 0;
+  g.ks_log2 = 0;
   for (size_t q = 0; q < M.size(); q++) g.m_pc[q] = (int8_t)index_of(C, M[q]);
   for (size_t q = 0; q < N.size(); q++) g.n_pc[q] = (int8_t)index_of(C, N[q]);
   for (size_t q = 0; q < Bt.size(); q++) g.b_pc[q] = (int8_t)index_of(C, Bt[q]);
@@ -513,21 +513,76 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       }
     }
   }
-  // fused steps: 0 = leaves, 1..n = nodes, last = final
+  // fused steps: 0 = leaves, then one step per node (two for a GEMM node
+  // with a split K: the parts, then their max), last = final
   p.steps.clear();
   p.tiles.clear();
   p.gemms.clear();
+  p.step_node.clear();
+  p.split_off.assign(in.n_nodes, -1);
   std::vector<int> step_of(total, 0);  // leaves -> step 0
   Step s0{STEP_LEAVES, 0, -1, -1, (T + kThreads - 1) / kThreads, 0};
   p.steps.push_back(s0);
+  p.step_node.push_back(-1);
   p.total_tiles = s0.n_tiles;
   std::string e;
+  int64_t extra = fused_end;  // K-part partials go after the tensors
   for (int j = 0; j < in.n_nodes; j++) {
     int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
     Step st{};
     GemmDesc g;
     if (gemm_node[j] &&
         plan_gemm(p.flabels[a], p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], g)) {
+      // split K when the output tiles alone leave the last wave of CTAs
+      // mostly idle: the fewest parts that keep >= 90% of the CTA slots busy
+      // (else the best), each unit keeping >= 2 K chunks of 32, <= 16 parts
+      int ks = 0;
+      {
+        const int64_t ctas = std::max(1, p.gemm_ctas);
+        double best_u = 0;
+        for (int k2 = 0; k2 <= 4 && g.k_log2 - k2 >= 6 - (k2 == 0); k2++) {
+          const int64_t units = (int64_t)g.n_tiles << k2;
+          const double util = (double)units / (double)(((units + ctas - 1) / ctas) * ctas);
+          if (util > best_u + 1e-9) {
+            best_u = util;
+            ks = k2;
+          }
+          if (util >= 0.9) break;
+        }
+      }
+      if (ks > 0 && ((int64_t)g.n_tiles << ks) <= 0x7fffffffLL) {
+        const int64_t csize = int64_t(1) << (g.m_log2 + g.n_log2 + g.bt_log2);
+        const int64_t part_off = extra;
+        extra = align_up(extra + (csize << ks), 32);
+        g.c_off = part_off;
+        g.ks_log2 = ks;
+        g.n_tiles <<= ks;
+        Step gs{STEP_GEMM, (int32_t)p.gemms.size(), step_of[a], step_of[b], g.n_tiles, 0};
+        gs.level = 1 + std::max(p.steps[gs.dep0].level, p.steps[gs.dep1].level);
+        p.gemms.push_back(g);
+        p.steps.push_back(gs);
+        p.step_node.push_back(j);
+        p.total_tiles += gs.n_tiles;
+        p.split_off[j] = part_off;
+        // the max over the parts: a unary stream tile over [C..., part bits]
+        std::vector<int32_t> pl = p.flabels[me];
+        for (int q = 0; q < ks; q++) pl.push_back(kSplitLabel + q);
+        TileDesc d;
+        if (!(e = plan_tile(pl, nullptr, p.flabels[me], part_off, -1, p.off[me], d, p.tile_bits)).empty())
+          return "node " + std::to_string(j) + " (K parts): " + e;
+        st.kind = STEP_TILE;
+        st.desc = (int32_t)p.tiles.size();
+        st.n_tiles = d.n_tiles;
+        p.tiles.push_back(d);
+        st.dep0 = (int32_t)p.steps.size() - 1;
+        st.dep1 = -1;
+        st.level = gs.level + 1;
+        step_of[me] = (int)p.steps.size();
+        p.steps.push_back(st);
+        p.step_node.push_back(-2 - j);
+        p.total_tiles += st.n_tiles;
+        continue;
+      }
       st.kind = STEP_GEMM;
       st.desc = (int32_t)p.gemms.size();
       st.n_tiles = g.n_tiles;
@@ -548,6 +603,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
     st.level = 1 + std::max(p.steps[st.dep0].level, p.steps[st.dep1].level);
     step_of[me] = (int)p.steps.size();
     p.steps.push_back(st);
+    p.step_node.push_back(j);
     p.total_tiles += st.n_tiles;
   }
   int64_t root_off = p.off[p.root];
@@ -561,12 +617,14 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
     p.tiles.push_back(d);
     step_of[0] = (int)p.steps.size();
     p.steps.push_back(st);
+    p.step_node.push_back(-1);
     p.total_tiles += st.n_tiles;
     root_off = single_out;
     root_rank = (int)single_labels.size();
   }
   Step fin{STEP_FINAL, 0, (int32_t)p.steps.size() - 1, -1, 1, p.steps.back().level + 1};
   p.steps.push_back(fin);
+  p.step_node.push_back(-1);
   p.levels.assign(fin.level + 1, {});
   for (size_t si = 0; si < p.steps.size(); si++) p.levels[p.steps[si].level].push_back((int32_t)si);
   p.total_tiles += 1;
@@ -584,6 +642,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       return "plain lowering of node " + std::to_string(j) + ": " + e;
   }
   p.plain_elems = fused_end + scratch;
+  p.arena_elems = extra;  // the plain path never touches the K-part partials
   return "";
 }
 
@@ -599,12 +658,21 @@ std::string retile_plan(PlanHost& p, int bits) {
   int64_t total = 0;
   for (size_t si = 0; si < steps.size(); si++) {
     Step& st = steps[si];
-    if (st.kind == STEP_TILE) {
-      const int j = (int)si - 1;  // step 1 + j runs node j
-      const int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+    const int sn = p.step_node[si];
+    if (st.kind == STEP_TILE && sn != -1) {
       TileDesc d;
-      std::string e = plan_tile(p.flabels[a], &p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], d, bits);
-      if (!e.empty()) return "node " + std::to_string(j) + ": " + e;
+      std::string e;
+      if (sn >= 0) {
+        const int j = sn, me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+        e = plan_tile(p.flabels[a], &p.flabels[b], p.flabels[me], p.off[a], p.off[b], p.off[me], d, bits);
+      } else {
+        const int j = -2 - sn, me = T + j;
+        const GemmDesc& g = p.gemms[steps[st.dep0].desc];
+        std::vector<int32_t> pl = p.flabels[me];
+        for (int q = 0; q < g.ks_log2; q++) pl.push_back(kSplitLabel + q);
+        e = plan_tile(pl, nullptr, p.flabels[me], p.split_off[j], -1, p.off[me], d, bits);
+      }
+      if (!e.empty()) return "step " + std::to_string(si) + ": " + e;
       tiles[st.desc] = d;
       st.n_tiles = d.n_tiles;
     }

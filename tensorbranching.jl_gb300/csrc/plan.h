@@ -10,6 +10,10 @@
 
 namespace tb {
 
+// label ids of the K-part index of a split-K GEMM node's partials (above
+// every real label)
+constexpr int32_t kSplitLabel = 1 << 28;
+
 enum PlainKind : int32_t { PLAIN_TILE = 1, PLAIN_GEMM = 2 };
 
 // One launch of the plain (OMEinsum-style) lowering.
@@ -61,6 +65,10 @@ struct PlanHost {
   double tc = 0, sc = 0, rwc = 0, ops = 0, bytes = 0;
   int64_t total_tiles = 0;
   int32_t tile_bits = 9;                       // stream tiles grow to 2^tile_bits outputs
+  int32_t gemm_ctas = 304;                     // resident GEMM CTAs the K split balances for
+  std::vector<int32_t> step_node;              // node a step contracts (-1: leaves, final); a split-K
+                                               // reduce step holds -2 - node
+  std::vector<int64_t> split_off;              // per node: arena offset of its K-part partials (-1)
 };
 
 // Compile; returns "" on success or an error message.

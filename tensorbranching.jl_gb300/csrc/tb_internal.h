@@ -59,8 +59,10 @@ struct GemmDesc {
   int64_t a_off, b_off, c_off;
   int32_t m_log2, n_log2, k_log2, bt_log2;
   int32_t bm_log2, bn_log2;  // CTA tile BM x BN
-  int32_t n_tiles;           // (M / BM) (N / BN) 2^bt
-  int32_t pad_;
+  int32_t n_tiles;           // (M / BM) (N / BN) 2^bt 2^ks work units
+  int32_t ks_log2;           // K split: unit part p covers K / 2^ks and writes
+                             // its partial C at c_off + p 2^(m+n+bt); a
+                             // reduce step takes the max over the parts
   int8_t m_pc[32], n_pc[32], b_pc[32];  // C position of m / n / batch bit i
 };
 

@@ -206,6 +206,68 @@ def load_raw(name: str):
 
 
 # -- loaders -------------------------------------------------------------------
+def gemm_node_network(m: int, n: int, k: int, bt: int, seed: int = 0):
+    """An MIS network whose middle contraction is a GEMM node with m, n, k
+    and bt labels in its M, N, K and batch groups: vertex groups M, N, K, Bt
+    with complete M-K and N-K bipartite edges, batch vertices joined to one M
+    and one N vertex, and pendant vertices keeping M, N and Bt open above the
+    node.  Returns (graph, weights U{1..9}, contraction plan)."""
+    rng = np.random.default_rng(seed)
+    M = list(range(0, m))
+    N = list(range(m, m + n))
+    K = list(range(m + n, m + n + k))
+    B = list(range(m + n + k, m + n + k + bt))
+    base = m + n + k + bt
+    OM = list(range(base, base + m))
+    ON = list(range(base + m, base + m + n))
+    OB = list(range(base + m + n, base + m + n + bt))
+    nv = base + m + n + bt
+    left_edges = [(x, y) for x in M for y in K] + [(x, y) for x in B for y in M[:1]]
+    right_edges = [(x, y) for x in N for y in K] + [(x, y) for x in B for y in N[:1]]
+    up_edges = list(zip(M, OM)) + list(zip(N, ON)) + list(zip(B, OB))
+    g = Graph(nv, left_edges + right_edges + up_edges)
+    ixs, iy = rawcode(g)
+    eid = {e: nv + i for i, e in enumerate(g.edges)}
+    key = lambda e: (min(e), max(e))  # noqa: E731
+    ch = []
+    nxt = [len(ixs)]
+
+    def chain(ids):
+        cur = ids[0]
+        for x in ids[1:]:
+            ch.append((cur, x))
+            cur = nxt[0]
+            nxt[0] += 1
+        return cur
+
+    a = chain(M + K + B + [eid[key(e)] for e in left_edges])
+    b = chain(N + [eid[key(e)] for e in right_edges])
+    ch.append((a, b))
+    cur = nxt[0]
+    nxt[0] += 1
+    for (x, o) in up_edges:
+        for y in (eid[key((x, o))], o):
+            ch.append((cur, y))
+            cur = nxt[0]
+            nxt[0] += 1
+    code = CompressedEinsum(ixs, iy, np.array(ch, np.int32), n_labels=nv)
+    w = rng.integers(1, 10, nv).astype(np.float32)
+    return g, w, code
+
+
+def _gemm_workload(name: str) -> dict:
+    # gemm_m<M>n<N>k<K>b<B>: one network around a GEMM node of that shape
+    import re
+
+    mt = re.fullmatch(r"gemm_m(\d+)n(\d+)k(\d+)b(\d+)", name)
+    if not mt:
+        raise KeyError(name)
+    m, n, k, bt = (int(x) for x in mt.groups())
+    g, w, code = gemm_node_network(m, n, k, bt)
+    b = SlicedBranch(MISProblem(g, w), code, 0.0)
+    return {"name": name, "graph": g, "branches": [b], "sliced": [], "slice_values": None}
+
+
 def load(name: str) -> dict:
     """Workload as host objects:
       branches     list of SlicedBranch (one per network to contract)
@@ -213,6 +275,8 @@ def load(name: str) -> dict:
       slice_values item rows for the sliced labels, or None
       mis          the known answer when the builder stored one
     """
+    if name.startswith("gemm_"):
+        return _gemm_workload(name)
     d = load_raw(name)
     if name == "rr220":
         g = random_regular_graph(220, 3, d["seed"])

@@ -68,43 +68,7 @@ def _merge_seq(ids, ch, nxt):
 
 
 def gemm_case(tb, m=4, n=4, k=4, bt=1, seed=0):
-    """An MIS network whose middle node is a GEMM: vertex groups M, N, K, Bt
-    with M-K and N-K complete bipartite edges, batch vertices adjacent to
-    both sides, and pendant vertices keeping M, N and Bt alive above it."""
-    rng = np.random.default_rng(seed)
-    M = list(range(0, m))
-    N = list(range(m, m + n))
-    K = list(range(m + n, m + n + k))
-    B = list(range(m + n + k, m + n + k + bt))
-    base = m + n + k + bt
-    OM = list(range(base, base + m))
-    ON = list(range(base + m, base + m + n))
-    OB = list(range(base + m + n, base + m + n + bt))
-    nv = base + m + n + bt
-    left_edges = [(x, y) for x in M for y in K] + [(x, y) for x in B for y in M[:1]]
-    right_edges = [(x, y) for x in N for y in K] + [(x, y) for x in B for y in N[:1]]
-    up_edges = list(zip(M, OM)) + list(zip(N, ON)) + list(zip(B, OB))
-    edges = left_edges + right_edges + up_edges
-    g = tb.Graph(nv, edges)
-    ixs, iy = tb.rawcode(g)
-    eid = {e: nv + i for i, e in enumerate(g.edges)}
-    key = lambda e: (min(e), max(e))
-    left = M + K + B + [eid[key(e)] for e in left_edges]
-    right = N + [eid[key(e)] for e in right_edges]
-    rest = []
-    for (x, o) in up_edges:
-        rest += [eid[key((x, o))], o]
-    ch = []
-    nxt = [len(ixs)]
-    a = _merge_seq(left, ch, nxt)
-    b = _merge_seq(right, ch, nxt)
-    ch.append((a, b))
-    cur = nxt[0]
-    nxt[0] += 1
-    for x in rest:
-        ch.append((cur, x))
-        cur = nxt[0]
-        nxt[0] += 1
-    code = tb.CompressedEinsum(ixs, iy, np.array(ch, np.int32), n_labels=nv)
-    w = rng.integers(1, 10, nv).astype(np.float32)
-    return g, w, code
+    """An MIS network whose middle node is a GEMM (workloads.gemm_node_network)."""
+    from tensorbranching_gb300 import workloads
+
+    return workloads.gemm_node_network(m, n, k, bt, seed)

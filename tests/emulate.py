@@ -53,7 +53,7 @@ class FinalDesc(ctypes.Structure):
 class GemmDesc(ctypes.Structure):
     _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64),
                 ("m_log2", c_int32), ("n_log2", c_int32), ("k_log2", c_int32), ("bt_log2", c_int32),
-                ("bm_log2", c_int32), ("bn_log2", c_int32), ("n_tiles", c_int32), ("pad_", c_int32),
+                ("bm_log2", c_int32), ("bn_log2", c_int32), ("n_tiles", c_int32), ("ks_log2", c_int32),
                 ("m_pc", c_int8 * 32), ("n_pc", c_int8 * 32), ("b_pc", c_int8 * 32)]
 
 
@@ -351,23 +351,27 @@ GEMM_TILES = {(7, 7), (7, 6), (6, 7), (6, 6), (5, 5), (4, 4)}
 
 
 def emu_gemm_step(g, arena, written):
-    """Fused GEMM tile: k-pair interleaved operands, scatter store to C."""
+    """Fused GEMM tile: k-pair interleaved operands, scatter store to C (or,
+    with a split K, part p of the partials at c_off + p |C|)."""
     assert (g.bm_log2, g.bn_log2) in GEMM_TILES
     assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 5
+    ks = g.ks_log2
+    assert 0 <= ks <= 4 and (ks == 0 or g.k_log2 - ks >= 6)
     M, N, K, Bt = 1 << g.m_log2, 1 << g.n_log2, 1 << g.k_log2, 1 << g.bt_log2
-    assert g.n_tiles == (M >> g.bm_log2) * (N >> g.bn_log2) * Bt
+    assert g.n_tiles == (M >> g.bm_log2) * (N >> g.bn_log2) * Bt << ks
     rc = tensor_rank([g.m_pc[i] for i in range(g.m_log2)] + [g.n_pc[i] for i in range(g.n_log2)] +
                      [g.b_pc[i] for i in range(g.bt_log2)], [], [])
-    for x, n in ((g.a_off, M * K * Bt), (g.b_off, N * K * Bt), (g.c_off, 1 << rc)):
+    for x, n in ((g.a_off, M * K * Bt), (g.b_off, N * K * Bt), (g.c_off, (1 << rc) << ks)):
         assert 0 <= x and x + n <= arena.size and x % 32 == 0
     # bulk copies: rows of 2*BM (2*BN) elements at 2*m0 within a k-pair row
     BM, BN = 1 << g.bm_log2, 1 << g.bn_log2
     assert (2 * BM * 4) % 16 == 0 and (2 * BN * 4) % 16 == 0
     A = arena[g.a_off:g.a_off + M * K * Bt].reshape(Bt, K // 2, M, 2)   # [b][kp][m][k&1]
     B = arena[g.b_off:g.b_off + N * K * Bt].reshape(Bt, K // 2, N, 2)
-    A = A.transpose(0, 1, 3, 2).reshape(Bt, K, M)
-    B = B.transpose(0, 1, 3, 2).reshape(Bt, K, N)
-    C = (A[:, :, None, :] + B[:, :, :, None]).max(axis=1)  # (Bt, N, M)
+    A = A.transpose(0, 1, 3, 2).reshape(Bt, 1 << ks, K >> ks, M)
+    B = B.transpose(0, 1, 3, 2).reshape(Bt, 1 << ks, K >> ks, N)
+    C = (A[:, :, :, None, :] + B[:, :, :, :, None]).max(axis=2)  # (Bt, P, N, M)
+    C = C.transpose(1, 0, 2, 3)  # (P, Bt, N, M)
     def scat(nbits, pos):
         idx = np.arange(1 << nbits)
         out = np.zeros(1 << nbits, np.int64)
@@ -377,7 +381,9 @@ def emu_gemm_step(g, arena, written):
     sm = scat(g.m_log2, g.m_pc)
     sn = scat(g.n_log2, g.n_pc)
     sb = scat(g.bt_log2, g.b_pc)
-    addr = g.c_off + sb[:, None, None] + sn[None, :, None] + sm[None, None, :]
+    part = (np.arange(1 << ks, dtype=np.int64) << rc)
+    addr = g.c_off + part[:, None, None, None] + sb[None, :, None, None] + sn[None, None, :, None] + \
+        sm[None, None, None, :]
     arena[addr.ravel()] = C.ravel()
     np.add.at(written, addr.ravel(), 1)
 

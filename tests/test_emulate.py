@@ -89,13 +89,19 @@ def test_invalid_plans_rejected(tb, lib):
                                                   n_labels=code.n_labels), use_node_iy=True)
 
 
-@pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1)])
+@pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (4, 4, 8, 0),
+                                   (6, 6, 9, 1), (5, 5, 7, 2)])
 def test_gemm_steps(tb, orc, lib, shape):
+    """GEMM steps, including K split into parts plus a max over the parts
+    when the output tiles are too few for the GPU."""
     from cases import gemm_case
 
     g, w, code = gemm_case(tb, *shape)
     d = emulate.describe(lib, code)
-    assert [s.kind for s in d["steps"]].count(emulate.STEP_GEMM) == 1
+    gem = [s for s in d["steps"] if s.kind == emulate.STEP_GEMM]
+    assert len(gem) == 1
+    ks = d["gemms"][gem[0].desc].ks_log2
+    assert (ks > 0) == (shape[2] >= 7)
     root, nodes = emulate.run_fused(d, w)
     ref, dumps = orc.execute(code, w, dump=True)
     assert np.array_equal(root, ref)

@@ -112,7 +112,7 @@ def test_contract_generic_tensors(tb, orc, engine):
 
 
 @pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (7, 7, 6, 2),
-                                   (8, 7, 5, 1)])
+                                   (8, 7, 5, 1), (4, 4, 8, 0), (6, 6, 9, 1), (5, 5, 7, 2), (7, 7, 8, 1)])
 def test_fused_gemm_nodes(tb, orc, engine, shape):
     from cases import gemm_case
 
