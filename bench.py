@@ -454,7 +454,8 @@ def main():
         "config": {"workload": args.config, "detail": _desc(args.config), "mode": args.mode,
                    "items_per_step": len(plans), "graphs_per_step": units, "tc": st["tc"], "sc": st["sc"],
                    "rwc": st["rwc"], "l2": "flushed between steps (256 MiB write)",
-                   "answer": mx0, "parallelism": f"replicas x{ws}", "autotune": tuned},
+                   "answer": mx0, "parallelism": f"replicas x{ws}", "autotune": tuned,
+                   "resident_ctas": eng.info()},
         "tropical_gops": ops / (ms_per_step / 1000.0) / 1e9,
         "roofline": roof,
         "e2e": {"value": ws * args.steps * units / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,

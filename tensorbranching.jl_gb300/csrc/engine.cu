@@ -103,7 +103,7 @@ __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int
 // One launch per tree level: block b runs ticket first_ticket + b.  No
 // waiting: the previous launch on the stream finished every dependency.
 template <typename T, int KINDS>
-__global__ void __launch_bounds__(kThreads, 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
+__global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
                                                    int64_t first_ticket, int64_t last_ticket, int64_t chunk,
                                                    float* out_item, const float* r, int* err) {
   extern __shared__ int tb_smem[];
@@ -1380,6 +1380,17 @@ __global__ void __launch_bounds__(256) k_peak_f32(float* out, int iters, float s
 #pragma unroll
   for (int j = 0; j < NC; j++) s += f[j] + lo32(x[j]);
   if (s == 1.2345f) out[0] = s;
+}
+
+// Resident CTAs of the context's kernels (stream tiles, GEMM tiles,
+// persistent executor) and its SM count, for reports.
+extern "C" int32_t tbi_ctx_info(const tb_ctx* c, int32_t* out4) {
+  if (!c || !out4) return TB_ERR_INVALID;
+  out4[0] = c->stream_ctas;
+  out4[1] = c->gemm_ctas;
+  out4[2] = c->persistent_ctas;
+  out4[3] = c->sms;
+  return TB_OK;
 }
 
 // Test hook for the bounded waits of the persistent executor: one item whose

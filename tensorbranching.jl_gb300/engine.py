@@ -110,6 +110,17 @@ class Engine:
         rr = None if r is None else np.ascontiguousarray(r, dtype=np.float32)
         return n, arr, sv, rr
 
+    def info(self) -> dict:
+        """Resident CTAs of the stream-tile, GEMM-tile and persistent kernels
+        on this device, and its SM count."""
+        f = self.lib.tbi_ctx_info
+        f.restype = c_int32
+        f.argtypes = [c_void_p, c_void_p]
+        out = np.zeros(4, np.int32)
+        _native.check(f(self.ctx, out.ctypes.data), self.ctx)
+        return {"stream_ctas": int(out[0]), "gemm_ctas": int(out[1]), "persistent_ctas": int(out[2]),
+                "sms": int(out[3])}
+
     def autotune(self, plans, slice_vals=None, r=None) -> dict:
         """tb_autotune on this batch: tile size and schedule by timing; the
         choice serves later mode="auto" solves."""
