@@ -408,15 +408,15 @@ def main():
     t_dev = sum(dev_ms) / 1000.0
     # e2e: bind weights from host (H2D) + solve + result read-back (D2H), wall clock
     uplans = list(uniq.values())
-    h2d = sum(int(p.stats()["n_tensors"]) * 32 for p in uplans) + 4 * len(plans) + sum(len(x) for x in svs)
+    # per step: the bound weights of every distinct plan, r and slice values
+    h2d = sum(4 * p.code.n_labels for p in uplans) + 4 * len(plans) + sum(len(x) for x in svs)
     d2h = 4 * (len(plans) + 1)
     host_w = [np.ascontiguousarray(_weights_of(wl, p), np.float32) for p in uplans]
     if ws > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for p, w in zip(uplans, host_w):
-            p.bind_mis(w)
+        eng.bind_batch(uplans, host_w)
         o, m = step()
         assert m == mx0
     t_e2e = time.perf_counter() - t0

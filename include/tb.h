@@ -160,6 +160,13 @@ tb_status tb_plan_node_labels(const tb_plan* plan, int32_t node, int32_t cap, in
 tb_status tb_plan_bind_mis(tb_plan* plan, const float* weights);
 
 /*
+ * tb_plan_bind_mis for n plans in one call: plan i takes the n_labels
+ * weights at weights + offsets[i].  The weights only reach the device with
+ * the next solve (one staged copy for the whole batch).
+ */
+tb_status tb_plan_bind_mis_batch(int32_t n, tb_plan* const* plans, const float* weights, const int64_t* offsets);
+
+/*
  * Solve a batch of n items.  Item i contracts plans[i] with its sliced labels
  * fixed to slice_vals[sv_off_i .. sv_off_i + n_sliced_i) (items concatenated
  * in order; NULL when no plan slices), and returns

@@ -89,6 +89,7 @@ ENGINE_SIGNATURES = {
     "tb_plan_stats_get": (c_int32, [c_void_p, POINTER(TbPlanStats)]),
     "tb_plan_node_labels": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, POINTER(c_int32)]),
     "tb_plan_bind_mis": (c_int32, [c_void_p, c_void_p]),
+    "tb_plan_bind_mis_batch": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p]),
     "tb_solve_batch": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32]),
     "tb_contract": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32]),
     "tb_dump_intermediates": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32]),

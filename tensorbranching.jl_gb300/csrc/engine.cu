@@ -20,6 +20,7 @@
 #include <mutex>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/tb.h"
@@ -32,8 +33,9 @@ using namespace tb;
 // kernels (thin __global__ wrappers over the device routines)
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_leaves(const LeafDesc* leaves, int n, const int8_t* sv, T* arena) {
-  leaves_tile<T>(leaves, n, sv, arena, blockIdx.x);
+__global__ void __launch_bounds__(kThreads) k_leaves(const LeafDesc* leaves, int n, const int8_t* sv, T* arena,
+                                                     const float* w) {
+  leaves_tile<T>(leaves, n, sv, arena, blockIdx.x, w);
 }
 
 // A stream-tile node: CTA b runs tiles [b * chunk, (b + 1) * chunk).
@@ -78,7 +80,7 @@ __device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, i
   if constexpr ((KINDS & 1) == 0) return;
   switch (st.kind) {
     case STEP_LEAVES:
-      leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile);
+      leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile, it.w);
       break;
     case STEP_TILE:
       stream_tile<T>(it.tiles[st.desc], tile, it.arena, smem);
@@ -266,10 +268,11 @@ struct HostBuf {
 struct tb_plan {
   tb_ctx* ctx = nullptr;
   PlanHost h;
+  std::vector<float> weights;  // bound vertex weights by label
   DevBuf d_steps, d_tiles, d_gemms, d_leaves;
-  bool uploaded = false;
   bool structure_uploaded = false;
-  uint64_t version = 0;  // bumps when device buffers move
+  bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
+  uint64_t version = 0;        // bumps when device buffers move
 };
 
 struct GraphKey {
@@ -292,7 +295,7 @@ struct tb_ctx {
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   size_t budget = 0;
-  DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals;
+  DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals, wvals;
   HostBuf h_items, h_groups, h_chunks, h_in, h_out;
   // batch state of the last upload (reused when the same plans come again)
   GraphKey key;
@@ -368,8 +371,11 @@ static tb_status set_kernel_attrs() {
   return TB_OK;
 }
 
-static tb_status upload_plan(tb_plan* p) {
-  if (p->uploaded) return TB_OK;
+// Descriptors to the device (once, and again after re-tiling).  Paths that
+// build leaves from LeafDesc::w (tb_contract, dumps, serving) also need the
+// leaves re-sent after a re-bind; the batched and plain solves read the
+// weights from a per-call weight array instead.
+static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
   auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
     if (bytes == 0) bytes = 16;
     cudaError_t e = b.ensure(bytes);
@@ -379,14 +385,20 @@ static tb_status upload_plan(tb_plan* p) {
   };
   const PlanHost& h = p->h;
   if (!p->structure_uploaded) {
+    void* before[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
     CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
     CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
     CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
+    CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
+    void* after[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
+    // captured graphs hold these device pointers: a move invalidates them
+    if (std::memcmp(before, after, sizeof(before)) != 0) p->version = ++p->ctx->plan_counter;
     p->structure_uploaded = true;
+    p->leaves_dirty = false;
+  } else if (leaf_weights && p->leaves_dirty) {
+    CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
+    p->leaves_dirty = false;
   }
-  // the leaves carry the weights: the only part a re-bind changes
-  CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
-  p->uploaded = true;
   return TB_OK;
 }
 
@@ -395,12 +407,12 @@ static tb_status upload_plan(tb_plan* p) {
 // ---------------------------------------------------------------------------
 template <typename T>
 static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv, bool leaves_from_mis,
-                            int64_t& launches) {
+                            const float* d_w, int64_t& launches) {
   const PlanHost& h = p->h;
   cudaStream_t s = c->stream;
   if (leaves_from_mis) {
     k_leaves<T><<<(h.n_tensors + kThreads - 1) / kThreads, kThreads, 0, s>>>(
-        reinterpret_cast<const LeafDesc*>(p->d_leaves.p), h.n_tensors, d_sv, arena);
+        reinterpret_cast<const LeafDesc*>(p->d_leaves.p), h.n_tensors, d_sv, arena, d_w);
     CU(cudaGetLastError());
     launches++;
   }
@@ -433,7 +445,8 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
 // ---------------------------------------------------------------------------
 template <typename T>
 static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std::vector<int64_t>& arena_off,
-                              const std::vector<int64_t>& sv_off, bool skip_leaves) {
+                              const std::vector<int64_t>& sv_off, bool skip_leaves,
+                              const std::vector<int64_t>* w_off) {
   // items
   CU(c->h_items.ensure(sizeof(ItemDev<T>) * n));
   ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(c->h_items.p);
@@ -447,6 +460,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
     it.slice_vals = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
+    it.w = w_off ? reinterpret_cast<const float*>(c->wvals.p) + (*w_off)[i] : nullptr;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = done_base;
@@ -605,7 +619,26 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if (!plans[i]) return fail(TB_ERR_INVALID, "null plan");
     if (plans[i]->ctx != c) return fail(TB_ERR_INVALID, "plan belongs to another context");
     if (!plans[i]->h.has_weights) return fail(TB_ERR_INVALID, "plan has no bound weights (tb_plan_bind_mis)");
-    if ((st = upload_plan(plans[i]))) return st;
+    if ((st = upload_plan(plans[i], false))) return st;
+  }
+  // weights of each distinct plan, staged once per call
+  std::vector<int64_t> w_off(n);
+  std::vector<char> w_first(n, 0);
+  int64_t w_total = 0;
+  {
+    std::unordered_map<const tb_plan*, int64_t> seen;
+    seen.reserve((size_t)n * 2);
+    for (int i = 0; i < n; i++) {
+      auto it = seen.find(plans[i]);
+      if (it != seen.end()) {
+        w_off[i] = it->second;
+      } else {
+        w_off[i] = w_total;
+        w_first[i] = 1;
+        seen.emplace(plans[i], w_total);
+        w_total += align_up(std::max<int64_t>(plans[i]->h.n_labels, 1), 4);
+      }
+    }
   }
   // slice values (concatenated)
   std::vector<int64_t> sv_off(n);
@@ -620,14 +653,21 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
   CU(c->slice_vals.ensure(std::max<size_t>(sv, 16)));
   CU(c->out_item.ensure(sizeof(float) * (n + 1)));
   CU(c->h_out.ensure(sizeof(float) * (n + 1) + 64));
-  // pinned staging of the per-call inputs: r values, then slice values
+  // pinned staging of the per-call inputs: r values, slice values, weights
   const size_t r_bytes = align_up(sizeof(float) * n, 16);
-  CU(c->h_in.ensure(r_bytes + std::max<size_t>(sv, 16)));
+  const size_t sv_bytes = align_up(std::max<size_t>(sv, 16), 16);
+  const size_t w_bytes = sizeof(float) * (size_t)std::max<int64_t>(w_total, 4);
+  CU(c->h_in.ensure(r_bytes + sv_bytes + w_bytes));
   CU(c->rvals.ensure(r_bytes));
+  CU(c->wvals.ensure(w_bytes));
   float* h_r = reinterpret_cast<float*>(c->h_in.p);
   int8_t* h_sv = reinterpret_cast<int8_t*>(c->h_in.p) + r_bytes;
+  float* h_w = reinterpret_cast<float*>(reinterpret_cast<char*>(c->h_in.p) + r_bytes + sv_bytes);
   for (int i = 0; i < n; i++) h_r[i] = r ? r[i] : 0.0f;
   if (sv) std::memcpy(h_sv, slice_vals, sv);
+  for (int i = 0; i < n; i++)
+    if (w_first[i]) std::memcpy(h_w + w_off[i], plans[i]->weights.data(), sizeof(float) * plans[i]->h.n_labels);
+  const float* d_w = reinterpret_cast<const float*>(c->wvals.p);
   float* hout = reinterpret_cast<float*>(c->h_out.p);
   int64_t launches = 0;
   CU(cudaEventRecord(c->ev0, c->stream));
@@ -639,11 +679,12 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if (bytes > c->budget) return fail(TB_ERR_OOM, "plan needs more device memory than the budget");
     CU(c->arena.ensure(bytes));
     if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, h_sv, sv, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->wvals.p, h_w, w_bytes, cudaMemcpyHostToDevice, c->stream));
     T* arena = reinterpret_cast<T*>(c->arena.p);
     for (int i = 0; i < n; i++) {
       tb_plan* p = plans[i];
       const int8_t* d_sv = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
-      if ((st = plain_item<T>(c, p, arena, d_sv, true, launches))) return st;
+      if ((st = plain_item<T>(c, p, arena, d_sv, true, d_w + w_off[i], launches))) return st;
       k_final<T><<<1, kThreads, 0, c->stream>>>(p->h.fin, arena, r ? r[i] : 0.0f,
                                                 reinterpret_cast<float*>(c->out_item.p) + i);
       CU(cudaGetLastError());
@@ -710,7 +751,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
         c->gexec = nullptr;
       }
       c->have_key = false;
-      if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, false))) return st;
+      if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, false, &w_off))) return st;
       CU(cudaStreamSynchronize(c->stream));
       c->key = key;
       c->have_key = true;
@@ -722,6 +763,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
         int64_t l2 = 0;
         cudaError_t e = cudaMemcpyAsync(c->rvals.p, h_r, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess && sv) e = cudaMemcpyAsync(c->slice_vals.p, h_sv, sv, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->wvals.p, h_w, w_bytes, cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) {
           cudaStreamEndCapture(c->stream, &g);
           return fail(TB_ERR_CUDA, cudaGetErrorString(e));
@@ -745,6 +787,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     } else {
       CU(cudaMemcpyAsync(c->rvals.p, h_r, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
       if (sv) CU(cudaMemcpyAsync(c->slice_vals.p, h_sv, sv, cudaMemcpyHostToDevice, c->stream));
+      CU(cudaMemcpyAsync(c->wvals.p, h_w, w_bytes, cudaMemcpyHostToDevice, c->stream));
       if ((st = enqueue_batched<T>(c, n, mode, done_words, launches))) return st;
       CU(cudaMemcpyAsync(hout, c->out_item.p, sizeof(float) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
     }
@@ -780,7 +823,6 @@ static void retile_all(tb_ctx* c, const std::vector<tb_plan*>& uniq, int bits, s
       return;
     }
     p->structure_uploaded = false;
-    p->uploaded = false;
     p->version = ++c->plan_counter;
   }
 }
@@ -1053,14 +1095,21 @@ tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
       ld.w = x;
     }
   }
+  // the weights travel with each solve (one staged copy for the whole
+  // batch); the device leaf descriptors are refreshed only for the paths
+  // that read LeafDesc::w
+  p->weights.assign(w, w + p->h.n_labels);
   p->h.has_weights = true;
-  p->uploaded = false;
-  void* before[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
-  tb_status st = upload_plan(p);
-  if (st) return st;
-  void* after[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
-  // captured graphs hold these device pointers: a move invalidates them
-  if (std::memcmp(before, after, sizeof(before)) != 0) p->version = ++p->ctx->plan_counter;
+  p->leaves_dirty = true;
+  return TB_OK;
+}
+
+tb_status tb_plan_bind_mis_batch(int32_t n, tb_plan* const* plans, const float* weights, const int64_t* offsets) {
+  if (n < 0 || (n > 0 && (!plans || !weights || !offsets))) return fail(TB_ERR_INVALID, "null argument");
+  for (int32_t i = 0; i < n; i++) {
+    tb_status st = tb_plan_bind_mis(plans[i], weights + offsets[i]);
+    if (st) return st;
+  }
   return TB_OK;
 }
 
@@ -1111,7 +1160,7 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
   CU(cudaSetDevice(c->device));
   tb_status st = set_kernel_attrs<T>();
   if (st) return st;
-  if ((st = upload_plan(p))) return st;
+  if ((st = upload_plan(p, true))) return st;
   const PlanHost& h = p->h;
   int64_t need = mode == TB_MODE_PLAIN ? h.plain_elems : h.arena_elems;
   size_t bytes = (size_t)need * sizeof(T) + 256;
@@ -1136,7 +1185,7 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
   int64_t launches = 0;
   const int8_t* d_sv = reinterpret_cast<const int8_t*>(c->slice_vals.p);
   if (mode == TB_MODE_PLAIN) {
-    if ((st = plain_item<T>(c, p, arena, d_sv, leaf_data == nullptr, launches))) return st;
+    if ((st = plain_item<T>(c, p, arena, d_sv, leaf_data == nullptr, nullptr, launches))) return st;
   } else {
     // fused tiles, one launch per level for this single item
     std::vector<int64_t> aoff{0}, svo{0};
@@ -1146,7 +1195,7 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
       cudaGraphExecDestroy(c->gexec);
       c->gexec = nullptr;
     }
-    if ((st = upload_batch<T>(c, 1, pl, aoff, svo, leaf_data != nullptr))) return st;
+    if ((st = upload_batch<T>(c, 1, pl, aoff, svo, leaf_data != nullptr, nullptr))) return st;
     CU(c->out_item.ensure(sizeof(float) * 2));
     CU(cudaMemsetAsync(c->misc.p, 0, 64, c->stream));
     const int smem = max_stream_smem_bytes();
@@ -1406,7 +1455,7 @@ extern "C" int32_t tbi_timeout_probe(tb_ctx* c, tb_plan* p, int32_t timeout_ms) 
   CU(cudaSetDevice(c->device));
   tb_status st = set_kernel_attrs<float>();
   if (st) return st;
-  if ((st = upload_plan(p))) return st;
+  if ((st = upload_plan(p, true))) return st;
   if (c->gexec) {
     cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
@@ -1417,7 +1466,7 @@ extern "C" int32_t tbi_timeout_probe(tb_ctx* c, tb_plan* p, int32_t timeout_ms) 
   CU(c->slice_vals.ensure(16));
   CU(c->out_item.ensure(sizeof(float) * 2));
   CU(c->rvals.ensure(16));
-  if ((st = upload_batch<float>(c, 1, &p, aoff, svoff, false))) return st;
+  if ((st = upload_batch<float>(c, 1, &p, aoff, svoff, false, nullptr))) return st;
   Chunk* ch = reinterpret_cast<Chunk*>(c->chunks.p);
   // the final step comes last (highest level): make it the only chunk
   CU(cudaMemcpyAsync(ch, ch + (c->n_chunks - 1), sizeof(Chunk), cudaMemcpyDeviceToDevice, c->stream));
@@ -1857,7 +1906,7 @@ tb_status tb_submit(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8_t* s
     std::lock_guard<std::mutex> lk(c->mu);
     tb_status st = TB_OK;
     for (auto& it : q->items)
-      if ((st = upload_plan(it.plan))) return st;
+      if ((st = upload_plan(it.plan, true))) return st;
   }
   q->items_left = n;
   q->t_submit = now_s();

@@ -80,12 +80,13 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ void leaves_tile(const LeafDesc* __restrict__ leaves, int n_leaves,
-                            const int8_t* __restrict__ slice_vals, T* __restrict__ arena, int tile) {
+                            const int8_t* __restrict__ slice_vals, T* __restrict__ arena, int tile,
+                            const float* __restrict__ weights) {
   int i = tile * kThreads + threadIdx.x;
   if (i >= n_leaves) return;
   const LeafDesc ld = leaves[i];
   const int nout = 1 << ld.n_out;
-  const T w = Trop<T>::from_w(ld.w);
+  const T w = Trop<T>::from_w(weights && ld.label >= 0 ? weights[ld.label] : ld.w);
   for (int e = 0; e < nout; e++) {
     T best = Trop<T>::neg();
     for (int raw = 0; raw < (1 << ld.nraw); raw++) {

@@ -428,6 +428,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       ld.out_bit[k] = (int8_t)index_of(p.labels[i], x);
       ld.slice_idx[k] = (int8_t)p.slice_index[x];
     }
+    ld.label = ld.nraw == 1 ? p.leaf_raw[i][0] : -1;
     ld.w = 0.0f;
     p.leaves.push_back(ld);
   }

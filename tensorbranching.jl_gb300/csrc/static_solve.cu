@@ -60,7 +60,7 @@ tb_status sfail(tb_status s, const std::string& m) {
   } while (0)
 
 __global__ void __launch_bounds__(kThreads) ks_leaves(const LeafDesc* leaves, int n, const int8_t* sv, float* arena) {
-  leaves_tile<float>(leaves, n, sv, arena, blockIdx.x);
+  leaves_tile<float>(leaves, n, sv, arena, blockIdx.x, nullptr);
 }
 
 __global__ void __launch_bounds__(kThreads) ks_tile(const TileDesc d, float* arena) {

@@ -74,8 +74,8 @@ struct LeafDesc {
   int32_t n_out;        // output rank
   int8_t out_bit[2];    // raw position -> output bit (-1: label sliced)
   int8_t slice_idx[2];  // raw position -> index into the item's slice values (-1)
-  int32_t pad_;
-  float w;              // vertex weight (vertex leaves)
+  int32_t label;        // vertex label of a vertex leaf (index into a weight array), else -1
+  float w;              // vertex weight (vertex leaves) for paths without a weight array
 };
 
 struct Step {
@@ -102,6 +102,7 @@ struct ItemDev {
   const GemmDesc* gemms;
   const LeafDesc* leaves;
   const int8_t* slice_vals;
+  const float* w;      // vertex weights by label (per call), or null: LeafDesc::w
   float r;
   int32_t n_leaves;
   int32_t done_base;   // offset of this item's step counters

@@ -96,6 +96,21 @@ class Engine:
             p.bind_mis(weights)
         return p
 
+    def bind_batch(self, plans, weights) -> None:
+        """tb_plan_bind_mis for many plans in one call (weights[i] for plans[i])."""
+        n = len(plans)
+        ws = [np.ascontiguousarray(w, dtype=np.float32) for w in weights]
+        for p, w in zip(plans, ws):
+            if w.shape[0] < p.code.n_labels:
+                raise ValueError("one weight per label is required")
+        offs = np.zeros(n, np.int64)
+        if n > 1:
+            offs[1:] = np.cumsum([w.shape[0] for w in ws[:-1]])
+        flat = np.concatenate(ws) if n else np.zeros(1, np.float32)
+        arr = (c_void_p * max(n, 1))(*[p.handle for p in plans])
+        _native.check(self.lib.tb_plan_bind_mis_batch(n, ctypes.cast(arr, c_void_p), flat.ctypes.data,
+                                                      offs.ctypes.data), self.ctx)
+
     @staticmethod
     def _batch_args(plans, slice_vals, r):
         n = len(plans)

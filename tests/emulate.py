@@ -43,7 +43,7 @@ class Step(ctypes.Structure):
 
 class LeafDesc(ctypes.Structure):
     _fields_ = [("off", c_int64), ("nraw", c_int32), ("n_out", c_int32), ("out_bit", c_int8 * 2),
-                ("slice_idx", c_int8 * 2), ("pad_", c_int32), ("w", c_float)]
+                ("slice_idx", c_int8 * 2), ("label", c_int32), ("w", c_float)]
 
 
 class FinalDesc(ctypes.Structure):

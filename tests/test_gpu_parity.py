@@ -127,3 +127,28 @@ def test_fused_gemm_nodes(tb, orc, engine, shape):
         got = engine.dump(plan, mode=mode)
         for a, b in zip(got, dumps):
             assert np.array_equal(a, b), mode
+
+
+def test_rebinding_weights_between_solves(tb, orc, engine):
+    """Weights travel with each solve: re-binding between two solves of the
+    same batch (CUDA graph replayed) gives the new weights' results in every
+    mode, and the dump path (LeafDesc weights) follows too."""
+    g, w, code = rr_case(tb, 36, 9)
+    plan = engine.plan(code, w)
+    plan2 = engine.plan(code, w)
+    rng = np.random.default_rng(3)
+    for rep in range(3):
+        w2 = rng.integers(1, 10, g.n).astype(np.float32)
+        plan.bind_mis(w2)
+        plan2.bind_mis(w2[::-1].copy())
+        ref = orc.solve(code, w2)
+        ref2 = orc.solve(code, w2[::-1].copy())
+        for mode in MODES:
+            out, mx = engine.solve_batch([plan, plan2, plan], r=[0.0, 0.0, 1.0], mode=mode)
+            assert list(out) == [np.float32(ref), np.float32(ref2), np.float32(ref + 1)], (rep, mode)
+        dumps = engine.dump(plan, mode="layered")
+        assert np.max(dumps[-1]) == np.float32(ref)
+    w3 = rng.integers(1, 10, g.n).astype(np.float32)
+    engine.bind_batch([plan, plan2], [w3, w3[::-1].copy()])
+    out, _ = engine.solve_batch([plan, plan2], mode="batched")
+    assert list(out) == [np.float32(orc.solve(code, w3)), np.float32(orc.solve(code, w3[::-1].copy()))]
