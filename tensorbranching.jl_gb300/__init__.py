@@ -12,7 +12,7 @@ from .mis import (ContractionTreeSlicer, KernelResult, contract_slices, dynamic_
 from .network import (CompressedEinsum, MISProblem, SlicedBranch, UnitWeight, add_r, derive_node_labels,
                       rawcode)
 from .order import GreedyMethod, TreeSA, complexity, greedy_slice, initialize_code, order2eincode, peak_memory
-from . import replicas, serving
+from . import replicas, serving, slice_io
 
 __all__ = [
     "Engine", "Plan", "default_engine", "Graph", "random_ksg", "random_regular_graph", "random_weights",

@@ -33,3 +33,21 @@ def test_golden_cases_in_one_batch(tb, engine):
     for mode in ("batched", "layered"):
         out, mx = engine.solve_batch(plans, mode=mode)
         assert np.array_equal(out, np.array(want, np.float32)), mode
+
+
+def test_slices_from_disk_on_the_gpu(tb, exact, engine, tmp_path):
+    """A directory in the reference's slice format (src/io.jl) contracted by
+    contract_slices on the GPU: max + r is the MIS."""
+    sio = tb.slice_io
+    g = tb.random_regular_graph(70, 3, 4)
+    w = tb.random_weights(g.n, 4)
+    kr = tb.kernelize(g, w)
+    code = tb.initialize_code(kr.g, tb.GreedyMethod(4))
+    branches = tb.slice(tb.MISProblem(kr.g, kr.weights), code, kr.r,
+                        tb.ContractionTreeSlicer(sc_target=8, refine=False))
+    for i, b in enumerate(branches):
+        sio.save_finished(str(tmp_path), b, 7 + i)
+    sio.save_slices_csv(str(tmp_path), [(7 + i, b.sc(), b.tc(), b.r) for i, b in enumerate(branches)])
+    back = sio.load_all_finished(str(tmp_path))
+    res = tb.contract_slices(back, engine=engine, mode="batched")
+    assert float(np.max(res)) == pytest.approx(exact.branch_and_bound(g.n, g.edges, w))
