@@ -483,8 +483,12 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
     if (gemm) {
       gemm_node[j] = 1;
       std::vector<int32_t> la = loose(a), lb = loose(b), none;
-      by_c(M, la);
-      by_c(N, lb);
+      // M / N order: the operand's producer prefers the labels it keeps from
+      // one side first (they sit in its CTA tile); this node's own stores
+      // prefer C's order (its tile then covers C's fastest positions).  The
+      // larger of the two tensors decides.
+      by_c(M, C.size() >= SA.size() ? none : la);
+      by_c(N, C.size() >= SB.size() ? none : lb);
       by_c(Bt, none);
       // k0 sits at position 0 of both operands: prefer a label each operand's
       // own node keeps from one side (it is then inside that node's CTA tile)
