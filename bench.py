@@ -59,13 +59,24 @@ def _node_work(plan, cache={}):
     return cache[key]
 
 
-def roofline(plans, seconds, simt_ops_s, hbm_gbs):
+def roofline(plans, seconds, simt_ops_s, hbm_gbs, i16_ops_s=None):
     """Node-weighted roofline of one step: every node is bounded by
-    max(ops / P_simt, bytes / BW_hbm); the step's bound is the sum."""
+    max(ops / P, bytes / BW_hbm), P the f32 SIMT max-plus peak, or the
+    packed-int16 one for GEMM-tile nodes running that form; the step's bound
+    is the sum."""
+    from tensorbranching_gb300.engine import plan_node_kinds
+
     ops = byts = t_simt = t_hbm = t_bound = 0.0
+    kinds_of = {}
     for p in plans:
         o, b = _node_work(p)
-        ts, th = o / simt_ops_s, b / (hbm_gbs * 1e9)
+        peak = np.full(o.shape, simt_ops_s)
+        if i16_ops_s:
+            k = kinds_of.get(id(p))
+            if k is None:
+                k = kinds_of[id(p)] = plan_node_kinds(p)
+            peak = np.where(k == 3, i16_ops_s, simt_ops_s)
+        ts, th = o / peak, b / (hbm_gbs * 1e9)
         ops += o.sum()
         byts += b.sum()
         t_simt += ts.sum()
@@ -381,6 +392,9 @@ def main():
     from tensorbranching_gb300.engine import measure_maxplus_peak
 
     simt = measure_maxplus_peak(dev)
+    from tensorbranching_gb300.engine import measure_maxplus_peak_i16
+
+    simt_i16 = measure_maxplus_peak_i16(dev)
     # L2 flush buffer (larger than the 129 MB L2)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")
 
@@ -431,7 +445,9 @@ def main():
     ms_per_step = 1000.0 * t_dev / args.steps
     hbm, peak_kind = _peaks()
     t_step = ms_per_step / 1000.0
-    r_ops, r_bytes, t_simt, t_hbm, t_bound = roofline(plans, t_step, simt, hbm)
+    gemm_arith = _gemm_arith(wl)
+    r_ops, r_bytes, t_simt, t_hbm, t_bound = roofline(plans, t_step, simt, hbm,
+                                                      simt_i16 if gemm_arith != "f32" else None)
     traffic = _profiled_traffic(args.config, args.mode)
     if t_simt >= t_hbm:
         roof = {"bound": "simt", "achieved": r_ops / t_step / 1e12, "peak": simt / 1e12, "unit": "TFLOP/s",
@@ -440,9 +456,11 @@ def main():
         roof = {"bound": "hbm", "achieved": r_bytes / t_step / 1e9, "peak": hbm, "unit": "GB/s",
                 "frac": r_bytes / t_step / (hbm * 1e9)}
     roof.update({
+        "peak_i16x2": simt_i16 / 1e12,
         "traffic": traffic, "attainable_frac": t_bound / t_step,
-        "peak_source": f"simt: measured max-plus probe on this GPU ({simt / 1e12:.2f} Tops); hbm: {peak_kind} "
-                       f"copy bandwidth ({hbm:.0f} GB/s)",
+        "peak_source": f"simt: measured f32 max-plus probe on this GPU ({simt / 1e12:.2f} Tops); packed-int16 "
+                       f"max-plus probe {simt_i16 / 1e12:.2f} Tops (the GEMM tiles' ceiling when they run that "
+                       f"form; used per node in attainable_frac); hbm: {peak_kind} copy bandwidth ({hbm:.0f} GB/s)",
         "note": "dominant kernel k_persistent (batched) / k_level (layered) runs the whole step; achieved = "
                 "algorithmic tropical ops 2*2^|L| (max and add, f32 SIMT, no tensor cores) or bytes "
                 "4(|A|+|B|+|C|) summed over nodes / device time of the step; attainable_frac = "
@@ -455,6 +473,7 @@ def main():
                    "items_per_step": len(plans), "graphs_per_step": units, "tc": st["tc"], "sc": st["sc"],
                    "rwc": st["rwc"], "l2": "flushed between steps (256 MiB write)",
                    "answer": mx0, "parallelism": f"replicas x{ws}", "autotune": tuned,
+                   "gemm_arithmetic": gemm_arith,
                    "resident_ctas": eng.info()},
         "tropical_gops": ops / (ms_per_step / 1000.0) / 1e9,
         "roofline": roof,
@@ -527,6 +546,16 @@ def run_serve(tb, args):
                           "mean": float(lat.mean()), "max": float(lat.max())},
            "server": st, "same_alone_and_in_mix": True, "clocks": clk.summary()}
     print(json.dumps(res))
+
+
+def _gemm_arith(wl):
+    """The GEMM tiles use exact packed-int16 DPX arithmetic when every bound
+    weight vector is integral, >= 0 and sums below 8192; f32 otherwise."""
+    ok = True
+    for w in wl.get("plan_weights", {}).values():
+        w = np.asarray(w, np.float64)
+        ok = ok and bool(np.all(w >= 0) and np.all(w == np.floor(w)) and w.sum() < 8192)
+    return "int16x2 DPX (exact: integer weights >= 0 summing below 8192)" if ok else "f32"
 
 
 def _weights_of(wl, plan):

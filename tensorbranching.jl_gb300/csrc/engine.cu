@@ -73,7 +73,7 @@ __device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, i
                                          float* out_item, const float* r, int item, int* err) {
   if constexpr ((KINDS & 2) != 0) {
     if (st.kind == STEP_GEMM) {
-      gemm_tile_any<T>(it.gemms[st.desc], tile, it.arena, smem, err);
+      gemm_tiles_any<T>(it.gemms[st.desc], tile, tile + 1, it.arena, smem, err, (it.flags & 1) != 0);
       return;
     }
   }
@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
       if ((KINDS & 1) && st.kind == STEP_TILE) {
         stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem);
       } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
-        gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err);
+        gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err,
+                          (it.flags & 1) != 0);
       } else {
         for (int64_t x = tk; x < g_end; x++) run_step<T, KINDS>(it, st, x - g.first, tb_smem, out_item, r, g.item, err);
       }
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
     if (st.kind == STEP_TILE) {
       stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem);
     } else if (st.kind == STEP_GEMM) {
-      gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
+      gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0);
     } else {
       for (int64_t x = ch.t0; x < ch.t1; x++) run_step<T>(it, st, x, tb_smem, out_item, r, g.item, err);
     }
@@ -272,6 +273,7 @@ struct tb_plan {
   DevBuf d_steps, d_tiles, d_gemms, d_leaves;
   bool structure_uploaded = false;
   bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
+  bool i16_ok = false;         // bound weights are integers >= 0 summing below 8192
   uint64_t version = 0;        // bumps when device buffers move
 };
 
@@ -461,6 +463,9 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
     it.slice_vals = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
     it.w = w_off ? reinterpret_cast<const float*>(c->wvals.p) + (*w_off)[i] : nullptr;
+    // exact packed-int16 GEMM tiles only where the per-call weights are the
+    // plan's bound ones (the batched solves)
+    it.flags = (w_off && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = done_base;
@@ -1101,6 +1106,22 @@ tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   p->weights.assign(w, w + p->h.n_labels);
   p->h.has_weights = true;
   p->leaves_dirty = true;
+  // every finite tensor value is then an integer in [0, 8191]: the GEMM tiles
+  // may add and max them as packed int16 exactly
+  double sum = 0;
+  bool ok16 = true;
+  for (int i = 0; i < p->h.n_tensors; i++) {
+    const LeafDesc& ld = p->h.leaves[i];
+    if (ld.nraw != 1) continue;
+    const float x = ld.w;
+    if (x < 0 || x != std::floor(x)) ok16 = false;
+    sum += x;
+  }
+  ok16 = ok16 && sum < 8192;
+  if (ok16 != p->i16_ok) {
+    p->i16_ok = ok16;
+    p->version = ++p->ctx->plan_counter;  // captured batches hold the flag
+  }
   return TB_OK;
 }
 
@@ -1431,6 +1452,24 @@ __global__ void __launch_bounds__(256) k_peak_f32(float* out, int iters, float s
   if (s == 1.2345f) out[0] = s;
 }
 
+// The same for the packed-int16 form: __viaddmax_s16x2, one instruction per
+// two tropical MACs; every chain's operand comes from another chain's
+// previous value, so nothing is loop-invariant.
+__global__ void __launch_bounds__(256) k_peak_i16(unsigned* out, int iters, unsigned seed) {
+  constexpr int NC = 16;
+  unsigned x[NC];
+#pragma unroll
+  for (int j = 0; j < NC; j++) x[j] = (seed * (unsigned)(j + 1 + threadIdx.x)) & 0x0fff0fffu;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int j = 0; j < NC; j++) x[j] = __viaddmax_s16x2(x[(j + 5) % NC], 0x00010001u, x[j]) & 0x7fff7fffu;
+  }
+  unsigned s = 0;
+#pragma unroll
+  for (int j = 0; j < NC; j++) s ^= x[j];
+  if (s == 0x12345678u) out[0] = s;
+}
+
 // Resident CTAs of the context's kernels (stream tiles, GEMM tiles,
 // persistent executor) and its SM count, for reports.
 extern "C" int32_t tbi_ctx_info(const tb_ctx* c, int32_t* out4) {
@@ -1486,6 +1525,52 @@ extern "C" int32_t tbi_timeout_probe(tb_ctx* c, tb_plan* p, int32_t timeout_ms) 
   c->have_key = false;
   if (e == TB_ERR_TIMEOUT) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
   return e ? fail(TB_ERR_CUDA, "unexpected device error word") : TB_OK;
+}
+
+// Measured packed-int16 max-plus rate (ops/s, a max and an add per MAC).
+extern "C" int32_t tbi_measure_maxplus_peak_i16(int32_t device, double* ops_per_s) {
+  if (!ops_per_s) return TB_ERR_INVALID;
+  CU(cudaSetDevice(device));
+  int sms = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  unsigned* out = nullptr;
+  CU(cudaMalloc(&out, 64));
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  const int blocks = sms * 8, iters = 4096;
+  k_peak_i16<<<blocks, 256>>>(out, iters, 7u);
+  float best = 1e30f;
+  for (int r = 0; r < 3; r++) {
+    cudaEventRecord(e0);
+    k_peak_i16<<<blocks, 256>>>(out, iters, 7u);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return fail(TB_ERR_CUDA, cudaGetErrorString(e));
+  // 16 chains x 1 instruction (2 MACs, 4 ops) per iteration per thread
+  *ops_per_s = (double)blocks * 256 * iters * 16 * 4 / (best * 1e-3);
+  return TB_OK;
+}
+
+// Per node of a plan: 2 if the fused form runs it as stream tiles, 3 as
+// GEMM tiles (the kind of the step that produces the node's output's parts).
+extern "C" int32_t tbi_plan_node_kinds(const tb_plan* p, int32_t* kinds) {
+  if (!p || !kinds) return TB_ERR_INVALID;
+  const PlanHost& h = p->h;
+  for (int j = 0; j < h.n_nodes; j++) kinds[j] = STEP_TILE;
+  for (size_t si = 0; si < h.steps.size(); si++) {
+    const int sn = h.step_node[si];
+    if (sn >= 0 && h.steps[si].kind == STEP_GEMM) kinds[sn] = STEP_GEMM;
+  }
+  return TB_OK;
 }
 
 extern "C" int32_t tbi_measure_maxplus_peak(int32_t device, double* ops_per_s) {

@@ -670,6 +670,39 @@ __device__ __forceinline__ void mp_step(const T* __restrict__ as, const T* __res
   }
 }
 
+// Packed-int16 form of one k-pair step: shared tiles hold [kp][x] words of
+// (x[k], x[k+1]) as two int16; __viaddmax_s16x2 adds the pairs and keeps the
+// even-k and odd-k maxima in the two halves of the accumulator.
+template <int TM, int TN, int BM, int BN>
+__device__ __forceinline__ void mp_step_i16(const uint32_t* __restrict__ as, const uint32_t* __restrict__ bs, int kp,
+                                            int wm, int wn, int lm, int ln, uint32_t (&acc)[TM][TN]) {
+  uint32_t b[TN];
+#pragma unroll
+  for (int j = 0; j < TN; j++) b[j] = bs[kp * BN + gm_col<TN, BN>(wn, ln, j)];
+#pragma unroll
+  for (int i = 0; i < TM; i++) {
+    const uint32_t a = as[kp * BM + gm_row<TM, BM>(wm, lm, i)];
+#pragma unroll
+    for (int j = 0; j < TN; j++) acc[i][j] = __viaddmax_s16x2(a, b[j], acc[i][j]);
+  }
+}
+
+// Exact int16 stand-ins for the tropical values of an MIS network whose
+// weights are integers >= 0 summing below 8192: every finite value is an
+// integer in [0, 8191], -inf becomes -8192, a sum involving it stays negative
+// and a sum of finite values stays below 16384.
+constexpr int kI16Neg = -8192;
+__device__ __forceinline__ uint32_t pack_i16(float x0, float x1) {
+  const int v0 = __float2int_rz(fmaxf(x0, (float)kI16Neg));
+  const int v1 = __float2int_rz(fmaxf(x1, (float)kI16Neg));
+  return (uint32_t)(v0 & 0xffff) | ((uint32_t)v1 << 16);
+}
+__device__ __forceinline__ float unpack_max_i16(uint32_t acc) {
+  const int lo = (int)(int16_t)(acc & 0xffffu), hi = (int)(int16_t)(acc >> 16);
+  const int m = lo > hi ? lo : hi;
+  return m < 0 ? __int_as_float(0xff800000) : (float)m;
+}
+
 template <typename T, int BM, int BN>
 __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T* __restrict__ B,
                                                T* __restrict__ C, int M, int N, int K, int64_t tiles_mn) {
@@ -824,14 +857,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-template <int BM, int BN, int S = kGemmStages, int BK = kGemmBK>
+template <int BM, int BN, int S = kGemmStages, int BK = kGemmBK, bool I16 = false>
 struct GemmSmem {
   static constexpr int KP = BK / 2;
   static constexpr int BAR_BYTES = 128;  // full[S] and empty[S] mbarriers
   static constexpr int A_STAGE = KP * BM * 2;  // elements
   static constexpr int B_STAGE = KP * BN * 2;
   static constexpr int SCAT_OFF = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;  // epilogue tables
-  static constexpr int BYTES = SCAT_OFF + (BM + BN) * 4;
+  static constexpr int PACK_OFF = SCAT_OFF + (BM + BN) * 4;  // packed-int16 chunk (I16)
+  static constexpr int BYTES = PACK_OFF + (I16 ? KP * (BM + BN) * 4 : 0);
 };
 
 // Work units [u0, u1) of one GEMM descriptor on this CTA: unit u is output
@@ -876,12 +910,14 @@ __device__ __forceinline__ void gemm_issue(const GemmDesc& d, int64_t u0, int q,
 // ring of S stages, so the next unit's operands load while this unit's last
 // chunks are reduced and its tile is stored.  Returns false after a timed-out
 // wait (err is set; copies in flight are drained with a bounded wait).
-template <typename T, int BM, int BN, int S = kGemmStages, int BK = kGemmBK>
+template <typename T, int BM, int BN, int S = kGemmStages, int BK = kGemmBK, bool I16 = false>
 __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restrict__ arena, int* __restrict__ smem,
                            int* err) {
-  using SM = GemmSmem<BM, BN, S, BK>;
+  using SM = GemmSmem<BM, BN, S, BK, I16>;
   constexpr int KP = SM::KP;
   constexpr int TM = BM / 16, TN = BN / 16;
+  static_assert(!I16 || std::is_same<T, float>::value, "packed int16 tiles stand in for f32 values");
+  using Acc = typename std::conditional<I16, uint32_t, T>::type;
   constexpr int BK_LOG2 = BK == 32 ? 5 : 4;
   static_assert(BK == 32 || BK == 16, "BK");
   const int t = threadIdx.x;
@@ -931,24 +967,55 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   for (int ui = 0; ui < n_units; ui++) {
     const int warp = t >> 5, lane = t & 31;
     const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
-    T acc[TM][TN];
+    Acc acc[TM][TN];
 #pragma unroll
     for (int i = 0; i < TM; i++)
 #pragma unroll
-      for (int j = 0; j < TN; j++) acc[i][j] = Trop<T>::neg();
+      for (int j = 0; j < TN; j++) {
+        if constexpr (I16) acc[i][j] = 0x80008000u;  // below every sum
+        else acc[i][j] = Trop<T>::neg();
+      }
     for (int kl = 0; kl < (1 << nkp_log2); kl++, q++) {
       if (ok) ok = mbar_wait(&full[slot], par);
       const T* as = As + slot * SM::A_STAGE;
       const T* bs = Bs + slot * SM::B_STAGE;
+      if constexpr (I16) {
+        // the stage's f32 k-pairs become packed int16 words in a chunk buffer
+        // of their own; the stage is released as soon as it is converted
+        constexpr int NA = KP * BM, NB = KP * BN;
+        uint32_t* pk = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(smem) + SM::PACK_OFF);
+        __syncthreads();  // every warp is done with the previous chunk's words
+        for (int e = t; e < NA; e += kThreads) {
+          const float2 v = reinterpret_cast<const float2*>(as)[e];
+          pk[e] = pack_i16(v.x, v.y);
+        }
+        for (int e = t; e < NB; e += kThreads) {
+          const float2 v = reinterpret_cast<const float2*>(bs)[e];
+          pk[NA + e] = pack_i16(v.x, v.y);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+        if (t == 0 && q + S < total_q && ok) {
+          ok = mbar_wait(&empty[slot], par);
+          if (ok) {
+            gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
+            issued = q + S + 1;
+          }
+        }
+        __syncthreads();  // the chunk's words are in place
 #pragma unroll 1
-      for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[slot]);
-      if (t == 0 && q + S < total_q && ok) {
-        ok = mbar_wait(&empty[slot], par);
-        if (ok) {
-          gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
-          issued = q + S + 1;
+        for (int kp = 0; kp < KP; kp++) mp_step_i16<TM, TN, BM, BN>(pk, pk + NA, kp, wm, wn, lm, ln, acc);
+      } else {
+#pragma unroll 1
+        for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+        if (t == 0 && q + S < total_q && ok) {
+          ok = mbar_wait(&empty[slot], par);
+          if (ok) {
+            gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
+            issued = q + S + 1;
+          }
         }
       }
       if (++slot == S) {
@@ -974,6 +1041,10 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
       T* Cb = arena + cb;
       // rows i, i + 1 (i even) of a thread differ in m bit 0 when BM >= 64:
       // adjacent in C when m bit 0 sits at C position 0
+      auto out = [&](int i, int j) -> T {
+        if constexpr (I16) return unpack_max_i16(acc[i][j]);
+        else return acc[i][j];
+      };
       if (TM >= 4 && d.m_pc[0] == 0) {
 #pragma unroll
         for (int i = 0; i < TM; i += 2) {
@@ -981,8 +1052,8 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
 #pragma unroll
           for (int j = 0; j < TN; j++) {
             typename Vec2<T>::type v;
-            v.x = acc[i][j];
-            v.y = acc[i + 1][j];
+            v.x = out(i, j);
+            v.y = out(i + 1, j);
             *reinterpret_cast<typename Vec2<T>::type*>(ro + scN[gm_col<TN, BN>(wn, ln, j)]) = v;
           }
         }
@@ -991,7 +1062,7 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
         for (int i = 0; i < TM; i++) {
           T* ro = Cb + scM[gm_row<TM, BM>(wm, lm, i)];
 #pragma unroll
-          for (int j = 0; j < TN; j++) ro[scN[gm_col<TN, BN>(wn, ln, j)]] = acc[i][j];
+          for (int j = 0; j < TN; j++) ro[scN[gm_col<TN, BN>(wn, ln, j)]] = out(i, j);
         }
       }
     }
@@ -1022,9 +1093,17 @@ __device__ __forceinline__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* ar
 // Dispatch on the CTA tile shape chosen by the plan compiler.
 template <typename T>
 __device__ __forceinline__ bool gemm_tiles_any(const GemmDesc& d, int64_t u0, int64_t u1, T* arena, int* smem,
-                                               int* err) {
+                                               int* err, bool i16 = false) {
   // copy stages: as many as fit the shared memory of the 128 x 128 form
   const int bm = d.bm_log2, bn = d.bn_log2;
+  if constexpr (std::is_same<T, float>::value) {
+    // exact packed-int16 arithmetic for the large tiles (see pack_i16)
+    if (i16) {
+      if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 2, kGemmBK, true>(d, u0, u1, arena, smem, err);
+      if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 3, kGemmBK, true>(d, u0, u1, arena, smem, err);
+      if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 3, kGemmBK, true>(d, u0, u1, arena, smem, err);
+    }
+  }
   if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 3>(d, u0, u1, arena, smem, err);
   if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 4>(d, u0, u1, arena, smem, err);
   if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 4>(d, u0, u1, arena, smem, err);
@@ -1038,6 +1117,10 @@ __device__ __forceinline__ bool gemm_tile_any(const GemmDesc& d, int64_t tile, T
 }
 
 __host__ __device__ constexpr int gemm_smem_bytes_max() { return GemmSmem<128, 128, 3>::BYTES; }
+static_assert(GemmSmem<128, 128, 2, kGemmBK, true>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<128, 64, 3, kGemmBK, true>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<64, 128, 3, kGemmBK, true>::BYTES <= gemm_smem_bytes_max(),
+              "packed-int16 GEMM stages exceed the shared memory of the 128 x 128 form");
 static_assert(GemmSmem<128, 64, 4>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<64, 128, 4>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<64, 64, 6>::BYTES <= gemm_smem_bytes_max() &&

@@ -103,6 +103,7 @@ struct ItemDev {
   const LeafDesc* leaves;
   const int8_t* slice_vals;
   const float* w;      // vertex weights by label (per call), or null: LeafDesc::w
+  int32_t flags;       // bit 0: GEMM tiles may use exact packed-int16 arithmetic
   float r;
   int32_t n_leaves;
   int32_t done_base;   // offset of this item's step counters

@@ -221,6 +221,29 @@ def measure_maxplus_peak(device: int = 0) -> float:
     return float(v.value)
 
 
+def measure_maxplus_peak_i16(device: int = 0) -> float:
+    """Measured packed-int16 max-plus rate in ops/s (__viaddmax_s16x2, two
+    tropical MACs per instruction), the ceiling of the int16 GEMM tiles."""
+    lib = _native.engine_lib()
+    f = lib.tbi_measure_maxplus_peak_i16
+    f.restype = c_int32
+    f.argtypes = [c_int32, POINTER(c_double)]
+    v = c_double()
+    _native.check(f(int(device), ctypes.byref(v)))
+    return float(v.value)
+
+
+def plan_node_kinds(plan: "Plan") -> np.ndarray:
+    """Per node: 2 = stream tiles, 3 = GEMM tiles in the fused form."""
+    lib = _native.engine_lib()
+    f = lib.tbi_plan_node_kinds
+    f.restype = c_int32
+    f.argtypes = [c_void_p, c_void_p]
+    out = np.zeros(max(plan.code.n_nodes, 1), np.int32)
+    _native.check(f(plan.handle, out.ctypes.data))
+    return out[: plan.code.n_nodes]
+
+
 def default_engine() -> Engine:
     global _default
     if _default is None:

@@ -152,3 +152,22 @@ def test_rebinding_weights_between_solves(tb, orc, engine):
     engine.bind_batch([plan, plan2], [w3, w3[::-1].copy()])
     out, _ = engine.solve_batch([plan, plan2], mode="batched")
     assert list(out) == [np.float32(orc.solve(code, w3)), np.float32(orc.solve(code, w3[::-1].copy()))]
+
+
+@pytest.mark.parametrize("kind", ["small_int", "large_int", "fractional"])
+def test_gemm_arithmetic_forms(tb, orc, engine, kind):
+    """GEMM tiles run exact packed-int16 arithmetic when the weights are
+    integers >= 0 summing below 8192, f32 otherwise; both equal the oracle."""
+    from cases import gemm_case
+
+    for shape in ((7, 7, 6, 1), (8, 7, 5, 1), (7, 6, 8, 0)):
+        g, w, code = gemm_case(tb, *shape)
+        if kind == "large_int":
+            w = (w * 300).astype(np.float32)           # sum > 8192
+        elif kind == "fractional":
+            w = (w + 0.5).astype(np.float32)
+        plan = engine.plan(code, w)
+        ref, dumps = orc.execute(code, w, node_iy=plan.all_node_labels(), dump=True)
+        for mode in ("batched", "layered"):
+            out, mx = engine.solve_batch([plan, plan], r=[0.0, 2.0], mode=mode)
+            assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode)
