@@ -426,11 +426,15 @@ def main():
     h2d = sum(4 * p.code.n_labels for p in uplans) + 4 * len(plans) + sum(len(x) for x in svs)
     d2h = 4 * (len(plans) + 1)
     host_w = [np.ascontiguousarray(_weights_of(wl, p), np.float32) for p in uplans]
+    w_offs = np.zeros(len(uplans), np.int64)
+    if len(uplans) > 1:
+        w_offs[1:] = np.cumsum([len(w) for w in host_w[:-1]])
+    w_flat = np.ascontiguousarray(np.concatenate(host_w), np.float32)  # the caller's host buffer
     if ws > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        eng.bind_batch(uplans, host_w)
+        eng.bind_batch(uplans, w_flat, w_offs)
         o, m = step()
         assert m == mx0
     t_e2e = time.perf_counter() - t0

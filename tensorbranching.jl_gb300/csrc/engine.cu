@@ -274,6 +274,8 @@ struct tb_plan {
   bool structure_uploaded = false;
   bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
   bool i16_ok = false;         // bound weights are integers >= 0 summing below 8192
+  bool mis_checked = false;    // leaves checked to be vertex / edge tensors
+  std::vector<int> vertex_leaves;
   uint64_t version = 0;        // bumps when device buffers move
 };
 
@@ -385,7 +387,9 @@ static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
     if (src) return cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice);
     return cudaSuccess;
   };
-  const PlanHost& h = p->h;
+  PlanHost& h = p->h;
+  if (p->leaves_dirty || !p->structure_uploaded)
+    for (int i : p->vertex_leaves) h.leaves[i].w = p->weights[h.leaves[i].label];
   if (!p->structure_uploaded) {
     void* before[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
     CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
@@ -1086,38 +1090,35 @@ tb_status tb_plan_node_labels(const tb_plan* p, int32_t node, int32_t cap, int32
 
 tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   if (!p || !w) return fail(TB_ERR_INVALID, "null argument");
-  const bool is_int = p->ctx->opt.dtype == TB_DTYPE_I32;
-  for (int i = 0; i < p->h.n_tensors; i++)
-    if (p->h.leaves[i].nraw < 1 || p->h.leaves[i].nraw > 2)
-      return fail(TB_ERR_INVALID, "independent-set leaves have one (vertex) or two (edge) labels");
-  for (int i = 0; i < p->h.n_tensors; i++) {
-    LeafDesc& ld = p->h.leaves[i];
-    if (ld.nraw == 1) {
-      float x = w[p->h.leaf_raw[i][0]];
-      if (!std::isfinite(x)) return fail(TB_ERR_INVALID, "weights must be finite");
-      if (is_int && (x != std::floor(x) || std::fabs(x) > 1e8f))
-        return fail(TB_ERR_INVALID, "int32 weights must be integers of magnitude below 1e8");
-      ld.w = x;
+  if (!p->mis_checked) {
+    for (int i = 0; i < p->h.n_tensors; i++) {
+      if (p->h.leaves[i].nraw < 1 || p->h.leaves[i].nraw > 2)
+        return fail(TB_ERR_INVALID, "independent-set leaves have one (vertex) or two (edge) labels");
+      if (p->h.leaves[i].nraw == 1) p->vertex_leaves.push_back(i);
     }
+    p->mis_checked = true;
   }
-  // the weights travel with each solve (one staged copy for the whole
-  // batch); the device leaf descriptors are refreshed only for the paths
-  // that read LeafDesc::w
-  p->weights.assign(w, w + p->h.n_labels);
-  p->h.has_weights = true;
-  p->leaves_dirty = true;
-  // every finite tensor value is then an integer in [0, 8191]: the GEMM tiles
-  // may add and max them as packed int16 exactly
+  const bool is_int = p->ctx->opt.dtype == TB_DTYPE_I32;
+  // every finite tensor value is an integer in [0, 8191] when the weights
+  // are integers >= 0 summing below 8192: the GEMM tiles may then add and max
+  // them as packed int16 exactly
   double sum = 0;
   bool ok16 = true;
-  for (int i = 0; i < p->h.n_tensors; i++) {
-    const LeafDesc& ld = p->h.leaves[i];
-    if (ld.nraw != 1) continue;
-    const float x = ld.w;
-    if (x < 0 || x != std::floor(x)) ok16 = false;
+  for (int i : p->vertex_leaves) {
+    const float x = w[p->h.leaves[i].label];
+    if (!std::isfinite(x)) return fail(TB_ERR_INVALID, "weights must be finite");
+    const bool integral = x == std::floor(x);
+    if (is_int && (!integral || std::fabs(x) > 1e8f))
+      return fail(TB_ERR_INVALID, "int32 weights must be integers of magnitude below 1e8");
+    if (x < 0 || !integral) ok16 = false;
     sum += x;
   }
   ok16 = ok16 && sum < 8192;
+  // the weights travel with each solve (one staged copy for the whole
+  // batch); LeafDesc::w is refreshed only for the paths that read it
+  p->weights.assign(w, w + p->h.n_labels);
+  p->h.has_weights = true;
+  p->leaves_dirty = true;
   if (ok16 != p->i16_ok) {
     p->i16_ok = ok16;
     p->version = ++p->ctx->plan_counter;  // captured batches hold the flag

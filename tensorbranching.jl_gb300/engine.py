@@ -96,26 +96,51 @@ class Engine:
             p.bind_mis(weights)
         return p
 
-    def bind_batch(self, plans, weights) -> None:
-        """tb_plan_bind_mis for many plans in one call (weights[i] for plans[i])."""
+    def bind_batch(self, plans, weights, offsets=None) -> None:
+        """tb_plan_bind_mis for many plans in one call: weights[i] for
+        plans[i], or one flat float32 array with plan i's weights at
+        offsets[i]."""
         n = len(plans)
-        ws = [np.ascontiguousarray(w, dtype=np.float32) for w in weights]
-        for p, w in zip(plans, ws):
-            if w.shape[0] < p.code.n_labels:
-                raise ValueError("one weight per label is required")
-        offs = np.zeros(n, np.int64)
-        if n > 1:
-            offs[1:] = np.cumsum([w.shape[0] for w in ws[:-1]])
-        flat = np.concatenate(ws) if n else np.zeros(1, np.float32)
-        arr = (c_void_p * max(n, 1))(*[p.handle for p in plans])
+        if offsets is None:
+            ws = [np.ascontiguousarray(w, dtype=np.float32) for w in weights]
+            for p, w in zip(plans, ws):
+                if w.shape[0] < p.code.n_labels:
+                    raise ValueError("one weight per label is required")
+            offs = np.zeros(n, np.int64)
+            if n > 1:
+                offs[1:] = np.cumsum([w.shape[0] for w in ws[:-1]])
+            flat = np.concatenate(ws) if n else np.zeros(1, np.float32)
+        else:
+            flat = weights
+            offs = offsets
+            if flat.dtype != np.float32 or not flat.flags.c_contiguous or offs.dtype != np.int64:
+                raise ValueError("flat weights must be contiguous float32 with int64 offsets")
+            for p, o in zip(plans, offs):
+                if o < 0 or o + p.code.n_labels > flat.shape[0]:
+                    raise ValueError("weights out of range")
+        cached = getattr(self, "_bind_cache", None)
+        if cached is not None and len(cached[0]) == n and all(a is b and a.handle for a, b in zip(cached[0], plans)):
+            arr = cached[1]
+        else:
+            arr = (c_void_p * max(n, 1))(*[p.handle for p in plans])
+            self._bind_cache = (list(plans), arr)
         _native.check(self.lib.tb_plan_bind_mis_batch(n, ctypes.cast(arr, c_void_p), flat.ctypes.data,
                                                       offs.ctypes.data), self.ctx)
 
-    @staticmethod
-    def _batch_args(plans, slice_vals, r):
+    def _batch_args(self, plans, slice_vals, r):
         n = len(plans)
-        arr = (c_void_p * n)(*[p.handle for p in plans])
+        # the handle array is kept with the plans it holds (so none of them
+        # can be freed while cached) and reused when the same plans come again
+        cached = getattr(self, "_arr_cache", None)
+        if cached is not None and len(cached[0]) == n and all(a is b and a.handle for a, b in zip(cached[0], plans)):
+            arr = cached[1]
+        else:
+            arr = (c_void_p * n)(*[p.handle for p in plans])
+            self._arr_cache = (list(plans), arr)
         sv = None
+        if slice_vals is not None and isinstance(slice_vals, (list, tuple)) and \
+                all(np.asarray(x).size == 0 for x in slice_vals):
+            slice_vals = None
         if slice_vals is not None:
             sv = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int8).ravel() for x in slice_vals])
                                       if isinstance(slice_vals, (list, tuple)) else
