@@ -1463,7 +1463,7 @@ __global__ void __launch_bounds__(256) k_peak_i16(unsigned* out, int iters, unsi
   for (int j = 0; j < NC; j++) x[j] = (seed * (unsigned)(j + 1 + threadIdx.x)) & 0x0fff0fffu;
   for (int it = 0; it < iters; it++) {
 #pragma unroll
-    for (int j = 0; j < NC; j++) x[j] = __viaddmax_s16x2(x[(j + 5) % NC], 0x00010001u, x[j]) & 0x7fff7fffu;
+    for (int j = 0; j < NC; j++) x[j] = __viaddmax_s16x2(x[(j + 5) % NC], 0x00010001u, x[j]);
   }
   unsigned s = 0;
 #pragma unroll
