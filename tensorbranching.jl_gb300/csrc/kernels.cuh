@@ -864,8 +864,9 @@ struct GemmSmem {
   static constexpr int A_STAGE = KP * BM * 2;  // elements
   static constexpr int B_STAGE = KP * BN * 2;
   static constexpr int SCAT_OFF = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;  // epilogue tables
-  static constexpr int PACK_OFF = SCAT_OFF + (BM + BN) * 4;  // packed-int16 chunk (I16)
-  static constexpr int BYTES = PACK_OFF + (I16 ? KP * (BM + BN) * 4 : 0);
+  static constexpr int PACK_OFF = SCAT_OFF + (BM + BN) * 4;  // two packed-int16 chunks (I16)
+  static constexpr int PACK_WORDS = KP * (BM + BN);
+  static constexpr int BYTES = PACK_OFF + (I16 ? 2 * PACK_WORDS * 4 : 0);
 };
 
 // Work units [u0, u1) of one GEMM descriptor on this CTA: unit u is output
@@ -980,11 +981,13 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
       const T* as = As + slot * SM::A_STAGE;
       const T* bs = Bs + slot * SM::B_STAGE;
       if constexpr (I16) {
-        // the stage's f32 k-pairs become packed int16 words in a chunk buffer
-        // of their own; the stage is released as soon as it is converted
+        // the stage's f32 k-pairs become packed int16 words in one of two
+        // chunk buffers (chunk q uses buffer q & 1: the last reader of that
+        // buffer was chunk q - 2, which every thread finished before the
+        // barrier of chunk q - 1)
         constexpr int NA = KP * BM, NB = KP * BN;
-        uint32_t* pk = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(smem) + SM::PACK_OFF);
-        __syncthreads();  // every warp is done with the previous chunk's words
+        uint32_t* pk =
+            reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(smem) + SM::PACK_OFF) + (q & 1) * SM::PACK_WORDS;
         for (int e = t; e < NA; e += kThreads) {
           const float2 v = reinterpret_cast<const float2*>(as)[e];
           pk[e] = pack_i16(v.x, v.y);
@@ -993,16 +996,12 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
           const float2 v = reinterpret_cast<const float2*>(bs)[e];
           pk[NA + e] = pack_i16(v.x, v.y);
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[slot]);
+        __syncthreads();  // the chunk's words are in place and its stage is free
         if (t == 0 && q + S < total_q && ok) {
-          ok = mbar_wait(&empty[slot], par);
-          if (ok) {
-            gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
-            issued = q + S + 1;
-          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // reads above, then async writes
+          gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
+          issued = q + S + 1;
         }
-        __syncthreads();  // the chunk's words are in place
 #pragma unroll 1
         for (int kp = 0; kp < KP; kp++) mp_step_i16<TM, TN, BM, BN>(pk, pk + NA, kp, wm, wn, lm, ln, acc);
       } else {
