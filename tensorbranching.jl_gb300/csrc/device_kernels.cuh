@@ -1,0 +1,274 @@
+// Kernels of the engine: thin __global__ wrappers over the device routines
+// of kernels.cuh, and the host-side launch wrappers of launch.h.  Each
+// kern_*.cu translation unit instantiates a share of them so the device code
+// compiles in parallel.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "../../include/tb.h"
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace tb {
+
+// ---------------------------------------------------------------------------
+// kernels (thin __global__ wrappers over the device routines)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_leaves(const LeafDesc* leaves, int n, const int8_t* sv, T* arena,
+                                                     const float* w) {
+  leaves_tile<T>(leaves, n, sv, arena, blockIdx.x, w);
+}
+
+// A stream-tile node: CTA b runs tiles [b * chunk, (b + 1) * chunk).
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 2) k_tile(const TileDesc d, T* arena, int64_t chunk) {
+  extern __shared__ int tb_smem[];
+  const int64_t t0 = (int64_t)blockIdx.x * chunk;
+  const int64_t t1 = t0 + chunk < d.n_tiles ? t0 + chunk : d.n_tiles;
+  stream_tiles<T>(d, t0, t1, arena, tb_smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_final(const FinalDesc f, const T* arena, float r, float* out) {
+  final_tile<T>(f, arena, r, out);
+}
+
+// Leaves and final steps (stream and GEMM steps run as runs of tiles).
+template <typename T>
+__device__ __forceinline__ void run_small_step(const ItemDev<T>& it, const Step& st, int64_t tile, float* out_item,
+                                               const float* r, int item) {
+  if (st.kind == STEP_LEAVES) leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile, it.w);
+  else if (st.kind == STEP_FINAL) final_tile<T>(it.fin, it.arena, r ? r[item] : 0.0f, out_item + item);
+}
+
+__device__ __forceinline__ int find_group(const Group* groups, int n_groups, int64_t tk) {
+  int lo = 0, hi = n_groups - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (groups[mid].first <= tk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One launch per tree level: block b runs ticket first_ticket + b.  No
+// waiting: the previous launch on the stream finished every dependency.
+template <typename T, int KINDS>
+__global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
+                                                   int64_t first_ticket, int64_t last_ticket, int64_t chunk,
+                                                   float* out_item, const float* r, int* err) {
+  extern __shared__ int tb_smem[];
+  __shared__ int s_g;
+  {
+    // CTA b runs tickets [b * chunk, (b + 1) * chunk) of this level, a run of
+    // tiles per group: each stream tile builds its tables once, each GEMM run
+    // keeps one copy pipeline across its tiles
+    int64_t tk = first_ticket + (int64_t)blockIdx.x * chunk;
+    const int64_t end = tk + chunk < last_ticket ? tk + chunk : last_ticket;
+    while (tk < end) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
+      __syncthreads();
+      const int gi = s_g;
+      const Group g = groups[gi];
+      const int64_t g_end = gi + 1 < n_groups && groups[gi + 1].first < end ? groups[gi + 1].first : end;
+      const ItemDev<T>& it = items[g.item];
+      const Step& st = it.steps[g.step];
+      if ((KINDS & 1) && st.kind == STEP_TILE) {
+        stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err);
+      } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
+        gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err,
+                          (it.flags & 1) != 0);
+      } else {
+        for (int64_t x = tk; x < g_end; x++) run_small_step<T>(it, st, x - g.first, out_item, r, g.item);
+      }
+      tk = g_end;
+    }
+  }
+}
+
+// Persistent executor.  Chunks of tiles are handed out in dependency order,
+// so a chunk only waits on chunks already held by running CTAs; every wait is
+// bounded by timeout_ns and ends with err set instead of hanging.
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* items, const Group* groups,
+                                                           const Chunk* chunks, int64_t n_chunks, int* done,
+                                                           unsigned long long* ticket, int* err, float* out_item,
+                                                           const float* r, int64_t timeout_ns) {
+  extern __shared__ int tb_smem[];
+  __shared__ long long s_c;
+  __shared__ int s_stop;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long c = (long long)atomicAdd(ticket, 1ull);
+      int stop = (c >= n_chunks) || (*(volatile int*)err != 0);
+      if (!stop) {
+        const Group g = groups[chunks[c].group];
+        const ItemDev<T>& it = items[g.item];
+        const Step st = it.steps[g.step];
+        const int deps[2] = {st.dep0, st.dep1};
+        uint64_t t0 = globaltimer();
+        for (int d = 0; d < 2 && !stop; d++) {
+          if (deps[d] < 0) continue;
+          const int need = it.steps[deps[d]].n_tiles;
+          const int* cnt = done + it.done_base + deps[d];
+          while (ld_acquire(cnt) < need) {
+            if (*(volatile int*)err != 0) { stop = 1; break; }
+            if (globaltimer() - t0 > (uint64_t)timeout_ns) {
+              atomicExch(err, TB_ERR_TIMEOUT);
+              stop = 1;
+              break;
+            }
+            __nanosleep(128);
+          }
+        }
+      }
+      s_c = c;
+      s_stop = stop;
+    }
+    __syncthreads();
+    if (s_stop) break;
+    const Chunk ch = chunks[s_c];
+    const Group g = groups[ch.group];
+    const ItemDev<T>& it = items[g.item];
+    const Step& st = it.steps[g.step];
+    if (st.kind == STEP_TILE) {
+      stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
+    } else if (st.kind == STEP_GEMM) {
+      gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0);
+    } else {
+      for (int64_t x = ch.t0; x < ch.t1; x++) run_small_step<T>(it, st, x, out_item, r, g.item);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(done + it.done_base + g.step, (int)(ch.t1 - ch.t0));
+  }
+}
+
+template <typename T, int BM, int BN>
+inline cudaError_t launch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
+                             cudaStream_t s) {
+  using Cfg = K1Cfg<T, BM, BN>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(gemm_k1<T, BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES);
+    attr = true;
+  }
+  int64_t tiles_mn = (M / BM) * (N / BN);
+  int64_t grid = tiles_mn * batch;
+  if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  gemm_k1<T, BM, BN><<<(unsigned)grid, 256, Cfg::SMEM_BYTES, s>>>(A, B, C, (int)M, (int)N, (int)K, tiles_mn);
+  return cudaGetLastError();
+}
+
+template <typename T>
+inline cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
+                               cudaStream_t s) {
+  int bm = M >= 128 ? 128 : M >= 64 ? 64 : M >= 32 ? 32 : 16;
+  int bn = N >= 128 ? 128 : N >= 64 ? 64 : N >= 32 ? 32 : 16;
+#define K1_CASE(X, Y) \
+  if (bm == X && bn == Y) return launch_k1<T, X, Y>(A, B, C, M, N, K, batch, s);
+  K1_CASE(128, 128) K1_CASE(128, 64) K1_CASE(128, 32) K1_CASE(128, 16)
+  K1_CASE(64, 128) K1_CASE(64, 64) K1_CASE(64, 32) K1_CASE(64, 16)
+  K1_CASE(32, 128) K1_CASE(32, 64) K1_CASE(32, 32) K1_CASE(32, 16)
+  K1_CASE(16, 128) K1_CASE(16, 64) K1_CASE(16, 32) K1_CASE(16, 16)
+#undef K1_CASE
+  return cudaErrorInvalidValue;
+}
+
+
+// ---------------------------------------------------------------------------
+// launch wrappers (declared in launch.h)
+// ---------------------------------------------------------------------------
+template <typename T>
+cudaError_t launch_leaves(unsigned grid, cudaStream_t s, const LeafDesc* leaves, int n, const int8_t* sv, T* arena,
+                          const float* w) {
+  k_leaves<T><<<grid, kThreads, 0, s>>>(leaves, n, sv, arena, w);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_tile(unsigned grid, int smem, cudaStream_t s, const TileDesc& d, T* arena, int64_t chunk) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         stream_smem_words_max() * 4);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_tile<T><<<grid, kThreads, smem, s>>>(d, arena, chunk);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_final(cudaStream_t s, const FinalDesc& f, const T* arena, float r, float* out) {
+  k_final<T><<<1, kThreads, 0, s>>>(f, arena, r, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_k1_any(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
+                          cudaStream_t s) {
+  return dispatch_k1<T>(A, B, C, M, N, K, batch, s);
+}
+
+template <typename T, int KINDS>
+static cudaError_t level_attr(int smem) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_level<T, KINDS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  return cudaSuccess;
+}
+
+template <typename T, int KINDS>
+cudaError_t launch_level(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const Group* groups,
+                         int n_groups, int64_t first, int64_t last, int64_t chunk, float* out_item, const float* r,
+                         int* err) {
+  cudaError_t e = level_attr<T, KINDS>(smem);
+  if (e != cudaSuccess) return e;
+  k_level<T, KINDS><<<grid, kThreads, smem, s>>>(items, groups, n_groups, first, last, chunk, out_item, r, err);
+  return cudaGetLastError();
+}
+
+template <typename T, int KINDS>
+cudaError_t occupancy_level(int* per_sm, int smem) {
+  cudaError_t e = level_attr<T, KINDS>(smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_level<T, KINDS>, kThreads, smem);
+}
+
+template <typename T>
+static cudaError_t persistent_attr(int smem) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t launch_persistent(unsigned ctas, int smem, cudaStream_t s, const ItemDev<T>* items, const Group* groups,
+                              const Chunk* chunks, int64_t n_chunks, int* done, unsigned long long* ticket, int* err,
+                              float* out_item, const float* r, int64_t timeout_ns) {
+  cudaError_t e = persistent_attr<T>(smem);
+  if (e != cudaSuccess) return e;
+  k_persistent<T><<<ctas, kThreads, smem, s>>>(items, groups, chunks, n_chunks, done, ticket, err, out_item, r,
+                                               timeout_ns);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t occupancy_persistent(int* per_sm, int smem) {
+  cudaError_t e = persistent_attr<T>(smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_persistent<T>, kThreads, smem);
+}
+
+}  // namespace tb

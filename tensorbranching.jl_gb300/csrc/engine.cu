@@ -25,33 +25,12 @@
 
 #include "../../include/tb.h"
 #include "kernels.cuh"
+#include "launch.h"
 #include "plan.h"
 
 using namespace tb;
 
 // ---------------------------------------------------------------------------
-// kernels (thin __global__ wrappers over the device routines)
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_leaves(const LeafDesc* leaves, int n, const int8_t* sv, T* arena,
-                                                     const float* w) {
-  leaves_tile<T>(leaves, n, sv, arena, blockIdx.x, w);
-}
-
-// A stream-tile node: CTA b runs tiles [b * chunk, (b + 1) * chunk).
-template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_tile(const TileDesc d, T* arena, int64_t chunk) {
-  extern __shared__ int tb_smem[];
-  const int64_t t0 = (int64_t)blockIdx.x * chunk;
-  const int64_t t1 = t0 + chunk < d.n_tiles ? t0 + chunk : d.n_tiles;
-  stream_tiles<T>(d, t0, t1, arena, tb_smem);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_final(const FinalDesc f, const T* arena, float r, float* out) {
-  final_tile<T>(f, arena, r, out);
-}
-
 // K4: max over per-item results (warp-shuffle tree).
 __global__ void __launch_bounds__(kThreads) k_reduce_max(const float* v, int n, float* out) {
   __shared__ float wmax[kThreads / 32];
@@ -65,166 +44,6 @@ __global__ void __launch_bounds__(kThreads) k_reduce_max(const float* v, int n, 
     for (int w = 1; w < kThreads / 32; w++) b = fmaxf(b, wmax[w]);
     *out = b;
   }
-}
-
-// KINDS: 1 = leaves / stream tiles / final, 2 = GEMM tiles, 3 = both.
-template <typename T, int KINDS = 3>
-__device__ __forceinline__ void run_step(const ItemDev<T>& it, const Step& st, int64_t tile, int* smem,
-                                         float* out_item, const float* r, int item, int* err) {
-  if constexpr ((KINDS & 2) != 0) {
-    if (st.kind == STEP_GEMM) {
-      gemm_tiles_any<T>(it.gemms[st.desc], tile, tile + 1, it.arena, smem, err, (it.flags & 1) != 0);
-      return;
-    }
-  }
-  if constexpr ((KINDS & 1) == 0) return;
-  switch (st.kind) {
-    case STEP_LEAVES:
-      leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile, it.w);
-      break;
-    case STEP_TILE:
-      stream_tile<T>(it.tiles[st.desc], tile, it.arena, smem);
-      break;
-    case STEP_FINAL:
-      final_tile<T>(it.fin, it.arena, r ? r[item] : 0.0f, out_item + item);
-      break;
-    default:
-      break;
-  }
-}
-
-__device__ __forceinline__ int find_group(const Group* groups, int n_groups, int64_t tk) {
-  int lo = 0, hi = n_groups - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (groups[mid].first <= tk) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
-// One launch per tree level: block b runs ticket first_ticket + b.  No
-// waiting: the previous launch on the stream finished every dependency.
-template <typename T, int KINDS>
-__global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
-                                                   int64_t first_ticket, int64_t last_ticket, int64_t chunk,
-                                                   float* out_item, const float* r, int* err) {
-  extern __shared__ int tb_smem[];
-  __shared__ int s_g;
-  {
-    // CTA b runs tickets [b * chunk, (b + 1) * chunk) of this level, a run of
-    // tiles per group: each stream tile builds its tables once, each GEMM run
-    // keeps one copy pipeline across its tiles
-    int64_t tk = first_ticket + (int64_t)blockIdx.x * chunk;
-    const int64_t end = tk + chunk < last_ticket ? tk + chunk : last_ticket;
-    while (tk < end) {
-      __syncthreads();
-      if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
-      __syncthreads();
-      const int gi = s_g;
-      const Group g = groups[gi];
-      const int64_t g_end = gi + 1 < n_groups && groups[gi + 1].first < end ? groups[gi + 1].first : end;
-      const ItemDev<T>& it = items[g.item];
-      const Step& st = it.steps[g.step];
-      if ((KINDS & 1) && st.kind == STEP_TILE) {
-        stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem);
-      } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
-        gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err,
-                          (it.flags & 1) != 0);
-      } else {
-        for (int64_t x = tk; x < g_end; x++) run_step<T, KINDS>(it, st, x - g.first, tb_smem, out_item, r, g.item, err);
-      }
-      tk = g_end;
-    }
-  }
-}
-
-// Persistent executor.  Chunks of tiles are handed out in dependency order,
-// so a chunk only waits on chunks already held by running CTAs; every wait is
-// bounded by timeout_ns and ends with err set instead of hanging.
-template <typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* items, const Group* groups,
-                                                           const Chunk* chunks, int64_t n_chunks, int* done,
-                                                           unsigned long long* ticket, int* err, float* out_item,
-                                                           const float* r, int64_t timeout_ns) {
-  extern __shared__ int tb_smem[];
-  __shared__ long long s_c;
-  __shared__ int s_stop;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      long long c = (long long)atomicAdd(ticket, 1ull);
-      int stop = (c >= n_chunks) || (*(volatile int*)err != 0);
-      if (!stop) {
-        const Group g = groups[chunks[c].group];
-        const ItemDev<T>& it = items[g.item];
-        const Step st = it.steps[g.step];
-        const int deps[2] = {st.dep0, st.dep1};
-        uint64_t t0 = globaltimer();
-        for (int d = 0; d < 2 && !stop; d++) {
-          if (deps[d] < 0) continue;
-          const int need = it.steps[deps[d]].n_tiles;
-          const int* cnt = done + it.done_base + deps[d];
-          while (ld_acquire(cnt) < need) {
-            if (*(volatile int*)err != 0) { stop = 1; break; }
-            if (globaltimer() - t0 > (uint64_t)timeout_ns) {
-              atomicExch(err, TB_ERR_TIMEOUT);
-              stop = 1;
-              break;
-            }
-            __nanosleep(128);
-          }
-        }
-      }
-      s_c = c;
-      s_stop = stop;
-    }
-    __syncthreads();
-    if (s_stop) break;
-    const Chunk ch = chunks[s_c];
-    const Group g = groups[ch.group];
-    const ItemDev<T>& it = items[g.item];
-    const Step& st = it.steps[g.step];
-    if (st.kind == STEP_TILE) {
-      stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem);
-    } else if (st.kind == STEP_GEMM) {
-      gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0);
-    } else {
-      for (int64_t x = ch.t0; x < ch.t1; x++) run_step<T>(it, st, x, tb_smem, out_item, r, g.item, err);
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(done + it.done_base + g.step, (int)(ch.t1 - ch.t0));
-  }
-}
-
-template <typename T, int BM, int BN>
-static cudaError_t launch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
-                             cudaStream_t s) {
-  using Cfg = K1Cfg<T, BM, BN>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(gemm_k1<T, BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES);
-    attr = true;
-  }
-  int64_t tiles_mn = (M / BM) * (N / BN);
-  int64_t grid = tiles_mn * batch;
-  if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  gemm_k1<T, BM, BN><<<(unsigned)grid, 256, Cfg::SMEM_BYTES, s>>>(A, B, C, (int)M, (int)N, (int)K, tiles_mn);
-  return cudaGetLastError();
-}
-
-template <typename T>
-static cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
-                               cudaStream_t s) {
-  int bm = M >= 128 ? 128 : M >= 64 ? 64 : M >= 32 ? 32 : 16;
-  int bn = N >= 128 ? 128 : N >= 64 ? 64 : N >= 32 ? 32 : 16;
-#define K1_CASE(X, Y) \
-  if (bm == X && bn == Y) return launch_k1<T, X, Y>(A, B, C, M, N, K, batch, s);
-  K1_CASE(128, 128) K1_CASE(128, 64) K1_CASE(128, 32) K1_CASE(128, 16)
-  K1_CASE(64, 128) K1_CASE(64, 64) K1_CASE(64, 32) K1_CASE(64, 16)
-  K1_CASE(32, 128) K1_CASE(32, 64) K1_CASE(32, 32) K1_CASE(32, 16)
-  K1_CASE(16, 128) K1_CASE(16, 64) K1_CASE(16, 32) K1_CASE(16, 16)
-#undef K1_CASE
-  return cudaErrorInvalidValue;
 }
 
 // ---------------------------------------------------------------------------
@@ -362,16 +181,9 @@ static int smem_bytes(int kinds) {
 }
 static int max_stream_smem_bytes() { return smem_bytes(3); }
 
+// The launch wrappers set each kernel's shared-memory limit on first use.
 template <typename T>
 static tb_status set_kernel_attrs() {
-  static bool done = false;
-  if (done) return TB_OK;
-  int sm = max_stream_smem_bytes();
-  CU(cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)));
-  CU(cudaFuncSetAttribute(k_level<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)));
-  CU(cudaFuncSetAttribute(k_level<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2)));
-  CU(cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-  done = true;
   return TB_OK;
 }
 
@@ -417,15 +229,15 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
   const PlanHost& h = p->h;
   cudaStream_t s = c->stream;
   if (leaves_from_mis) {
-    k_leaves<T><<<(h.n_tensors + kThreads - 1) / kThreads, kThreads, 0, s>>>(
-        reinterpret_cast<const LeafDesc*>(p->d_leaves.p), h.n_tensors, d_sv, arena, d_w);
+    CU(launch_leaves<T>((h.n_tensors + kThreads - 1) / kThreads, s, 
+        reinterpret_cast<const LeafDesc*>(p->d_leaves.p), h.n_tensors, d_sv, arena, d_w));
     CU(cudaGetLastError());
     launches++;
   }
   if (h.n_nodes == 0) {
     const TileDesc& d = h.tiles[0];
     int64_t grid = std::min<int64_t>(d.n_tiles, c->stream_ctas);
-    k_tile<T><<<(unsigned)grid, kThreads, stream_smem_words(d) * 4, s>>>(d, arena, (d.n_tiles + grid - 1) / grid);
+    CU(launch_tile<T>((unsigned)grid, stream_smem_words(d) * 4, s, d, arena, (d.n_tiles + grid - 1) / grid));
     CU(cudaGetLastError());
     launches++;
     return TB_OK;
@@ -434,11 +246,11 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
     for (const PlainOp& op : h.plain[j]) {
       if (op.kind == PLAIN_TILE) {
         int64_t grid = std::min<int64_t>(op.tile.n_tiles, c->stream_ctas);
-        k_tile<T><<<(unsigned)grid, kThreads, stream_smem_words(op.tile) * 4, s>>>(op.tile, arena,
-                                                                                    (op.tile.n_tiles + grid - 1) / grid);
+        CU(launch_tile<T>((unsigned)grid, stream_smem_words(op.tile) * 4, s, op.tile, arena,
+                                                                                    (op.tile.n_tiles + grid - 1) / grid));
         CU(cudaGetLastError());
       } else {
-        CU(dispatch_k1<T>(arena + op.a_off, arena + op.b_off, arena + op.c_off, op.M, op.N, op.K, op.batch, s));
+        CU(launch_k1_any<T>(arena + op.a_off, arena + op.b_off, arena + op.c_off, op.M, op.N, op.K, op.batch, s));
       }
       launches++;
     }
@@ -587,10 +399,10 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
     int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
     int64_t timeout_ns = (int64_t)c->opt.timeout_ms * 1000000LL;
-    k_persistent<T><<<c->persistent_ctas, kThreads, smem, s>>>(items, groups,
+    CU(launch_persistent<T>(c->persistent_ctas, smem, s, items, groups,
                                                                reinterpret_cast<const Chunk*>(c->chunks.p),
                                                                c->n_chunks, reinterpret_cast<int*>(c->done.p),
-                                                               ticket, err, out_item, rv, timeout_ns);
+                                                               ticket, err, out_item, rv, timeout_ns));
     CU(cudaGetLastError());
     launches++;
   } else {
@@ -599,14 +411,14 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
       if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
       if (lr.kinds == 2) {
         const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-        k_level<T, 2><<<(unsigned)grid, kThreads, smem_bytes(2), s>>>(
+        CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), s, 
             items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv,
-            err);
+            err)));
       } else {
         const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-        k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), s>>>(
+        CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, 
             items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv,
-            err);
+            err)));
       }
       CU(cudaGetLastError());
       launches++;
@@ -694,8 +506,8 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
       tb_plan* p = plans[i];
       const int8_t* d_sv = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
       if ((st = plain_item<T>(c, p, arena, d_sv, true, d_w + w_off[i], launches))) return st;
-      k_final<T><<<1, kThreads, 0, c->stream>>>(p->h.fin, arena, r ? r[i] : 0.0f,
-                                                reinterpret_cast<float*>(c->out_item.p) + i);
+      CU(launch_final<T>(c->stream, p->h.fin, arena, r ? r[i] : 0.0f,
+                                                reinterpret_cast<float*>(c->out_item.p) + i));
       CU(cudaGetLastError());
       launches++;
       // synchronous read-back per item (Array(...)[] in solve_slice)
@@ -823,10 +635,11 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
 // ---------------------------------------------------------------------------
 // Autotuner: tile shapes, then the executor's schedule, by timing the batch.
 // ---------------------------------------------------------------------------
-static void retile_all(tb_ctx* c, const std::vector<tb_plan*>& uniq, int bits, std::string& err) {
+static void retile_all(tb_ctx* c, const std::vector<tb_plan*>& uniq, int bits, std::string& err,
+                       bool bulk = false) {
   for (tb_plan* p : uniq) {
-    if (p->h.tile_bits == bits) continue;
-    std::string e = retile_plan(p->h, bits);
+    if (p->h.tile_bits == bits && p->h.bulk_copies == bulk) continue;
+    std::string e = retile_plan(p->h, bits, bulk);
     if (!e.empty()) {
       err = e;
       return;
@@ -882,6 +695,18 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   }
   retile_all(c, uniq, best_bits, err);
   if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
+  // bulk-copy staging of the stream tiles that allow it
+  bool best_bulk = false;
+  retile_all(c, uniq, best_bits, err, true);
+  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
+  if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
+  res.n_tried++;
+  if (ms < best) {
+    best = ms;
+    best_bulk = true;
+  }
+  retile_all(c, uniq, best_bits, err, best_bulk);
+  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
   // 2. schedule: per-level launches, or the persistent executor with 1..max
   // CTAs per SM and coarser or finer runs of stream tiles
   int best_mode = TB_MODE_BATCHED, best_cps = c->ctas_per_sm_max, best_div = 4;
@@ -912,6 +737,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   c->chunk_div = best_div;
   res.mode = best_mode;
   res.tile_bits = best_bits;
+  res.bulk_copies = best_bulk ? 1 : 0;
   res.ctas_per_sm = c->persistent_ctas / std::max(1, c->sms);
   res.chunk_div = best_div;
   res.ms = best;
@@ -976,23 +802,23 @@ tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
   if (st) return st;
   int per_sm = 0;
   if (c->opt.dtype == TB_DTYPE_F32)
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<float>, kThreads, max_stream_smem_bytes()));
+    CU(occupancy_persistent<float>(&per_sm, max_stream_smem_bytes()));
   else
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<int32_t>, kThreads, max_stream_smem_bytes()));
+    CU(occupancy_persistent<int32_t>(&per_sm, max_stream_smem_bytes()));
   per_sm = std::max(1, per_sm);
   c->ctas_per_sm_max = per_sm;
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : per_sm * c->sms;
   int per_sm_stream = 0;
   if (c->opt.dtype == TB_DTYPE_F32)
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_stream, k_level<float, 1>, kThreads, smem_bytes(1)));
+    CU((occupancy_level<float, 1>(&per_sm_stream, smem_bytes(1))));
   else
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_stream, k_level<int32_t, 1>, kThreads, smem_bytes(1)));
+    CU((occupancy_level<int32_t, 1>(&per_sm_stream, smem_bytes(1))));
   c->stream_ctas = std::max(1, per_sm_stream) * c->sms;
   int per_sm_gemm = 0;
   if (c->opt.dtype == TB_DTYPE_F32)
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_gemm, k_level<float, 2>, kThreads, smem_bytes(2)));
+    CU((occupancy_level<float, 2>(&per_sm_gemm, smem_bytes(2))));
   else
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_gemm, k_level<int32_t, 2>, kThreads, smem_bytes(2)));
+    CU((occupancy_level<int32_t, 2>(&per_sm_gemm, smem_bytes(2))));
   c->gemm_ctas = std::max(1, per_sm_gemm) * c->sms;
   *out = c.release();
   return TB_OK;
@@ -1228,14 +1054,14 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
     for (auto& lr : c->level_ranges) {
       if (lr.kinds == 2) {
         const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-        k_level<T, 2><<<(unsigned)grid, kThreads, smem_bytes(2), c->stream>>>(
+        CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, 
             items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr,
-            err);
+            err)));
       } else {
         const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-        k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), c->stream>>>(
+        CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, 
             items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr,
-            err);
+            err)));
       }
       CU(cudaGetLastError());
     }
@@ -1333,9 +1159,9 @@ tb_status tb_gemm_device(tb_ctx* c, int64_t M, int64_t N, int64_t K, int64_t bat
   CU(cudaSetDevice(c->device));
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);  // NULL: the default stream
   if (c->opt.dtype == TB_DTYPE_F32) {
-    CU(dispatch_k1<float>((const float*)A, (const float*)B, (float*)C, M, N, K, batch, s));
+    CU(launch_k1_any<float>((const float*)A, (const float*)B, (float*)C, M, N, K, batch, s));
   } else {
-    CU(dispatch_k1<int32_t>((const int32_t*)A, (const int32_t*)B, (int32_t*)C, M, N, K, batch, s));
+    CU(launch_k1_any<int32_t>((const int32_t*)A, (const int32_t*)B, (int32_t*)C, M, N, K, batch, s));
   }
   return TB_OK;
 }
@@ -1356,15 +1182,15 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
                                      const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
                                      const int32_t* children, const int32_t* node_iy_off,
                                      const int32_t* node_iy_lab, int32_t n_sliced, const int32_t* sliced,
-                                     int32_t gemm_min, int32_t tile_bits, void** blob, int64_t* blob_bytes,
-                                     char* err, int32_t err_cap) {
+                                     int32_t gemm_min, int32_t tile_bits, int32_t bulk, void** blob,
+                                     int64_t* blob_bytes, char* err, int32_t err_cap) {
   PlanInput in;
   in.n_labels = n_labels; in.n_tensors = n_tensors; in.ix_off = ix_off; in.ix_lab = ix_lab;
   in.n_iy = n_iy; in.iy = iy; in.n_nodes = n_nodes; in.children = children;
   in.node_iy_off = node_iy_off; in.node_iy_lab = node_iy_lab; in.n_sliced = n_sliced; in.sliced = sliced;
   PlanHost h;
   std::string e = compile_plan(in, h, gemm_min);
-  if (e.empty() && tile_bits != h.tile_bits) e = retile_plan(h, tile_bits);
+  if (e.empty() && (tile_bits != h.tile_bits || bulk)) e = retile_plan(h, tile_bits, bulk != 0);
   if (!e.empty()) {
     if (err && err_cap > 0) {
       std::strncpy(err, e.c_str(), err_cap - 1);
@@ -1515,10 +1341,10 @@ extern "C" int32_t tbi_timeout_probe(tb_ctx* c, tb_plan* p, int32_t timeout_ms) 
   CU(cudaMemsetAsync(c->rvals.p, 0, 16, c->stream));
   unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
   int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
-  k_persistent<float><<<c->persistent_ctas, kThreads, max_stream_smem_bytes(), c->stream>>>(
+  CU(launch_persistent<float>(c->persistent_ctas, max_stream_smem_bytes(), c->stream, 
       reinterpret_cast<const ItemDev<float>*>(c->items.p), reinterpret_cast<const Group*>(c->groups.p), ch, 1,
       reinterpret_cast<int*>(c->done.p), ticket, err, reinterpret_cast<float*>(c->out_item.p),
-      reinterpret_cast<const float*>(c->rvals.p), (int64_t)timeout_ms * 1000000LL);
+      reinterpret_cast<const float*>(c->rvals.p), (int64_t)timeout_ms * 1000000LL));
   CU(cudaGetLastError());
   CU(cudaStreamSynchronize(c->stream));
   int e = 0;
@@ -1558,6 +1384,18 @@ extern "C" int32_t tbi_measure_maxplus_peak_i16(int32_t device, double* ops_per_
   if (e != cudaSuccess) return fail(TB_ERR_CUDA, cudaGetErrorString(e));
   // 16 chains x 1 instruction (2 MACs, 4 ops) per iteration per thread
   *ops_per_s = (double)blocks * 256 * iters * 16 * 4 / (best * 1e-3);
+  return TB_OK;
+}
+
+// Re-tile a plan's stream steps (tile size, bulk-copy staging), as the
+// autotuner does; for tests that pin one configuration.
+extern "C" int32_t tbi_plan_retile(tb_plan* p, int32_t bits, int32_t bulk) {
+  if (!p) return TB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(p->ctx->mu);
+  std::string e = retile_plan(p->h, bits, bulk != 0);
+  if (!e.empty()) return fail(TB_ERR_INVALID, e);
+  p->structure_uploaded = false;
+  p->version = ++p->ctx->plan_counter;
   return TB_OK;
 }
 
@@ -1794,16 +1632,16 @@ static tb_status serve_step(Server* S) {
   int* derr = reinterpret_cast<int*>(S->err.p);
   if (t1 > 0) {
     const int64_t grid = std::min<int64_t>(t1, c->stream_ctas);
-    k_level<T, 1><<<(unsigned)grid, kThreads, smem_bytes(1), s>>>(di, dg, (int)g1.size(), 0, t1, (t1 + grid - 1) / grid,
-                                                                   dout, drv, derr);
+    CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, di, dg, (int)g1.size(), 0, t1, (t1 + grid - 1) / grid,
+                                                                   dout, drv, derr)));
     CU(cudaGetLastError());
     S->launches++;
   }
   if (t2 > 0) {
     if (t2 > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "step too large for one launch");
     const int64_t grid2 = std::min<int64_t>(t2, c->gemm_ctas);
-    k_level<T, 2><<<(unsigned)grid2, kThreads, smem_bytes(2), s>>>(di, dg + g1.size(), (int)g2.size(), 0, t2,
-                                                                   (t2 + grid2 - 1) / grid2, dout, drv, derr);
+    CU((launch_level<T, 2>((unsigned)grid2, smem_bytes(2), s, di, dg + g1.size(), (int)g2.size(), 0, t2,
+                                                                   (t2 + grid2 - 1) / grid2, dout, drv, derr)));
     CU(cudaGetLastError());
     S->launches++;
   }
