@@ -109,8 +109,7 @@ typedef struct tb_tune_result {
   double ms;           /* device time of the batch with the chosen settings */
   double ms_default;   /* device time with the defaults */
   int32_t n_tried;     /* configurations timed */
-  int32_t bulk_copies; /* 1: stream tiles stage long contiguous runs with bulk copies */
-  int32_t reserved[6];
+  int32_t reserved[7];
 } tb_tune_result;
 
 /* Fill *opt with defaults (f32, graphs on, autotune on for TB_MODE_AUTO). */

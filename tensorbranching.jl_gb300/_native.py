@@ -66,8 +66,7 @@ class TbTuneResult(ctypes.Structure):
         ("ms", c_double),
         ("ms_default", c_double),
         ("n_tried", c_int32),
-        ("bulk_copies", c_int32),
-        ("reserved", c_int32 * 6),
+        ("reserved", c_int32 * 7),
     ]
 
 

@@ -635,11 +635,10 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
 // ---------------------------------------------------------------------------
 // Autotuner: tile shapes, then the executor's schedule, by timing the batch.
 // ---------------------------------------------------------------------------
-static void retile_all(tb_ctx* c, const std::vector<tb_plan*>& uniq, int bits, std::string& err,
-                       bool bulk = false) {
+static void retile_all(tb_ctx* c, const std::vector<tb_plan*>& uniq, int bits, std::string& err) {
   for (tb_plan* p : uniq) {
-    if (p->h.tile_bits == bits && p->h.bulk_copies == bulk) continue;
-    std::string e = retile_plan(p->h, bits, bulk);
+    if (p->h.tile_bits == bits) continue;
+    std::string e = retile_plan(p->h, bits);
     if (!e.empty()) {
       err = e;
       return;
@@ -695,18 +694,6 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   }
   retile_all(c, uniq, best_bits, err);
   if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
-  // bulk-copy staging of the stream tiles that allow it
-  bool best_bulk = false;
-  retile_all(c, uniq, best_bits, err, true);
-  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
-  if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
-  res.n_tried++;
-  if (ms < best) {
-    best = ms;
-    best_bulk = true;
-  }
-  retile_all(c, uniq, best_bits, err, best_bulk);
-  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
   // 2. schedule: per-level launches, or the persistent executor with 1..max
   // CTAs per SM and coarser or finer runs of stream tiles
   int best_mode = TB_MODE_BATCHED, best_cps = c->ctas_per_sm_max, best_div = 4;
@@ -737,7 +724,6 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   c->chunk_div = best_div;
   res.mode = best_mode;
   res.tile_bits = best_bits;
-  res.bulk_copies = best_bulk ? 1 : 0;
   res.ctas_per_sm = c->persistent_ctas / std::max(1, c->sms);
   res.chunk_div = best_div;
   res.ms = best;
@@ -1182,15 +1168,15 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
                                      const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_nodes,
                                      const int32_t* children, const int32_t* node_iy_off,
                                      const int32_t* node_iy_lab, int32_t n_sliced, const int32_t* sliced,
-                                     int32_t gemm_min, int32_t tile_bits, int32_t bulk, void** blob,
-                                     int64_t* blob_bytes, char* err, int32_t err_cap) {
+                                     int32_t gemm_min, int32_t tile_bits, void** blob, int64_t* blob_bytes,
+                                     char* err, int32_t err_cap) {
   PlanInput in;
   in.n_labels = n_labels; in.n_tensors = n_tensors; in.ix_off = ix_off; in.ix_lab = ix_lab;
   in.n_iy = n_iy; in.iy = iy; in.n_nodes = n_nodes; in.children = children;
   in.node_iy_off = node_iy_off; in.node_iy_lab = node_iy_lab; in.n_sliced = n_sliced; in.sliced = sliced;
   PlanHost h;
   std::string e = compile_plan(in, h, gemm_min);
-  if (e.empty() && (tile_bits != h.tile_bits || bulk)) e = retile_plan(h, tile_bits, bulk != 0);
+  if (e.empty() && tile_bits != h.tile_bits) e = retile_plan(h, tile_bits);
   if (!e.empty()) {
     if (err && err_cap > 0) {
       std::strncpy(err, e.c_str(), err_cap - 1);
@@ -1387,12 +1373,12 @@ extern "C" int32_t tbi_measure_maxplus_peak_i16(int32_t device, double* ops_per_
   return TB_OK;
 }
 
-// Re-tile a plan's stream steps (tile size, bulk-copy staging), as the
-// autotuner does; for tests that pin one configuration.
-extern "C" int32_t tbi_plan_retile(tb_plan* p, int32_t bits, int32_t bulk) {
+// Re-tile a plan's stream steps (tile size), as the autotuner does; for
+// tests that pin one configuration.
+extern "C" int32_t tbi_plan_retile(tb_plan* p, int32_t bits) {
   if (!p) return TB_ERR_INVALID;
   std::lock_guard<std::mutex> lk(p->ctx->mu);
-  std::string e = retile_plan(p->h, bits, bulk != 0);
+  std::string e = retile_plan(p->h, bits);
   if (!e.empty()) return fail(TB_ERR_INVALID, e);
   p->structure_uploaded = false;
   p->version = ++p->ctx->plan_counter;

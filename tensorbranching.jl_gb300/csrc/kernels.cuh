@@ -168,44 +168,6 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
-  asm volatile("mbarrier.inval.shared.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait on one phase of an mbarrier: false when the limit is reached.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < (1 << 22); i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
 // wait until at most n (0..7) committed groups are pending
 __device__ __forceinline__ void cp_async_wait_n(int n) {
   switch (n) {
@@ -243,28 +205,6 @@ __device__ __forceinline__ void issue_sub(T* __restrict__ dst, const T* __restri
   }
 }
 
-// Async copies of a short sub-tensor (<= 16 elements) into unswizzled
-// shared memory (the bulk-copy mode's form for a tiny operand).
-template <typename T>
-__device__ __forceinline__ void issue_sub_lin(T* __restrict__ dst, const T* __restrict__ src, int n, int p,
-                                              const int* __restrict__ hi) {
-  const int N = 1 << n;
-  if (p >= 2) {
-    const int lowmask = (1 << p) - 1;
-    for (int q = threadIdx.x; q < (N >> 2); q += kThreads) {
-      const int j = q << 2;
-      cp_async16(dst + j, src + ((j & lowmask) + hi[j >> p]));
-    }
-  } else if (p == 1) {
-    for (int q = threadIdx.x; q < (N >> 1); q += kThreads) {
-      const int j = q << 1;
-      cp_async8(dst + j, src + hi[j >> 1]);
-    }
-  } else {
-    for (int j = threadIdx.x; j < N; j += kThreads) cp_async4(dst + j, src + hi[j]);
-  }
-}
-
 // Per-CTA state of a run of stream tiles: shared-memory tables, the
 // thread's fixed indices and the copy / compute / store cursors.
 template <typename T>
@@ -288,12 +228,6 @@ struct StreamRun {
   int na, pa, nb, pb, pc;
   int nloop, ntr, lo_bits, split, opt;
   bool hasB, act;
-  // bulk mode: one bulk copy per contiguous run, an mbarrier per stage; a
-  // tiny operand (<= 16 elements) goes by per-thread async copies instead
-  bool bulk, ok, a_thr, b_thr;
-  uint64_t* full;
-  uint32_t phase;  // bit s: parity of the next wait on stage s
-  int* err;
   int cl, s;
   int iah[kMaxOpt], ibh[kMaxOpt];
   int64_t n_items;
@@ -306,24 +240,8 @@ struct StreamRun {
 
   __device__ __forceinline__ void issue() {
     T* dst = buf0 + ib * BUF;
-    if (bulk) {
-      if (threadIdx.x == 0) {
-        // the stage's last readers passed the barrier before this issue
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const int ra = a_thr ? 0 : 1 << pa, nra = a_thr ? 0 : 1 << (na - pa);
-        const int rb = (hasB && !b_thr) ? 1 << pb : 0, nrb = (hasB && !b_thr) ? 1 << (nb - pb) : 0;
-        mbar_expect_tx(&full[ib], (uint32_t)((ra * nra + rb * nrb) * sizeof(T)));
-        const T* a = A0 + (pa_g + pa_l);
-        for (int r = 0; r < nra; r++) bulk_g2s(dst + r * ra, a + ldA[r], ra * sizeof(T), &full[ib]);
-        const T* b = B0 + (pb_g + pb_l);
-        for (int r = 0; r < nrb; r++) bulk_g2s(dst + NA + r * rb, b + ldB[r], rb * sizeof(T), &full[ib]);
-      }
-      if (a_thr) issue_sub_lin<T>(dst, A0 + (pa_g + pa_l), na, pa, ldA);
-      if (b_thr) issue_sub_lin<T>(dst + NA, B0 + (pb_g + pb_l), nb, pb, ldB);
-    } else {
-      issue_sub<T>(dst, A0 + (pa_g + pa_l), na, pa, ldA);
-      if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), nb, pb, ldB);
-    }
+    issue_sub<T>(dst, A0 + (pa_g + pa_l), na, pa, ldA);
+    if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), nb, pb, ldB);
     ib = ib + 1 == S ? 0 : ib + 1;
     if (pr + 1 < nloop) {
       const int k = __ffs(~pr) - 1;
@@ -343,15 +261,7 @@ struct StreamRun {
   // item `issued` into the buffer freed by the item before the current one
   __device__ __forceinline__ void refill() {
     if (issued < n_items) issue();
-    if (!bulk || a_thr || b_thr) cp_async_commit();
-  }
-  // item `it` (in buffer cb) has landed for this thread
-  __device__ __forceinline__ void wait_item() {
-    if (!bulk || a_thr || b_thr) cp_async_wait_n(S - 2);
-    if (bulk) {
-      if (ok) ok = mbar_wait(&full[cb], (phase >> cb) & 1u);
-      phase ^= 1u << cb;
-    }
+    cp_async_commit();
   }
   __device__ __forceinline__ void store(const T* acc) {
     const int cmask = (1 << pc) - 1;
@@ -388,7 +298,7 @@ __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
   for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
   const int last = R.nloop - 1;
   for (int64_t it = 0; it < R.n_items; it++) {
-    R.wait_item();
+    cp_async_wait_n(R.S - 2);
     __syncthreads();
     R.refill();
     const T* As = R.buf0 + R.cb * R.BUF;
@@ -425,7 +335,7 @@ __device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
   const int step = 1 << R.split;
   const int last = R.nloop - 1;
   for (int64_t it = 0; it < R.n_items; it++) {
-    R.wait_item();
+    cp_async_wait_n(R.S - 2);
     __syncthreads();
     R.refill();
     const T* As = R.buf0 + R.cb * R.BUF;
@@ -476,6 +386,7 @@ __device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
 template <typename T>
 __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __restrict__ arena,
                              int* __restrict__ smem, int* err = nullptr) {
+  (void)err;  // the per-thread copy pipeline has no waits to bound
   const int t = threadIdx.x;
   __syncthreads();  // the previous user of this shared memory is done
   {
@@ -494,19 +405,6 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   R.nb = d.nb;
   R.pb = d.pb;
   R.pc = d.pc;
-  // bulk copies need a place to report a timed-out wait
-  const bool bulk = (d.copy_mode & 1) != 0 && err != nullptr;
-  R.bulk = bulk;
-  R.a_thr = bulk && (d.copy_mode & 2) != 0;
-  R.b_thr = bulk && (d.copy_mode & 4) != 0;
-  R.ok = true;
-  R.err = err;
-  R.phase = 0;
-  R.full = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(smem) + kDescBarOff);
-  if (bulk && t == 0) {
-    for (int i = 0; i < R.S; i++) mbar_init(&R.full[i], 1);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
   T* buf0 = reinterpret_cast<T*>(smem + kDescWords);
   R.buf0 = buf0;
   int* ldA = reinterpret_cast<int*>(buf0 + R.S * R.BUF);
@@ -548,8 +446,8 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
         if (d.tr_b[b] >= 0) xb |= 1 << d.tr_b[b];
       }
     }
-    IAr[j] = bulk ? xa : swz16(xa);
-    IBr[j] = bulk ? xb : swz16(xb);
+    IAr[j] = swz16(xa);
+    IBr[j] = swz16(xb);
   }
   if (t < 5 * kMaxBits) {
     const int which = t / kMaxBits, k = t % kMaxBits;
@@ -591,10 +489,8 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
       if (d.tc_b[b] >= 0) ibt |= 1 << d.tc_b[b];
     }
   }
-  if (!bulk) {
-    iat = swz16(iat);
-    ibt = swz16(ibt);
-  }
+  iat = swz16(iat);
+  ibt = swz16(ibt);
 #pragma unroll
   for (int i = 0; i < kMaxOpt; i++) {
     int xa = 0, xb = 0;
@@ -604,8 +500,8 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
         if (d.tc_b[b] >= 0) xb |= 1 << d.tc_b[b];
       }
     }
-    R.iah[i] = iat ^ (bulk ? xa : swz16(xa));
-    R.ibh[i] = ibt ^ (bulk ? xb : swz16(xb));
+    R.iah[i] = iat ^ swz16(xa);
+    R.ibh[i] = ibt ^ swz16(xb);
   }
   // absolute grid offsets of the first tile (32-bit within each tensor)
   int ga = 0, gb = 0, gc = 0;
@@ -653,23 +549,7 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   } else {
     stream_loop_any<T>(R);
   }
-  if (R.a_thr || R.b_thr) cp_async_wait<0>();
-  if (bulk) {
-    // every issued item was waited for; after a timed-out wait, the copies
-    // still in flight land (bounded) before the shared memory is reused
-    if (__syncthreads_or(!R.ok)) {
-      if (t == 0) {
-        atomicExch(err, 3 /* TB_ERR_TIMEOUT */);
-        // the last use of stage i completes the phase before its next wait
-        for (int i = 0; i < R.S; i++) mbar_wait(&R.full[i], ((R.phase >> i) & 1u) ^ 1u);
-      }
-      __syncthreads();
-    }
-    if (t == 0)
-      for (int i = 0; i < R.S; i++) mbar_inval(&R.full[i]);
-  } else {
-    cp_async_wait<0>();
-  }
+  cp_async_wait<0>();
 }
 
 // One tile (the launch-per-tile form used by the plain path's kernels).
@@ -939,6 +819,44 @@ __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T*
 // ---------------------------------------------------------------------------
 constexpr int kGemmStages = 3;
 constexpr int kGemmBK = 32;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on one phase of an mbarrier: false when the limit is reached.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 22); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
 
 template <int BM, int BN, int S = kGemmStages, int BK = kGemmBK, bool I16 = false>
 struct GemmSmem {

@@ -142,7 +142,7 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
   while ((1 << lt) < kThreads) lt++;
   d.split_log2 = d.n_tc >= lt ? 0 : std::min(lt - d.n_tc, d.n_tr);
   d.n_tiles = 1 << d.n_grid;
-  d.copy_mode = 0;
+  d.pad_ = 0;
   for (size_t i = 0; i < G.size(); i++) {
     d.g_pa[i] = (int8_t)index_of(A, G[i]);
     d.g_pb[i] = (int8_t)index_of(B, G[i]);
@@ -163,59 +163,7 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
     d.tr_a[i] = (int8_t)index_of(TA, Tr[i]);
     d.tr_b[i] = (int8_t)index_of(TB, Tr[i]);
   }
-  d.copy_mode = stream_copy_mode(d, Bp != nullptr);
   return "";
-}
-
-int stream_copy_mode(const TileDesc& d, bool hasB) {
-  // bulk copies: contiguous runs of >= 16 elements, at most 16 runs an
-  // operand; an operand of <= 16 elements may go by per-thread copies
-  // (bits 1 / 2 of the mode), but at least one operand goes by bulk copies
-  auto runs_ok = [](int n, int p) { return p >= 4 && n - p <= 4; };
-  const bool a_bulk = runs_ok(d.na, d.pa), b_bulk = hasB && runs_ok(d.nb, d.pb);
-  const bool a_tiny = d.na <= 4, b_tiny = hasB && d.nb <= 4;
-  if (!(a_bulk || a_tiny) || (hasB && !(b_bulk || b_tiny))) return 0;
-  if (!a_bulk && !b_bulk) return 0;
-  const int mode = 1 | (a_bulk ? 0 : 2) | (hasB && !b_bulk ? 4 : 0);
-  // ... and reads of the unswizzled tiles without worse than 2-way bank
-  // conflicts: the addresses one warp reads in one instruction (warp 0, as
-  // the kernel maps threads to outputs and reduction terms)
-  const int lo = d.n_tc < 8 ? d.n_tc : 8;
-  const int step = 1 << d.split_log2, ntr = 1 << d.n_tr, opt = 1 << (d.n_tc - lo);
-  const int active = 1 << (lo + d.split_log2);
-  for (int which = 0; which < (hasB ? 2 : 1); which++) {
-    const int8_t* tcx = which == 0 ? d.tc_a : d.tc_b;
-    const int8_t* trx = which == 0 ? d.tr_a : d.tr_b;
-    for (int i = 0; i < opt; i++) {
-      for (int k = 0; k * step < ntr; k++) {
-        int addr[32], n = 0;
-        for (int lane = 0; lane < 32 && lane < active; lane++) {
-          const int cl = lane & ((1 << lo) - 1), sidx = lane >> lo;
-          const int r = sidx + k * step;
-          if (r >= ntr) continue;
-          int x = 0;
-          for (int b = 0; b < d.n_tc; b++) {
-            const int bit = b < lo ? (cl >> b) & 1 : ((i << lo) >> b) & 1;
-            if (bit && tcx[b] >= 0) x |= 1 << tcx[b];
-          }
-          for (int b = 0; b < d.n_tr; b++)
-            if (((r >> b) & 1) && trx[b] >= 0) x |= 1 << trx[b];
-          addr[n++] = x;
-        }
-        for (int bank = 0; bank < 32; bank++) {
-          int distinct = 0;
-          for (int u = 0; u < n; u++) {
-            if ((addr[u] & 31) != bank) continue;
-            bool seen = false;
-            for (int v = 0; v < u; v++) seen = seen || addr[v] == addr[u];
-            distinct += !seen;
-          }
-          if (distinct > 2) return 0;
-        }
-      }
-    }
-  }
-  return mode;
 }
 
 bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
@@ -627,7 +575,6 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
         TileDesc d;
         if (!(e = plan_tile(pl, nullptr, p.flabels[me], part_off, -1, p.off[me], d, p.tile_bits)).empty())
           return "node " + std::to_string(j) + " (K parts): " + e;
-        if (!p.bulk_copies) d.copy_mode = 0;
         st.kind = STEP_TILE;
         st.desc = (int32_t)p.tiles.size();
         st.n_tiles = d.n_tiles;
@@ -651,7 +598,6 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
                           p.tile_bits))
                .empty())
         return "node " + std::to_string(j) + ": " + e;
-      if (!p.bulk_copies) d.copy_mode = 0;
       st.kind = STEP_TILE;
       st.desc = (int32_t)p.tiles.size();
       st.n_tiles = d.n_tiles;
@@ -705,9 +651,8 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
   return "";
 }
 
-std::string retile_plan(PlanHost& p, int bits, bool bulk) {
+std::string retile_plan(PlanHost& p, int bits) {
   if (bits < 8 || bits > 10) return "tile bits outside 8..10";
-  p.bulk_copies = bulk;
   const int T = p.n_tensors;
   if (p.n_nodes == 0) {
     p.tile_bits = bits;
@@ -733,7 +678,6 @@ std::string retile_plan(PlanHost& p, int bits, bool bulk) {
         e = plan_tile(pl, nullptr, p.flabels[me], p.split_off[j], -1, p.off[me], d, bits);
       }
       if (!e.empty()) return "step " + std::to_string(si) + ": " + e;
-      if (!bulk) d.copy_mode = 0;
       tiles[st.desc] = d;
       st.n_tiles = d.n_tiles;
     }

@@ -65,7 +65,6 @@ struct PlanHost {
   double tc = 0, sc = 0, rwc = 0, ops = 0, bytes = 0;
   int64_t total_tiles = 0;
   int32_t tile_bits = 9;                       // stream tiles grow to 2^tile_bits outputs
-  bool bulk_copies = false;                    // stream tiles may use bulk-copy staging (copy_mode)
   int32_t gemm_ctas = 304;                     // resident GEMM CTAs the K split balances for
   std::vector<int32_t> step_node;              // node a step contracts (-1: leaves, final); a split-K
                                                // reduce step holds -2 - node
@@ -75,13 +74,9 @@ struct PlanHost {
 // Compile; returns "" on success or an error message.
 std::string compile_plan(const PlanInput& in, PlanHost& out, int gemm_min_log2);
 
-// Copy mode of a planned stream tile (TileDesc::copy_mode).
-int stream_copy_mode(const TileDesc& d, bool hasB);
-
 // Re-plan every stream-tile step of the fused form with tiles of up to
-// 2^bits outputs (8..10), with or without bulk-copy staging where a tile
-// allows it; GEMM steps and the arena layout are unchanged.
-std::string retile_plan(PlanHost& p, int bits, bool bulk = false);
+// 2^bits outputs (8..10); GEMM steps and the arena layout are unchanged.
+std::string retile_plan(PlanHost& p, int bits);
 
 // Plan one stream tile for C = max_{R} A (+ B).  A, C (and B if non-null)
 // are label lists in their memory order.  Returns "" or an error.

@@ -35,9 +35,7 @@ struct TileDesc {
   int32_t pa, pb, pc;           // leading tile bits that are tensor positions 0..p-1
   int32_t split_log2;           // threads cooperating on one output (reduction split)
   int32_t n_tiles;              // CTAs = 2^n_grid
-  int32_t copy_mode;            // 0: per-thread 16/8/4-byte async copies into swizzled
-                                // shared memory; 1: one bulk copy per contiguous run
-                                // (runs of >= 16 elements), unswizzled
+  int32_t pad_;
   int8_t g_pa[kMaxBits], g_pb[kMaxBits], g_pc[kMaxBits];  // grid bit -> tensor position (-1)
   int8_t l_pa[kMaxBits], l_pb[kMaxBits];                  // loop bit -> tensor position (-1)
   int8_t ta_pos[kMaxTileBits], tb_pos[kMaxTileBits];      // tile bit -> tensor position
@@ -47,11 +45,8 @@ struct TileDesc {
 };
 // a TileDesc copied to the front of a stream tile's shared memory, padded
 // so the operand buffers after it start on a 16-byte boundary
-constexpr int kDescWords = 128;  // descriptor, then the bulk-copy mbarriers
-constexpr int kDescBarOff = 432;  // byte offset of the stages' mbarriers
-static_assert(sizeof(TileDesc) <= kDescBarOff && kDescBarOff + 8 * kMaxStages <= kDescWords * 4 &&
-                  kDescWords % 4 == 0,
-              "descriptor copy and mbarriers");
+constexpr int kDescWords = 108;
+static_assert(sizeof(TileDesc) <= kDescWords * 4 && kDescWords % 4 == 0, "descriptor copy");
 
 // Register-blocked GEMM for a contraction node with large M, N and K label
 // groups.  The plan compiler lays the operands out "k-pair interleaved":

@@ -171,8 +171,7 @@ class Engine:
         _native.check(st, self.ctx)
         names = {v: k for k, v in _native.MODES.items()}
         return {"mode": names[res.mode], "tile_bits": res.tile_bits, "ctas_per_sm": res.ctas_per_sm,
-                "chunk_div": res.chunk_div, "bulk_copies": bool(res.bulk_copies), "ms": res.ms,
-                "ms_default": res.ms_default, "n_tried": res.n_tried}
+                "chunk_div": res.chunk_div, "ms": res.ms, "ms_default": res.ms_default, "n_tried": res.n_tried}
 
     def solve_batch(self, plans, slice_vals=None, r=None, mode: str = "batched"):
         """Per-item results (max root + r) and their max."""

@@ -21,14 +21,14 @@ KMAXTILE = 16
 KTHREADS = 256
 KMAXOPT = 4
 KSMEM = 8192
-KDESCWORDS = 128  # descriptor copy (and the bulk-copy mbarriers) in front of the operand buffers
+KDESCWORDS = 108  # descriptor copy in front of the operand buffers
 
 
 class TileDesc(ctypes.Structure):
     _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64),
                 ("n_grid", c_int32), ("n_loop", c_int32), ("n_tc", c_int32), ("n_tr", c_int32),
                 ("na", c_int32), ("nb", c_int32), ("pa", c_int32), ("pb", c_int32), ("pc", c_int32),
-                ("split_log2", c_int32), ("n_tiles", c_int32), ("copy_mode", c_int32),
+                ("split_log2", c_int32), ("n_tiles", c_int32), ("pad_", c_int32),
                 ("g_pa", c_int8 * KMAXBITS), ("g_pb", c_int8 * KMAXBITS), ("g_pc", c_int8 * KMAXBITS),
                 ("l_pa", c_int8 * KMAXBITS), ("l_pb", c_int8 * KMAXBITS),
                 ("ta_pos", c_int8 * KMAXTILE), ("tb_pos", c_int8 * KMAXTILE), ("tc_pos", c_int8 * KMAXTILE),
@@ -74,11 +74,10 @@ def check_layout(lib):
     assert list(out)[:5] == want, (list(out), want)
 
 
-def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4, tile_bits=9, bulk=False):
+def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4, tile_bits=9):
     lib.tbi_plan_describe.restype = c_int32
     lib.tbi_plan_describe.argtypes = [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p,
-                                      c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_int32, c_int32,
-                                      ctypes.POINTER(c_void_p),
+                                      c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_int32, ctypes.POINTER(c_void_p),
                                       ctypes.POINTER(c_int64), ctypes.c_char_p, c_int32]
     lib.tbi_free.argtypes = [c_void_p]
     lib.tbi_sizes.argtypes = [c_void_p, c_int32]
@@ -95,7 +94,7 @@ def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4, tile_bits=9, b
                                iy.ctypes.data, code.n_nodes, ch.ctypes.data,
                                None if noff is None else noff.ctypes.data,
                                None if nlab is None else nlab.ctypes.data, len(sliced), sl.ctypes.data,
-                               gemm_min, tile_bits, int(bulk), ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
+                               gemm_min, tile_bits, ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
     if rc:
         raise ValueError(err.value.decode())
     raw = ctypes.string_at(blob, nbytes.value)
@@ -178,20 +177,8 @@ class Neg:
     f32 = np.float32(-np.inf)
 
 
-def emu_stream_tile(d, arena, written, expect=None, bulk_ok=False):
-    """Run every CTA of one stream-tile descriptor on the arena (in place).
-    bulk_ok: the launch may use the descriptor's bulk-copy mode (the fused
-    kernels; the plain path always uses per-thread copies)."""
-    bulk = bulk_ok and (d.copy_mode & 1) == 1
-    sw = (lambda j: j) if bulk else swz
-    thr = {0: bool(d.copy_mode & 2), 1: bool(d.copy_mode & 4)}  # operand by per-thread copies
-    if d.copy_mode:
-        hasB_ = d.b_off >= 0
-        for k, (n, p) in enumerate(((d.na, d.pa), (d.nb, d.pb))):
-            if k == 1 and not hasB_:
-                continue
-            assert (n <= 4) if thr[k] else (p >= 4 and n - p <= 4)
-        assert not thr[0] or not (hasB_ and thr[1]), "no operand by bulk copies"
+def emu_stream_tile(d, arena, written, expect=None):
+    """Run every CTA of one stream-tile descriptor on the arena (in place)."""
     hasB = d.b_off >= 0
     ra = tensor_rank(d.ta_pos[:d.na], d.g_pa[:d.n_grid], d.l_pa[:d.n_loop])
     rb = tensor_rank(d.tb_pos[:d.nb], d.g_pb[:d.n_grid], d.l_pb[:d.n_loop]) if hasB else 0
@@ -227,8 +214,8 @@ def emu_stream_tile(d, arena, written, expect=None, bulk_ok=False):
                     xa |= 1 << d.tr_a[b]
                 if d.tr_b[b] >= 0:
                     xb |= 1 << d.tr_b[b]
-        IAr[j] = sw(xa)
-        IBr[j] = sw(xb)
+        IAr[j] = swz(xa)
+        IBr[j] = swz(xb)
     lo_bits = min(d.n_tc, 8)
     split = d.split_log2
     active = 1 << (lo_bits + split)
@@ -246,8 +233,8 @@ def emu_stream_tile(d, arena, written, expect=None, bulk_ok=False):
                 out |= ((xbits >> b) & 1) << tab[b]
         return out
 
-    iat = sw(part(cl, d.tc_a))
-    ibt = sw(part(cl, d.tc_b))
+    iat = swz(part(cl, d.tc_a))
+    ibt = swz(part(cl, d.tc_b))
     neg = np.float32(-np.inf)
     for tile in range(d.n_tiles):
         oa, ob, oc = d.a_off, d.b_off, d.c_off
@@ -268,22 +255,14 @@ def emu_stream_tile(d, arena, written, expect=None, bulk_ok=False):
                     if d.l_pb[i] >= 0:
                         lb += 1 << d.l_pb[i]
 
-            def load(base, n, p, hi, lo, hi_b, region, opnd):
+            def load(base, n, p, hi, lo, hi_b, region):
                 j = np.arange(1 << n)
                 g = base + (j & ((1 << p) - 1)) + hi[j >> p]
                 assert g.min() >= lo and g.max() < hi_b, "global load out of bounds"
                 # async copies: 16 bytes when p >= 2, 8 when p == 1; both ends aligned
                 for b in range(stages(d)):  # every pipeline buffer
-                    dst = KDESCWORDS + b * buf_words(d) + region + sw(j)
-                    if bulk and not thr[opnd]:
-                        # one bulk copy per run of 2^p elements: 16-byte aligned ends, 16-byte multiple size
-                        runs = (1 << n) >> p
-                        starts = g[:: 1 << p]
-                        assert len(starts) == runs <= 16 and (1 << p) * 4 % 16 == 0
-                        assert np.all(starts % 4 == 0), "misaligned bulk-copy source"
-                        assert np.all(dst[:: 1 << p] % 4 == 0), "misaligned bulk-copy destination"
-                        assert np.all(np.diff(g.reshape(runs, -1), axis=1) == 1), "run not contiguous"
-                    elif p >= 2:
+                    dst = KDESCWORDS + b * buf_words(d) + region + swz(j)
+                    if p >= 2:
                         assert np.all(g[::4] % 4 == 0), "misaligned 16-byte global source"
                         assert np.all(dst[::4] % 4 == 0), "misaligned 16-byte shared destination"
                         assert np.all(np.diff(dst.reshape(-1, 4), axis=1) == 1), "16-byte chunk split by swizzle"
@@ -291,13 +270,13 @@ def emu_stream_tile(d, arena, written, expect=None, bulk_ok=False):
                         assert np.all(g[::2] % 2 == 0), "misaligned 8-byte global source"
                         assert np.all(dst[::2] % 2 == 0), "misaligned 8-byte shared destination"
                 sm = np.empty(1 << n, np.float32)
-                ph = sw(j)
+                ph = swz(j)
                 assert sorted(ph.tolist()) == list(range(1 << n))
                 sm[ph] = arena[g]
                 return sm
 
-            As = load(la, d.na, d.pa, ldA, a_lo, a_hi, 0, 0)
-            Bs = load(lb, d.nb, d.pb, ldB, b_lo, b_hi, a_words(d), 1) if hasB else None
+            As = load(la, d.na, d.pa, ldA, a_lo, a_hi, 0)
+            Bs = load(lb, d.nb, d.pb, ldB, b_lo, b_hi, a_words(d)) if hasB else None
             act_idx = np.nonzero(act)[0]
             step = 1 << split
             nq = ntr // step
@@ -311,8 +290,8 @@ def emu_stream_tile(d, arena, written, expect=None, bulk_ok=False):
                             xa |= 1 << d.tc_a[b]
                         if d.tc_b[b] >= 0:
                             xb |= 1 << d.tc_b[b]
-                ia = (iat ^ sw(xa))[act_idx]
-                ib = (ibt ^ sw(xb))[act_idx]
+                ia = (iat ^ swz(xa))[act_idx]
+                ib = (ibt ^ swz(xb))[act_idx]
                 idxa = ia[:, None] ^ IAr[rmat]
                 assert idxa.max() < NA and idxa.min() >= 0
                 v = As[idxa]
@@ -444,7 +423,7 @@ def run_fused(desc, weights, slice_vals=()):
                 # node j's operands are its children; ranks known from the blob
                 node_of_step[si] = j
                 j += 1
-            emu_stream_tile(d, arena, written, bulk_ok=True)
+            emu_stream_tile(d, arena, written)
         elif st.kind == STEP_GEMM:
             emu_gemm_step(desc["gemms"][st.desc], arena, written)
     fin = desc["fin"]

@@ -109,15 +109,12 @@ def test_gemm_steps(tb, orc, lib, shape):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("bits,bulk", [(8, False), (10, False), (9, True), (10, True)])
-def test_tile_sizes_of_the_autotuner(tb, orc, lib, bits, bulk):
-    """Every stream tile size tb_autotune may pick (tile_bits 8..10), with or
-    without bulk-copy staging, keeps every access in bounds and aligned and
-    every intermediate equal to the oracle's."""
+@pytest.mark.parametrize("bits", [8, 10])
+def test_tile_sizes_of_the_autotuner(tb, orc, lib, bits):
+    """Every stream tile size tb_autotune may pick (tile_bits 8..10) keeps
+    every access in bounds and every intermediate equal to the oracle's."""
     for g, w, code in (rr_case(tb, 60, 3), ksg_case(tb, 8, 2)):
-        D = emulate.describe(lib, code, tile_bits=bits, bulk=bulk)
-        if bulk:
-            assert any(D["tiles"][s.desc].copy_mode for s in D["steps"] if s.kind == emulate.STEP_TILE)
+        D = emulate.describe(lib, code, tile_bits=bits)
         root, nodes = emulate.run_fused(D, w, ())
         ref, dumps = orc.execute(code, w, dump=True)
         assert np.array_equal(root, ref)
