@@ -7,8 +7,8 @@ branching pipeline and the Python mirror of the reference API.
 """
 from .engine import Engine, Plan, default_engine
 from .graphs import Graph, random_ksg, random_regular_graph, random_weights
-from .mis import (ContractionTreeSlicer, KernelResult, contract_slices, dynamic_ob_mis, eincode2order,
-                  index_slices, kernelize, slice, solve_slice, update_code, update_order)
+from .mis import (LP_MWIS, ContractionTreeSlicer, KernelResult, contract_slices, dynamic_ob_mis, eincode2order,
+                  index_slices, kernelize, slice, slice_dfs_lp, solve_slice, update_code, update_order)
 from .network import (CompressedEinsum, MISProblem, SlicedBranch, UnitWeight, add_r, derive_node_labels,
                       rawcode)
 from .order import GreedyMethod, TreeSA, complexity, greedy_slice, initialize_code, order2eincode, peak_memory
@@ -17,7 +17,7 @@ from . import replicas, serving, slice_io
 __all__ = [
     "Engine", "Plan", "default_engine", "Graph", "random_ksg", "random_regular_graph", "random_weights",
     "ContractionTreeSlicer", "KernelResult", "contract_slices", "dynamic_ob_mis", "eincode2order",
-    "index_slices", "kernelize", "slice", "solve_slice", "update_code", "update_order", "CompressedEinsum", "MISProblem",
+    "index_slices", "kernelize", "slice", "slice_dfs_lp", "LP_MWIS", "solve_slice", "update_code", "update_order", "CompressedEinsum", "MISProblem",
     "SlicedBranch", "UnitWeight", "add_r", "derive_node_labels", "rawcode", "GreedyMethod", "TreeSA",
     "complexity", "greedy_slice", "initialize_code", "order2eincode", "peak_memory",
 ]

@@ -15,6 +15,7 @@ the MIS value of a branch set equals the MIS of the input graph.
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -206,6 +207,111 @@ def slice(p: MISProblem, code: CompressedEinsum, r: float, slicer: ContractionTr
         scs = [x.sc() for x in done]
         print(f"branches: {len(done)}, max sc: {max(scs) if scs else 0}")
     return done
+
+
+def _branch_once(b: SlicedBranch, slicer: ContractionTreeSlicer) -> list[SlicedBranch]:
+    """The two children of one branching step on b (v out, v in)."""
+    g = b.p.g
+    w = b.p.weight_array()
+    v = _branch_vertex(b.code, slicer.sc_target)
+    nbv = set(g.neighbors(v))
+    base = b.vmap if b.vmap is not None else list(range(g.n))
+    out = []
+    for child in (_make_branch(g, w, b.code, b.r, {v}, slicer),
+                  _make_branch(g, w, b.code, b.r + float(w[v]), nbv | {v}, slicer)):
+        child.vmap = [base[x] for x in child.vmap]
+        out.append(child)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# LP bound and the depth-first slicing loop with pruning
+# ---------------------------------------------------------------------------
+def LP_MWIS(g: Graph, weights) -> float:
+    """Upper bound on the weighted MIS: the LP relaxation with one
+    constraint x_u + x_v <= 1 per edge and x_a + x_b + x_c <= 1 per triangle,
+    0 <= x <= 1 (LP_MWIS, src/utils.jl:274-293), solved with scipy's HiGHS."""
+    from scipy.optimize import linprog
+    from scipy.sparse import coo_matrix
+
+    n = g.n
+    if n == 0:
+        return 0.0
+    w = weights_array(weights, n).astype(np.float64)
+    adj = g.adjacency()
+    rows, cols = [], []
+    k = 0
+    for u, v in g.edges:
+        if u == v:
+            rows.append(k); cols.append(u)
+        else:
+            rows += [k, k]; cols += [u, v]
+        k += 1
+    for u in range(n):
+        for v in adj[u]:
+            if v <= u:
+                continue
+            for x in adj[u] & adj[v]:
+                if x > v:
+                    rows += [k, k, k]; cols += [u, v, x]
+                    k += 1
+    if k == 0:
+        return float(np.sum(np.maximum(w, 0.0)))
+    A = coo_matrix((np.ones(len(rows)), (rows, cols)), shape=(k, n)).tocsr()
+    res = linprog(-w, A_ub=A, b_ub=np.ones(k), bounds=[(0.0, 1.0)] * n, method="highs")
+    if not res.success:
+        raise RuntimeError(f"LP_MWIS: {res.message}")
+    return float(-res.fun)
+
+
+def slice_dfs_lp(branch: SlicedBranch, slicer: ContractionTreeSlicer, dirname: str, element_type=np.float32,
+                 usecuda: bool = True, engine: Engine | None = None, solve=None, verbose: int = 0) -> dict:
+    """Branch until sc <= sc_target, solving each finished slice at once on
+    the GPU (plain single-slice path, solve_slice) to raise a primal bound;
+    children whose LP bound + r cannot beat the primal bound by 0.99 are
+    pruned, the rest are visited best LP bound first, and finished slices are
+    written to ``dirname`` in the reference's slice format with their
+    solutions (slice_dfs_lp / _slice_single, src/slice.jl:13-66,118-146).
+    The loop stops once a solution reaches the LP bound of the root.
+    ``solve(branch)`` replaces the GPU solve (the MIS of the branch without
+    r).  Returns the primal bound, the LP bound and the slice count."""
+    from . import slice_io
+
+    os.makedirs(dirname, exist_ok=True)
+    solve = solve or (lambda b: solve_slice(b, element_type, usecuda, engine, mode="plain"))
+    rows = []
+    lp_bound = LP_MWIS(branch.p.g, branch.p.weight_array()) + branch.r
+    primal = 0.0
+    unfinished = [branch]
+    next_id = 1
+    converged = False
+    while unfinished:
+        b = unfinished.pop()
+        sc = b.sc()
+        if b.code is None or sc <= slicer.sc_target:
+            value = b.r if b.code is None or b.p.g.n == 0 else solve(b) + b.r
+            rows.append((next_id, sc, b.tc(), b.r, value))
+            if b.code is not None:
+                slice_io.save_finished(dirname, b, next_id)
+            next_id += 1
+            primal = max(primal, float(value))
+            if verbose:
+                print(f"feasible solution {value}, primal bound {primal}")
+            if abs(value - lp_bound) < 1e-6:
+                converged = True
+                break
+            continue
+        kids = []
+        for c in _branch_once(b, slicer):
+            lp = LP_MWIS(c.p.g, c.p.weight_array()) + c.r if c.p.g.n else c.r
+            if lp >= primal + 0.99:
+                kids.append((lp, c))
+        kids.sort(key=lambda t: (-t[0], t[1].p.g.n))
+        # children go to the front of the list, which is consumed from its
+        # end (the visiting order of src/slice.jl:28-57)
+        unfinished[:0] = [c for _, c in kids]
+    slice_io.save_slices_csv(dirname, rows)
+    return {"primal": primal, "lp_bound": lp_bound, "slices": len(rows), "converged": converged}
 
 
 # ---------------------------------------------------------------------------

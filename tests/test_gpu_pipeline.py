@@ -51,3 +51,15 @@ def test_slices_from_disk_on_the_gpu(tb, exact, engine, tmp_path):
     back = sio.load_all_finished(str(tmp_path))
     res = tb.contract_slices(back, engine=engine, mode="batched")
     assert float(np.max(res)) == pytest.approx(exact.branch_and_bound(g.n, g.edges, w))
+
+
+def test_slice_dfs_lp_on_the_gpu(tb, exact, engine, tmp_path):
+    g = tb.random_regular_graph(80, 3, 6)
+    w = tb.random_weights(g.n, 6)
+    kr = tb.kernelize(g, w)
+    code = tb.initialize_code(kr.g, tb.GreedyMethod(6))
+    b = tb.SlicedBranch(tb.MISProblem(kr.g, kr.weights), code, kr.r)
+    res = tb.slice_dfs_lp(b, tb.ContractionTreeSlicer(sc_target=8, refine=False), str(tmp_path), engine=engine)
+    assert res["primal"] == pytest.approx(exact.branch_and_bound(g.n, g.edges, w))
+    back = tb.slice_io.load_all_finished(str(tmp_path))
+    assert len(back) == sum(1 for x in back)  # the directory reads back

@@ -59,3 +59,33 @@ def test_tree_variants_agree(tb, orc):
         c2 = tb.order2eincode(g, tb.eincode2order(code))
         c3 = tb.initialize_code(g, tb.TreeSA(ntrials=1, niters=5, betas=np.arange(1.0, 6.0), nthreads=1))
         assert orc.solve(c2, w) == ref and orc.solve(c3, w) == ref
+
+
+def test_lp_bound_is_an_upper_bound(tb, exact):
+    for seed in range(4):
+        g = tb.random_regular_graph(30, 3, seed)
+        w = tb.random_weights(g.n, seed)
+        lp = tb.LP_MWIS(g, w)
+        assert lp >= exact.branch_and_bound(g.n, g.edges, w) - 1e-6
+    g = tb.Graph(3, [(0, 1), (1, 2), (0, 2)])  # a triangle: the clique cut makes the LP exact
+    assert tb.LP_MWIS(g, np.ones(3, np.float32)) == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("seed", range(2))
+def test_slice_dfs_lp(tb, orc, exact, tmp_path, seed):
+    """Depth-first slicing with LP pruning (test/slice.jl:37-48): the best
+    solution written to slices.csv is the MIS."""
+    import csv
+
+    g = tb.random_regular_graph(50, 3, seed)
+    w = tb.random_weights(g.n, seed)
+    kr = tb.kernelize(g, w)
+    code = tb.initialize_code(kr.g, tb.GreedyMethod(seed))
+    b = tb.SlicedBranch(tb.MISProblem(kr.g, kr.weights), code, kr.r)
+    res = tb.slice_dfs_lp(b, tb.ContractionTreeSlicer(sc_target=6, refine=False), str(tmp_path),
+                          solve=lambda x: orc.solve(x.code, x.p.weight_array()))
+    want = exact.branch_and_bound(g.n, g.edges, w)
+    assert res["primal"] == pytest.approx(want)
+    with open(tmp_path / "slices.csv") as f:
+        sols = [float(r["solution"]) for r in csv.DictReader(f)]
+    assert max(sols) == pytest.approx(want) and len(sols) == res["slices"]
