@@ -182,6 +182,22 @@ tb_status tb_solve_batch(tb_ctx* ctx, int32_t n, tb_plan* const* plans, const in
                          const float* r, float* out_item, float* out_max, int32_t mode);
 
 /*
+ * Score n_trees contraction trees of one network on the device: for tree t
+ * (post-order pairs at children + t * 2 (n_tensors - 1)), out[4 t .. 4 t + 3]
+ * = log2 time complexity (sum over nodes of 2^|labels(left) u labels(right)|),
+ * space complexity (largest tensor rank), log2 read-write complexity and
+ * log2 peak live elements of a post-order evaluation (every leaf live at the
+ * start; each step allocates its output, then frees its operands).  Node
+ * output labels follow the tb_plan_create rule.  Up to 4096 labels.
+ * Replaces: contraction_complexity on candidate trees (src/types.jl:115-121,
+ * sc_score src/branch.jl:132-147) and contraction_peak_memory
+ * (src/utils.jl:197-219), evaluated one tree at a time on the host there.
+ */
+tb_status tb_score_trees(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const int32_t* ix_off,
+                         const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_trees,
+                         const int32_t* children, double* out);
+
+/*
  * Choose the stream tile size (tile_bits 8..10) and the executor schedule
  * (persistent launch with 1..2 CTAs per SM and three run lengths, or
  * per-level launches) for this batch by running it with each setting and

@@ -99,6 +99,8 @@ ENGINE_SIGNATURES = {
     "tb_solve_static": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
                                   c_void_p]),
     "tb_autotune": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, POINTER(TbTuneResult)]),
+    "tb_score_trees": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_int32,
+                                 c_void_p, c_void_p]),
     "tb_serve_start": (c_int32, [c_void_p, c_int64, c_int32]),
     "tb_serve_stop": (c_int32, [c_void_p]),
     "tb_submit": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, POINTER(c_void_p)]),

@@ -21,7 +21,8 @@ OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 ENGINE_SOURCES = ["engine.cu", "static_solve.cu", "plan.cpp", "kern_level_f32.cu", "kern_level_i32.cu",
-                  "kern_persist_f32.cu", "kern_persist_i32.cu", "kern_misc_f32.cu", "kern_misc_i32.cu"]
+                  "kern_persist_f32.cu", "kern_persist_i32.cu", "kern_misc_f32.cu", "kern_misc_i32.cu",
+                  "score.cu"]
 ENGINE_HEADERS = ["kernels.cuh", "device_kernels.cuh", "launch.h", "plan.h", "tb_internal.h"]
 ORDER_SOURCES = ["order.cpp"]
 

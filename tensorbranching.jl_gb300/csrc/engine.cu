@@ -938,6 +938,64 @@ tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   return TB_OK;
 }
 
+tb_status tb_score_trees(tb_ctx* c, int32_t n_labels, int32_t n_tensors, const int32_t* ix_off,
+                         const int32_t* ix_lab, int32_t n_iy, const int32_t* iy, int32_t n_trees,
+                         const int32_t* children, double* out) {
+  if (!c || !ix_off || !out || (n_trees > 0 && n_tensors > 1 && !children)) return fail(TB_ERR_INVALID, "null argument");
+  if (n_tensors < 1 || n_trees < 1) return fail(TB_ERR_INVALID, "no tensors or no trees");
+  if (n_labels < 1 || n_labels > 4096) return fail(TB_ERR_UNSUPPORTED, "tree scoring takes 1..4096 labels");
+  if (n_iy < 0 || (n_iy > 0 && !iy)) return fail(TB_ERR_INVALID, "bad iy");
+  const int T = n_tensors, nodes = T - 1, nn = 2 * T - 1, W = (n_labels + 31) / 32;
+  std::vector<uint32_t> leaf((size_t)T * W, 0), iyb(W, 0);
+  if (ix_off[0] != 0) return fail(TB_ERR_INVALID, "ix_off[0] must be 0");
+  for (int i = 0; i < T; i++) {
+    if (ix_off[i + 1] < ix_off[i]) return fail(TB_ERR_INVALID, "ix_off not monotone");
+    for (int k = ix_off[i]; k < ix_off[i + 1]; k++) {
+      const int l = ix_lab[k];
+      if (l < 0 || l >= n_labels) return fail(TB_ERR_INVALID, "label out of range");
+      leaf[(size_t)i * W + l / 32] |= 1u << (l % 32);
+    }
+  }
+  for (int k = 0; k < n_iy; k++) {
+    if (iy[k] < 0 || iy[k] >= n_labels) return fail(TB_ERR_INVALID, "open label out of range");
+    iyb[iy[k] / 32] |= 1u << (iy[k] % 32);
+  }
+  // every tree: post-order pairs over ids < T + j, each id used once
+  std::vector<char> used(nn);
+  for (int tr = 0; tr < n_trees; tr++) {
+    std::fill(used.begin(), used.end(), 0);
+    const int32_t* ch = children + (size_t)tr * 2 * nodes;
+    for (int j = 0; j < nodes; j++)
+      for (int q = 0; q < 2; q++) {
+        const int x = ch[2 * j + q];
+        if (x < 0 || x >= T + j || used[x]) return fail(TB_ERR_INVALID, "tree " + std::to_string(tr) + " is not a post-order binary tree");
+        used[x] = 1;
+      }
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  CU(cudaSetDevice(c->device));
+  int warps = std::min(n_trees, 16 * c->sms);
+  const size_t per_warp = (size_t)2 * nn * W + nn;
+  while (warps > 8 && (size_t)((warps + 7) / 8 * 8) * per_warp * 4 > ((size_t)1 << 30)) warps /= 2;
+  const size_t scratch_words = (size_t)((warps + 7) / 8 * 8) * per_warp;
+  DevBuf d_leaf, d_iy, d_ch, d_out, d_scr;
+  CU(d_leaf.ensure(leaf.size() * 4));
+  CU(d_iy.ensure(iyb.size() * 4 + 4));
+  CU(d_ch.ensure(std::max<size_t>((size_t)n_trees * 2 * nodes * 4, 4)));
+  CU(d_out.ensure((size_t)n_trees * 4 * sizeof(double)));
+  CU(d_scr.ensure(scratch_words * 4));
+  CU(cudaMemcpyAsync(d_leaf.p, leaf.data(), leaf.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaMemcpyAsync(d_iy.p, iyb.data(), iyb.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  if (nodes > 0)
+    CU(cudaMemcpyAsync(d_ch.p, children, (size_t)n_trees * 2 * nodes * 4, cudaMemcpyHostToDevice, c->stream));
+  CU(launch_score_trees(warps, c->stream, n_trees, T, W, reinterpret_cast<const uint32_t*>(d_leaf.p),
+                        reinterpret_cast<const uint32_t*>(d_iy.p), reinterpret_cast<const int32_t*>(d_ch.p),
+                        reinterpret_cast<uint32_t*>(d_scr.p), reinterpret_cast<double*>(d_out.p)));
+  CU(cudaMemcpyAsync(out, d_out.p, (size_t)n_trees * 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return TB_OK;
+}
+
 tb_status tb_plan_bind_mis_batch(int32_t n, tb_plan* const* plans, const float* weights, const int64_t* offsets) {
   if (n < 0 || (n > 0 && (!plans || !weights || !offsets))) return fail(TB_ERR_INVALID, "null argument");
   for (int32_t i = 0; i < n; i++) {

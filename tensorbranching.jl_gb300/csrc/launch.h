@@ -33,4 +33,9 @@ cudaError_t launch_persistent(unsigned ctas, int smem, cudaStream_t s, const Ite
 template <typename T>
 cudaError_t occupancy_persistent(int* per_sm, int smem);
 
+// Complexities and peak memory of many contraction trees of one network
+// (csrc/score.cu): one warp per tree.
+cudaError_t launch_score_trees(int warps, cudaStream_t s, int n_trees, int T, int W, const uint32_t* leaf_bits,
+                               const uint32_t* iy_bits, const int32_t* children, uint32_t* scratch, double* out);
+
 }  // namespace tb

@@ -161,6 +161,24 @@ class Engine:
         return {"stream_ctas": int(out[0]), "gemm_ctas": int(out[1]), "persistent_ctas": int(out[2]),
                 "sms": int(out[3])}
 
+    def score_trees(self, codes) -> np.ndarray:
+        """tb_score_trees: (tc, sc, rwc, log2 peak memory) of each tree; the
+        codes share leaves and open labels and differ in their trees."""
+        c0 = codes[0]
+        off, lab = c0.csr()
+        iy = np.array(c0.iy if c0.iy else [0], np.int32)
+        nodes = c0.n_tensors - 1
+        for c in codes:
+            if c.ixs != c0.ixs or c.iy != c0.iy:
+                raise ValueError("trees of one network only")
+        ch = np.ascontiguousarray(np.stack([c.children for c in codes]).reshape(-1) if nodes else
+                                  np.zeros(1, np.int32), dtype=np.int32)
+        out = np.zeros((len(codes), 4), np.float64)
+        st = self.lib.tb_score_trees(self.ctx, c0.n_labels, c0.n_tensors, off.ctypes.data, lab.ctypes.data,
+                                     len(c0.iy), iy.ctypes.data, len(codes), ch.ctypes.data, out.ctypes.data)
+        _native.check(st, self.ctx)
+        return out
+
     def autotune(self, plans, slice_vals=None, r=None) -> dict:
         """tb_autotune on this batch: tile size and schedule by timing; the
         choice serves later mode="auto" solves."""
