@@ -103,7 +103,7 @@ typedef struct tb_plan_stats {
 /* Result of tb_autotune: the chosen tile size and schedule. */
 typedef struct tb_tune_result {
   int32_t mode;        /* TB_MODE_BATCHED or TB_MODE_LAYERED */
-  int32_t tile_bits;   /* stream tiles of up to 2^tile_bits outputs (8..10) */
+  int32_t tile_bits;   /* stream tiles of up to 2^tile_bits outputs (8..11) */
   int32_t ctas_per_sm; /* resident CTAs per SM of the persistent executor */
   int32_t chunk_div;   /* runs of stream tiles hold >= 1/(chunk_div CTAs) of a level */
   double ms;           /* device time of the batch with the chosen settings */
@@ -198,7 +198,7 @@ tb_status tb_score_trees(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const
                          const int32_t* children, double* out);
 
 /*
- * Choose the stream tile size (tile_bits 8..10) and the executor schedule
+ * Choose the stream tile size (tile_bits 8..11) and the executor schedule
  * (persistent launch with 1..2 CTAs per SM and three run lengths, or
  * per-level launches) for this batch by running it with each setting and
  * keeping the fastest; the chosen tiles stay in the plans and the schedule in

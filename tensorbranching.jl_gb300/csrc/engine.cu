@@ -681,7 +681,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   // 1. stream tile size
   int best_bits = base_bits;
   double best = ms;
-  for (int bits = 8; bits <= 10; bits++) {
+  for (int bits = 8; bits <= 11; bits++) {
     if (bits == base_bits) continue;
     retile_all(c, uniq, bits, err);
     if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);

@@ -544,6 +544,8 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
       case 4 * 8 + 1: stream_loop_fixed<T, 4, 1>(R); break;
       case 4 * 8 + 2: stream_loop_fixed<T, 4, 2>(R); break;
       case 4 * 8 + 4: stream_loop_fixed<T, 4, 4>(R); break;
+      case 8 * 8 + 1: stream_loop_fixed<T, 8, 1>(R); break;
+      case 8 * 8 + 2: stream_loop_fixed<T, 8, 2>(R); break;
       default: stream_loop_any<T>(R); break;
     }
   } else {

@@ -67,7 +67,7 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
     while (pa < (int)A.size() && index_of(s, A[pa]) >= 0) pa++;
     while (pb < (int)B.size() && index_of(s, B[pb]) >= 0) pb++;
     while (pc < (int)C.size() && index_of(s, C[pc]) >= 0) pc++;
-    if (tc > 10 || tr > 8 || na > 13 || nb > 13) return false;
+    if (tc > std::max(10, out_bits_target) || tr > 8 || na > 13 || nb > 13) return false;
     if (na - pa > 9 || nb - pb > 9 || tc - pc > 9) return false;
     int64_t sm = (int64_t(1) << na) + (Bp ? (int64_t(1) << nb) : 0);
     return sm <= kSmemFloats;
@@ -107,7 +107,7 @@ std::string plan_tile(const std::vector<int32_t>& A, const std::vector<int32_t>*
       if (!inS(x)) { next = x; break; }
     if (next < 0) break;
     if (tc >= out_bits_target && grid <= 12) break;
-    if (tc >= 10) break;
+    if (tc >= std::max(10, out_bits_target)) break;
     auto s2 = with(S, next);
     if (!feasible(s2)) break;
     S = s2;
@@ -652,7 +652,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
 }
 
 std::string retile_plan(PlanHost& p, int bits) {
-  if (bits < 8 || bits > 10) return "tile bits outside 8..10";
+  if (bits < 8 || bits > 11) return "tile bits outside 8..11";
   const int T = p.n_tensors;
   if (p.n_nodes == 0) {
     p.tile_bits = bits;

@@ -75,7 +75,7 @@ struct PlanHost {
 std::string compile_plan(const PlanInput& in, PlanHost& out, int gemm_min_log2);
 
 // Re-plan every stream-tile step of the fused form with tiles of up to
-// 2^bits outputs (8..10); GEMM steps and the arena layout are unchanged.
+// 2^bits outputs (8..11); GEMM steps and the arena layout are unchanged.
 std::string retile_plan(PlanHost& p, int bits);
 
 // Plan one stream tile for C = max_{R} A (+ B).  A, C (and B if non-null)

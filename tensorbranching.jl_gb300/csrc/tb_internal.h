@@ -8,7 +8,7 @@ namespace tb {
 constexpr int kMaxTileBits = 16;  // labels inside one CTA tile (per tensor)
 constexpr int kMaxBits = 48;      // labels of one tensor / grid / loop
 constexpr int kThreads = 256;     // threads of every tile kernel
-constexpr int kMaxOpt = 4;        // outputs per thread in the stream tile
+constexpr int kMaxOpt = 8;        // outputs per thread in the stream tile
 constexpr int kSmemFloats = 8192; // stream tile staging (As + Bs), floats
 constexpr int kMaxStages = 8;     // stream tile pipeline depth (short operand tiles)
 

@@ -19,7 +19,7 @@ import numpy as np
 KMAXBITS = 48
 KMAXTILE = 16
 KTHREADS = 256
-KMAXOPT = 4
+KMAXOPT = 8
 KSMEM = 8192
 KDESCWORDS = 108  # descriptor copy in front of the operand buffers
 

@@ -109,9 +109,9 @@ def test_gemm_steps(tb, orc, lib, shape):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("bits", [8, 10])
+@pytest.mark.parametrize("bits", [8, 10, 11])
 def test_tile_sizes_of_the_autotuner(tb, orc, lib, bits):
-    """Every stream tile size tb_autotune may pick (tile_bits 8..10) keeps
+    """Every stream tile size tb_autotune may pick (tile_bits 8..11) keeps
     every access in bounds and every intermediate equal to the oracle's."""
     for g, w, code in (rr_case(tb, 60, 3), ksg_case(tb, 8, 2)):
         D = emulate.describe(lib, code, tile_bits=bits)

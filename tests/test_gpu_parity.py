@@ -173,7 +173,7 @@ def test_gemm_arithmetic_forms(tb, orc, engine, kind):
             assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode)
 
 
-@pytest.mark.parametrize("bits", [8, 10])
+@pytest.mark.parametrize("bits", [8, 10, 11])
 def test_stream_tile_configurations(tb, orc, engine, bits):
     """Every stream tile size the autotuner may choose gives the oracle's
     intermediates in the fused modes."""
