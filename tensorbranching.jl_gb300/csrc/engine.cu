@@ -678,32 +678,34 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
   res.ms_default = ms;
   res.n_tried++;
-  // 1. stream tile size
-  int best_bits = base_bits;
-  double best = ms;
+  // 1. stream tile size under both schedules (per-level launches and the
+  // persistent executor prefer different tile sizes)
+  int best_bits = base_bits, best_mode = TB_MODE_BATCHED, batched_bits = base_bits;
+  double best = ms, best_batched = ms;
   for (int bits = 8; bits <= 11; bits++) {
-    if (bits == base_bits) continue;
     retile_all(c, uniq, bits, err);
     if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
-    if ((st = time_batch(c, n, plans, sv, r, TB_MODE_BATCHED, ms))) return st;
-    res.n_tried++;
-    if (ms < best) {
-      best = ms;
-      best_bits = bits;
+    for (int mode : {TB_MODE_BATCHED, TB_MODE_LAYERED}) {
+      if (bits == base_bits && mode == TB_MODE_BATCHED) continue;  // timed above
+      if ((st = time_batch(c, n, plans, sv, r, mode, ms))) return st;
+      res.n_tried++;
+      if (ms < best) {
+        best = ms;
+        best_bits = bits;
+        best_mode = mode;
+      }
+      if (mode == TB_MODE_BATCHED && ms < best_batched) {
+        best_batched = ms;
+        batched_bits = bits;
+      }
     }
   }
-  retile_all(c, uniq, best_bits, err);
-  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
-  // 2. schedule: per-level launches, or the persistent executor with 1..max
-  // CTAs per SM and coarser or finer runs of stream tiles
-  int best_mode = TB_MODE_BATCHED, best_cps = c->ctas_per_sm_max, best_div = 4;
-  if ((st = time_batch(c, n, plans, sv, r, TB_MODE_LAYERED, ms))) return st;
-  res.n_tried++;
-  if (ms < best) {
-    best = ms;
-    best_mode = TB_MODE_LAYERED;
-  }
+  // 2. the persistent executor with 1..max CTAs per SM and coarser or finer
+  // runs of stream tiles, at its own best tile size
+  int best_cps = c->ctas_per_sm_max, best_div = 4;
   if (c->opt.persistent_ctas <= 0) {
+    retile_all(c, uniq, batched_bits, err);
+    if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
     for (int cps = 1; cps <= c->ctas_per_sm_max; cps++) {
       for (int div : {1, 4, 16}) {
         if (cps == c->ctas_per_sm_max && div == 4) continue;  // timed above
@@ -714,12 +716,15 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
         if (ms < best) {
           best = ms;
           best_mode = TB_MODE_BATCHED;
+          best_bits = batched_bits;
           best_cps = cps;
           best_div = div;
         }
       }
     }
   }
+  retile_all(c, uniq, best_bits, err);
+  if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : best_cps * c->sms;
   c->chunk_div = best_div;
   res.mode = best_mode;

@@ -494,10 +494,12 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
 #pragma unroll
   for (int i = 0; i < kMaxOpt; i++) {
     int xa = 0, xb = 0;
-    for (int b = R.lo_bits; b < d.n_tc; b++) {
-      if (((i << R.lo_bits) >> b) & 1) {
-        if (d.tc_a[b] >= 0) xa |= 1 << d.tc_a[b];
-        if (d.tc_b[b] >= 0) xb |= 1 << d.tc_b[b];
+    if (i < R.opt) {
+      for (int b = R.lo_bits; b < d.n_tc; b++) {
+        if (((i << R.lo_bits) >> b) & 1) {
+          if (d.tc_a[b] >= 0) xa |= 1 << d.tc_a[b];
+          if (d.tc_b[b] >= 0) xb |= 1 << d.tc_b[b];
+        }
       }
     }
     R.iah[i] = iat ^ swz16(xa);
