@@ -263,11 +263,12 @@ struct StreamRun {
     if (issued < n_items) issue();
     cp_async_commit();
   }
+  template <int N = kMaxOpt>
   __device__ __forceinline__ void store(const T* acc) {
     const int cmask = (1 << pc) - 1;
     T* Ct = C0 + oc;
 #pragma unroll
-    for (int i = 0; i < kMaxOpt; i++) {
+    for (int i = 0; i < N; i++) {
       if (i < opt) {
         const int c = cl + (i << lo_bits);
         Ct[(c & cmask) + stC[c >> pc]] = acc[i];
@@ -314,7 +315,7 @@ __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
       }
     }
     if (R.rl == last) {
-      if (R.act) R.store(acc);
+      if (R.act) R.template store<OPT>(acc);
 #pragma unroll
       for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
       R.next_tile();
@@ -326,12 +327,13 @@ __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
 }
 
 // Any shape: unary nodes, reduction splits, longer in-tile reductions.
-template <typename T>
+// MAXOPT bounds the outputs per thread (1 for tiles of <= 256 outputs).
+template <typename T, int MAXOPT>
 __device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
   const int t = threadIdx.x;
-  T acc[kMaxOpt];
+  T acc[MAXOPT];
 #pragma unroll
-  for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+  for (int i = 0; i < MAXOPT; i++) acc[i] = Trop<T>::neg();
   const int step = 1 << R.split;
   const int last = R.nloop - 1;
   for (int64_t it = 0; it < R.n_items; it++) {
@@ -343,7 +345,7 @@ __device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
     R.cb = R.cb + 1 == R.S ? 0 : R.cb + 1;
     if (R.act) {
 #pragma unroll
-      for (int i = 0; i < kMaxOpt; i++) {
+      for (int i = 0; i < MAXOPT; i++) {
         if (i < R.opt) {
           T a = acc[i];
           const int ia = R.iah[i], ib = R.ibh[i];
@@ -367,9 +369,9 @@ __device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
           acc[0] = a;
         }
       }
-      if (R.act && R.s == 0) R.store(acc);
+      if (R.act && R.s == 0) R.template store<MAXOPT>(acc);
 #pragma unroll
-      for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+      for (int i = 0; i < MAXOPT; i++) acc[i] = Trop<T>::neg();
       R.next_tile();
       R.rl = 0;
     } else {
@@ -548,10 +550,15 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
       case 4 * 8 + 4: stream_loop_fixed<T, 4, 4>(R); break;
       case 8 * 8 + 1: stream_loop_fixed<T, 8, 1>(R); break;
       case 8 * 8 + 2: stream_loop_fixed<T, 8, 2>(R); break;
-      default: stream_loop_any<T>(R); break;
+      default:
+        if (R.opt == 1) stream_loop_any<T, 1>(R);
+        else stream_loop_any<T, kMaxOpt>(R);
+        break;
     }
+  } else if (R.opt == 1) {
+    stream_loop_any<T, 1>(R);
   } else {
-    stream_loop_any<T>(R);
+    stream_loop_any<T, kMaxOpt>(R);
   }
   cp_async_wait<0>();
 }
