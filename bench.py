@@ -321,6 +321,8 @@ def main():
                     help="run only the first N branches / sliced items (small cases for ncu captures)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch kernels directly instead of replaying a CUDA graph")
+    ap.add_argument("--tile-bits", type=int, default=0,
+                    help="stream tiles of up to 2^N outputs (8..11) instead of the default / autotuned size")
     args = ap.parse_args()
 
     tb = _ge.load_package()
@@ -380,6 +382,9 @@ def main():
         wl["branches"] = [b for b in wl["branches"] if b.code is not None][: args.max_items]
     plans, svs, rs = make_items(eng, wl, tb, args.max_items)
     units = expected_answer(wl)
+    if args.tile_bits:
+        for p in {id(p): p for p in plans}.values():
+            eng.retile(p, args.tile_bits)
     st = plans[0].stats()
     uniq = {id(p): p for p in plans}
     ops = sum(uniq[k].stats()["ops"] for k in uniq) if not wl["sliced"] else st["ops"] * len(plans)

@@ -161,6 +161,14 @@ class Engine:
         return {"stream_ctas": int(out[0]), "gemm_ctas": int(out[1]), "persistent_ctas": int(out[2]),
                 "sms": int(out[3])}
 
+    def retile(self, plan: "Plan", bits: int) -> None:
+        """Re-plan a plan's stream tiles for up to 2^bits outputs (8..11), as
+        the autotuner does (tbi_plan_retile, an internal engine symbol)."""
+        f = self.lib.tbi_plan_retile
+        f.restype = c_int32
+        f.argtypes = [c_void_p, c_int32]
+        _native.check(f(plan.handle, int(bits)), self.ctx)
+
     def score_trees(self, codes) -> np.ndarray:
         """tb_score_trees: (tc, sc, rwc, log2 peak memory) of each tree; the
         codes share leaves and open labels and differ in their trees."""
