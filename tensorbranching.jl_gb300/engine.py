@@ -113,17 +113,17 @@ class Engine:
         else:
             flat = weights
             offs = offsets
-            if flat.dtype != np.float32 or not flat.flags.c_contiguous or offs.dtype != np.int64:
-                raise ValueError("flat weights must be contiguous float32 with int64 offsets")
-            for p, o in zip(plans, offs):
-                if o < 0 or o + p.code.n_labels > flat.shape[0]:
-                    raise ValueError("weights out of range")
+            if flat.dtype != np.float32 or not flat.flags.c_contiguous or offs.dtype != np.int64 or len(offs) != n:
+                raise ValueError("flat weights must be contiguous float32 with one int64 offset per plan")
         cached = getattr(self, "_bind_cache", None)
         if cached is not None and len(cached[0]) == n and all(a is b and a.handle for a, b in zip(cached[0], plans)):
-            arr = cached[1]
+            arr, n_labels = cached[1], cached[2]
         else:
             arr = (c_void_p * max(n, 1))(*[p.handle for p in plans])
-            self._bind_cache = (list(plans), arr)
+            n_labels = np.array([p.code.n_labels for p in plans], np.int64)
+            self._bind_cache = (list(plans), arr, n_labels)
+        if offsets is not None and n and (np.any(offs < 0) or np.any(offs + n_labels > flat.shape[0])):
+            raise ValueError("weights out of range")
         _native.check(self.lib.tb_plan_bind_mis_batch(n, ctypes.cast(arr, c_void_p), flat.ctypes.data,
                                                       offs.ctypes.data), self.ctx)
 
@@ -138,8 +138,7 @@ class Engine:
             arr = (c_void_p * n)(*[p.handle for p in plans])
             self._arr_cache = (list(plans), arr)
         sv = None
-        if slice_vals is not None and isinstance(slice_vals, (list, tuple)) and \
-                all(np.asarray(x).size == 0 for x in slice_vals):
+        if slice_vals is not None and isinstance(slice_vals, (list, tuple)) and all(len(x) == 0 for x in slice_vals):
             slice_vals = None
         if slice_vals is not None:
             sv = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int8).ravel() for x in slice_vals])
