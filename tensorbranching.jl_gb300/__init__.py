@@ -7,12 +7,13 @@ branching pipeline and the Python mirror of the reference API.
 """
 from .engine import Engine, Plan, default_engine
 from .graphs import Graph, random_ksg, random_regular_graph, random_weights
-from .mis import (LP_MWIS, ContractionTreeSlicer, KernelResult, contract_slices, dynamic_ob_mis, eincode2order,
-                  index_slices, kernelize, slice, slice_dfs_lp, solve_slice, update_code, update_order)
+from .branching import FixedPointBrancher, GreedyBrancher, IPSolver, ScoreRS
+from .mis import (LP_MWIS, ContractionTreeSlicer, KernelResult, VertexBrancher, contract_slices, dynamic_ob_mis,
+                  eincode2order, index_slices, kernelize, slice, slice_dfs_lp, solve_slice, update_code, update_order)
 from .network import (CompressedEinsum, MISProblem, SlicedBranch, UnitWeight, add_r, derive_node_labels,
                       rawcode)
 from .order import GreedyMethod, TreeSA, complexity, greedy_slice, initialize_code, order2eincode, peak_memory
-from . import replicas, serving, slice_io
+from . import branching, replicas, serving, slice_io
 
 __all__ = [
     "Engine", "Plan", "default_engine", "Graph", "random_ksg", "random_regular_graph", "random_weights",
@@ -20,4 +21,5 @@ __all__ = [
     "index_slices", "kernelize", "slice", "slice_dfs_lp", "LP_MWIS", "solve_slice", "update_code", "update_order", "CompressedEinsum", "MISProblem",
     "SlicedBranch", "UnitWeight", "add_r", "derive_node_labels", "rawcode", "GreedyMethod", "TreeSA",
     "complexity", "greedy_slice", "initialize_code", "order2eincode", "peak_memory",
+    "ScoreRS", "GreedyBrancher", "FixedPointBrancher", "IPSolver", "VertexBrancher",
 ]

@@ -9,9 +9,10 @@
   ContractionTreeSlicer src/types.jl:43-49
 
 The contraction itself always runs on the GPU through include/tb.h.  The
-reductions and the branching rule are our own simplifications of the
-reference's (which live in OptimalBranchingMIS): every rule used is exact, so
-the MIS value of a branch set equals the MIS of the input graph.
+reductions are our own simplification of the reference's (which live in
+OptimalBranchingMIS); the branching rule is the reference's optimal branching
+(``branching``) or a plain vertex rule.  Every rule used is exact, so the MIS
+value of a branch set equals the MIS of the input graph.
 """
 from __future__ import annotations
 
@@ -20,6 +21,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import branching as _br
 from . import order as _order
 from .engine import Engine, Plan
 from .graphs import Graph
@@ -102,9 +104,19 @@ def kernelize(g: Graph, weights=None, verbose: int = 0, rules=REDUCTIONS_ALL) ->
 # slicing by branching (ContractionTreeSlicer)
 # ---------------------------------------------------------------------------
 @dataclass
+class VertexBrancher:
+    """Two-way branching on the vertex that appears in the most large
+    tensors (weighted by 2^(size - sc_target)): v out, or v in with its
+    neighbours out."""
+
+
+@dataclass
 class ContractionTreeSlicer:
-    """Branch on vertices of the largest tensors until every branch has
-    sc <= sc_target (ContractionTreeSlicer, src/types.jl:43-49)."""
+    """Branch until every branch has sc <= sc_target (ContractionTreeSlicer,
+    src/types.jl:43-49).  The default rule is the reference's: a region
+    chosen by ``region_selector`` and the clause set chosen by ``brancher``
+    (``branching.GreedyBrancher`` / ``branching.FixedPointBrancher``);
+    ``VertexBrancher()`` selects the plain two-way vertex rule."""
 
     sc_target: int = 30
     refine: bool = True
@@ -112,6 +124,8 @@ class ContractionTreeSlicer:
         betas=np.arange(1.0, 16.0, 1.0), ntrials=2, niters=30, nthreads=1))
     max_branches: int = 1 << 16
     reductions: tuple = REDUCTIONS_ALL
+    region_selector: _br.ScoreRS = field(default_factory=_br.ScoreRS)
+    brancher: object = field(default_factory=_br.GreedyBrancher)
 
 
 def eincode2order(code: CompressedEinsum) -> list[int]:
@@ -181,8 +195,8 @@ def _make_branch(g: Graph, w: np.ndarray, code: CompressedEinsum, r: float, remo
 def slice(p: MISProblem, code: CompressedEinsum, r: float, slicer: ContractionTreeSlicer,
           verbose: int = 0) -> list[SlicedBranch]:
     """Branch until every branch has sc <= sc_target (slice / slice_bfs,
-    src/slice.jl:4-11,68-90).  Branch rule on vertex v: v out (drop v) or v
-    in (drop N[v], r += w_v); both followed by kernelization."""
+    src/slice.jl:4-11,68-90), each step by the slicer's rule (``_branch_once``);
+    every child is kernelized and re-ordered."""
     root = SlicedBranch(p, code, r)
     if code is None or code.complexity()[1] <= slicer.sc_target:
         return [root]
@@ -194,15 +208,7 @@ def slice(p: MISProblem, code: CompressedEinsum, r: float, slicer: ContractionTr
             continue
         if len(done) + len(todo) > slicer.max_branches:
             raise RuntimeError("branching exceeded max_branches")
-        g = b.p.g
-        w = b.p.weight_array()
-        v = _branch_vertex(b.code, slicer.sc_target)
-        nbv = set(g.neighbors(v))
-        base = b.vmap if b.vmap is not None else list(range(g.n))
-        for child in (_make_branch(g, w, b.code, b.r, {v}, slicer),
-                      _make_branch(g, w, b.code, b.r + float(w[v]), nbv | {v}, slicer)):
-            child.vmap = [base[x] for x in child.vmap]  # relative to the graph slice() was given
-            todo.append(child)
+        todo.extend(_branch_once(b, slicer))
     if verbose:
         scs = [x.sc() for x in done]
         print(f"branches: {len(done)}, max sc: {max(scs) if scs else 0}")
@@ -210,18 +216,21 @@ def slice(p: MISProblem, code: CompressedEinsum, r: float, slicer: ContractionTr
 
 
 def _branch_once(b: SlicedBranch, slicer: ContractionTreeSlicer) -> list[SlicedBranch]:
-    """The two children of one branching step on b (v out, v in)."""
+    """The children of one branching step on b under the slicer's rule, with
+    ``vmap`` relative to the graph the branching started from."""
     g = b.p.g
-    w = b.p.weight_array()
-    v = _branch_vertex(b.code, slicer.sc_target)
-    nbv = set(g.neighbors(v))
+    if isinstance(slicer.brancher, VertexBrancher):
+        w = b.p.weight_array()
+        v = _branch_vertex(b.code, slicer.sc_target)
+        nbv = set(g.neighbors(v))
+        kids = [_make_branch(g, w, b.code, b.r, {v}, slicer),
+                _make_branch(g, w, b.code, b.r + float(w[v]), nbv | {v}, slicer)]
+    else:
+        kids = _br.branch_step(b, slicer)
     base = b.vmap if b.vmap is not None else list(range(g.n))
-    out = []
-    for child in (_make_branch(g, w, b.code, b.r, {v}, slicer),
-                  _make_branch(g, w, b.code, b.r + float(w[v]), nbv | {v}, slicer)):
+    for child in kids:
         child.vmap = [base[x] for x in child.vmap]
-        out.append(child)
-    return out
+    return kids
 
 
 # ---------------------------------------------------------------------------

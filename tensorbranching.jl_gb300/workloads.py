@@ -4,8 +4,11 @@ Each workload follows one configuration of the benchmark plan:
 
   rr100_b10   random 3-regular n=100, unit weights, kernelize + branch until
               sc <= 10 (dynamic_ob_mis with ContractionTreeSlicer(sc_target=10),
-              test/dynamic_ob.jl:10-26); 32 graphs (seeds 1..32), every branch
-              of every graph in one batch
+              test/dynamic_ob.jl:10-26) by the two-way vertex rule; 32 graphs
+              (seeds 1..32), every branch of every graph in one batch
+  rr100_ob10  the same 32 graphs branched by the reference's default rule
+              (ScoreRS + GreedyBrancher, src/types.jl:43-49): fewer, larger
+              branches
   rr220       random 3-regular n=220, unit weights, one contraction, no slicing
   rr220w_s22  the rr220 graph and tree with integer weights U{1..10}; index
               slicing until every slice has sc <= 22; 2^k slices (the sliced
@@ -38,6 +41,8 @@ DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
 WORKLOADS = {
     "rr100_b10": "32 random 3-regular graphs n=100 (seeds 1..32), unit weights, branched to sc<=10",
+    "rr100_ob10": "32 random 3-regular graphs n=100 (seeds 1..32), unit weights, branched to sc<=10 by the "
+                  "optimal branching rule (ScoreRS sc_score regions, GreedyBrancher)",
     "rr220": "random 3-regular n=220 (seed 1), unit weights, one contraction, no slicing",
     "rr220w_s22": "random 3-regular n=220 (seed 1), weights U{1..10} (seed 1), rr220's tree index-sliced to sc<=22",
     "ksg32_b20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, isolated/pendant reductions, "
@@ -132,16 +137,18 @@ def _unpack_branches(kernel_g: Graph, kernel_w: np.ndarray, d) -> list[SlicedBra
     return out
 
 
-def _branch_set(g: Graph, w, sc_target: int, seed: int, init_niters: int, reductions):
+def _branch_set(g: Graph, w, sc_target: int, seed: int, init_niters: int, reductions, brancher=None):
     """Kernelize, anneal briefly, branch without re-annealing (so every tree
-    is determined by its elimination order)."""
+    is determined by its elimination order); the vertex rule unless
+    ``brancher`` is given."""
     kr = _mis.kernelize(g, w, rules=reductions)
     if kr.g.n == 0:
         return kr, [SlicedBranch(MISProblem(kr.g, kr.weights), None, kr.r, vmap=[])]
     code = _order.initialize_code(kr.g, _order.GreedyMethod(seed))
     code = _order.treesa(code, _order.TreeSA(sc_target=sc_target, betas=np.arange(1.0, 15.0, 1.0), ntrials=2,
                                              niters=init_niters, seed=seed))
-    slicer = _mis.ContractionTreeSlicer(sc_target=sc_target, refine=False, reductions=reductions)
+    slicer = _mis.ContractionTreeSlicer(sc_target=sc_target, refine=False, reductions=reductions,
+                                        brancher=brancher or _mis.VertexBrancher())
     brs = _mis.slice(MISProblem(kr.g, kr.weights), code, kr.r, slicer)
     if len(brs) == 1 and brs[0].vmap is None:
         # no branching needed: the root tree is the annealed one; store its order
@@ -152,14 +159,20 @@ def _branch_set(g: Graph, w, sc_target: int, seed: int, init_niters: int, reduct
     return kr, brs
 
 
-def build_rr100_b10() -> dict:
+def build_rr100_b10(brancher=None) -> dict:
     graphs = {}
     for s in range(1, 33):
         g = random_regular_graph(100, 3, s)
-        kr, brs = _branch_set(g, np.ones(100, np.float32), 10, s, 20, _mis.REDUCTIONS_ALL)
+        kr, brs = _branch_set(g, np.ones(100, np.float32), 10, s, 20, _mis.REDUCTIONS_ALL, brancher)
         for k, v in _pack_branches(brs).items():
             graphs[f"g{s}_{k}"] = v
     return graphs
+
+
+def build_rr100_ob10() -> dict:
+    from .branching import GreedyBrancher
+
+    return build_rr100_b10(GreedyBrancher())
 
 
 def build_ksg32_b20() -> dict:
@@ -172,10 +185,11 @@ def build_ksg32_b20() -> dict:
 
 
 BUILDERS = {"rr220": build_rr220, "rr220w_s22": build_rr220w_s22, "rr100_b10": build_rr100_b10,
-            "ksg32_b20": build_ksg32_b20}
+            "rr100_ob10": build_rr100_ob10, "ksg32_b20": build_ksg32_b20}
 
 
-NPZ = {"rr100_b10", "ksg32_b20"}
+NPZ = {"rr100_b10", "rr100_ob10", "ksg32_b20"}
+MULTI = {"rr100_b10", "rr100_ob10"}  # 32 graphs per step
 
 
 def path(name: str) -> str:
@@ -294,7 +308,7 @@ def load(name: str) -> dict:
         b = SlicedBranch(MISProblem(g, w), code, 0.0)
         return {"name": name, "graph": g, "branches": [b], "sliced": list(d["sliced"]), "slice_values": None,
                 "open_bits": 0}
-    if name == "rr100_b10":
+    if name in MULTI:
         brs, gs = [], []
         for s in range(1, 33):
             g = random_regular_graph(100, 3, s)

@@ -22,6 +22,23 @@ def test_dynamic_ob_mis(tb, exact, engine, seed, mode):
     assert got == pytest.approx(exact.branch_and_bound(g.n, g.edges, w))
 
 
+@pytest.mark.parametrize("brancher", ["greedy", "fixed_point", "vertex"])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_dynamic_ob_mis_branchers(tb, orc, engine, brancher, weighted):
+    """The brancher grid of test/dynamic_ob.jl:10-26 (sc_target=10): the
+    reference's optimal branching with either brancher, and the vertex rule;
+    every branch set is contracted in one batch on the GPU and the answer is
+    the full network's (the oracle's contraction of the unbranched graph, as
+    the reference test compares with the full solve)."""
+    seed = 11 if weighted else 12
+    g = tb.random_regular_graph(80, 3, seed)
+    w = tb.random_weights(g.n, seed) if weighted else np.ones(g.n, np.float32)
+    b = {"greedy": tb.GreedyBrancher(), "fixed_point": tb.FixedPointBrancher(), "vertex": tb.VertexBrancher()}[brancher]
+    slicer = tb.ContractionTreeSlicer(sc_target=10, refine=False, brancher=b)
+    got = tb.dynamic_ob_mis(g, w, slicer=slicer, engine=engine, mode="auto")
+    assert got == orc.solve(tb.initialize_code(g, tb.GreedyMethod(seed)), w)
+
+
 def test_golden_cases_in_one_batch(tb, engine):
     cases = json.load(open(os.path.join(HERE, "golden", "mis_known.json")))["cases"]
     plans, want = [], []
