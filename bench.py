@@ -310,7 +310,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="rr220")
-    ap.add_argument("--mode", default="auto", choices=["auto", "batched", "layered", "plain"],
+    ap.add_argument("--mode", default="auto", choices=["auto", "batched", "layered", "plain", "fused"],
                     help="auto: tb_autotune picks tile size and schedule before the warm-up (untimed)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

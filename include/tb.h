@@ -71,6 +71,12 @@ typedef int32_t tb_status;
 #define TB_MODE_AUTO 3    /* the schedule tb_autotune chose for this context
                              (tuned on first use when tb_options.autotune is 1;
                              TB_MODE_BATCHED before any tuning) */
+#define TB_MODE_FUSED 4   /* one warp per item contracts the whole network in
+                             shared memory, one launch for the batch; every
+                             plan must have the small form (tensors of at most
+                             2^13 entries, at most 48 KiB live per network,
+                             tb_plan_stats.small_words > 0), else
+                             TB_ERR_UNSUPPORTED */
 
 typedef struct tb_ctx tb_ctx;
 typedef struct tb_plan tb_plan;
@@ -97,12 +103,13 @@ typedef struct tb_plan_stats {
   int32_t n_open;         /* labels left open in the root tensor */
   int32_t n_sliced;       /* labels fixed per item by tb_solve_batch */
   int32_t n_tiles;        /* CTA tiles of one item in the fused form */
-  int32_t reserved[7];
+  int32_t small_words;    /* shared-memory words of the TB_MODE_FUSED form (0: none) */
+  int32_t reserved[6];
 } tb_plan_stats;
 
 /* Result of tb_autotune: the chosen tile size and schedule. */
 typedef struct tb_tune_result {
-  int32_t mode;        /* TB_MODE_BATCHED or TB_MODE_LAYERED */
+  int32_t mode;        /* TB_MODE_BATCHED, TB_MODE_LAYERED or TB_MODE_FUSED */
   int32_t tile_bits;   /* stream tiles of up to 2^tile_bits outputs (8..11) */
   int32_t ctas_per_sm; /* resident CTAs per SM of the persistent executor */
   int32_t chunk_div;   /* runs of stream tiles hold >= 1/(chunk_div CTAs) of a level */

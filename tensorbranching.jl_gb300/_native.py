@@ -24,8 +24,10 @@ TB_MODE_PLAIN = 0
 TB_MODE_BATCHED = 1
 TB_MODE_LAYERED = 2
 TB_MODE_AUTO = 3
+TB_MODE_FUSED = 4
 
-MODES = {"plain": TB_MODE_PLAIN, "batched": TB_MODE_BATCHED, "layered": TB_MODE_LAYERED, "auto": TB_MODE_AUTO}
+MODES = {"plain": TB_MODE_PLAIN, "batched": TB_MODE_BATCHED, "layered": TB_MODE_LAYERED, "auto": TB_MODE_AUTO,
+         "fused": TB_MODE_FUSED}
 
 
 class TbOptions(ctypes.Structure):
@@ -53,7 +55,8 @@ class TbPlanStats(ctypes.Structure):
         ("n_open", c_int32),
         ("n_sliced", c_int32),
         ("n_tiles", c_int32),
-        ("reserved", c_int32 * 7),
+        ("small_words", c_int32),
+        ("reserved", c_int32 * 6),
     ]
 
 

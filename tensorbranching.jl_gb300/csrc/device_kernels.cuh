@@ -147,6 +147,85 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
   }
 }
 
+// Fused small form: block b (one warp) contracts item b's whole network in
+// shared memory (leaves, every node in post-order, the root max) and writes
+// one value.  Node j: lane l computes outputs o = l, l + 32, ...; the
+// addresses of A and B follow from the bits of o (and of the reduced index
+// k) through the node's 4-bit label positions.
+__device__ __forceinline__ int small_stride(uint32_t p0, uint32_t p1, int i) {
+  const uint32_t q = ((i < 8 ? p0 : p1) >> (4 * (i & 7))) & 15u;
+  return (int)((1u << q) & 0x7fffu);  // position 15: not in this operand
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, int n_items, float* out_item,
+                                              const float* r) {
+  extern __shared__ int tb_smem[];
+  T* sm = reinterpret_cast<T*>(tb_smem);
+  const int lane = threadIdx.x;
+  const int item = blockIdx.x;
+  if (item >= n_items) return;
+  const ItemDev<T>& it = items[item];
+  for (int i = lane; i < it.n_leaves; i += 32) {
+    const LeafDesc ld = it.leaves[i];
+    const T w = Trop<T>::from_w(it.w && ld.label >= 0 ? it.w[ld.label] : ld.w);
+    T* dst = sm + it.small_leaf[i];
+    for (int e = 0; e < (1 << ld.n_out); e++) {
+      T best = Trop<T>::neg();
+      for (int raw = 0; raw < (1 << ld.nraw); raw++) {
+        bool ok = true;
+        for (int k = 0; k < ld.nraw; k++) {
+          const int x = (raw >> k) & 1;
+          if (ld.slice_idx[k] >= 0) {
+            if (x != (int)it.slice_vals[ld.slice_idx[k]]) ok = false;
+          } else if (((e >> ld.out_bit[k]) & 1) != x) {
+            ok = false;
+          }
+        }
+        if (!ok) continue;
+        const T v = ld.nraw == 1 ? ((raw & 1) ? w : T(0)) : (raw == 3 ? Trop<T>::neg() : T(0));
+        best = Trop<T>::mx(best, v);
+      }
+      dst[e] = best;
+    }
+  }
+  __syncwarp();
+  for (int j = 0; j < it.n_small; j++) {
+    const SmallNode nd = it.small[j];
+    const int nc = nd.nc_nk & 0xff, nk = (nd.nc_nk >> 8) & 0xff;
+    const T* A = sm + nd.a_off;
+    const T* B = sm + nd.b_off;
+    T* C = sm + nd.c_off;
+    for (int o = lane; o < (1 << nc); o += 32) {
+      int ao = 0, bo = 0;
+      for (int i = 0; i < nc; i++) {
+        if ((o >> i) & 1) {
+          ao += small_stride(nd.pa[0], nd.pa[1], i);
+          bo += small_stride(nd.pb[0], nd.pb[1], i);
+        }
+      }
+      T acc = Trop<T>::neg();
+      for (int k = 0; k < (1 << nk); k++) {
+        int ak = ao, bk = bo;
+        for (int i = 0; i < nk; i++) {
+          if ((k >> i) & 1) {
+            ak += small_stride(nd.pa[0], nd.pa[1], nc + i);
+            bk += small_stride(nd.pb[0], nd.pb[1], nc + i);
+          }
+        }
+        acc = Trop<T>::mac(acc, A[ak], B[bk]);
+      }
+      C[o] = acc;
+    }
+    __syncwarp();
+  }
+  T m = Trop<T>::neg();
+  for (int i = lane; i < (1 << it.small_root_log2); i += 32) m = Trop<T>::mx(m, sm[it.small_root + i]);
+  float v = Trop<T>::to_f(m);
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) out_item[item] = v + (r ? r[item] : 0.0f);
+}
+
 template <typename T, int BM, int BN>
 inline cudaError_t launch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
                              cudaStream_t s) {
@@ -182,6 +261,13 @@ inline cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t 
 // ---------------------------------------------------------------------------
 // launch wrappers (declared in launch.h)
 // ---------------------------------------------------------------------------
+template <typename T>
+cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, int n, float* out_item,
+                         const float* r) {
+  k_small<T><<<grid, 32, smem, s>>>(items, n, out_item, r);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_leaves(unsigned grid, cudaStream_t s, const LeafDesc* leaves, int n, const int8_t* sv, T* arena,
                           const float* w) {

@@ -89,7 +89,7 @@ struct tb_plan {
   tb_ctx* ctx = nullptr;
   PlanHost h;
   std::vector<float> weights;  // bound vertex weights by label
-  DevBuf d_steps, d_tiles, d_gemms, d_leaves;
+  DevBuf d_steps, d_tiles, d_gemms, d_leaves, d_small, d_small_leaf;
   bool structure_uploaded = false;
   bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
   bool i16_ok = false;         // bound weights are integers >= 0 summing below 8192
@@ -117,6 +117,8 @@ struct tb_ctx {
   int persistent_ctas = 0;
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
+  int small_smem = 0;   // shared bytes per item of the fused small form (this batch)
+  int tune_fallback = TB_MODE_BATCHED;  // tuned mode for batches the fused form cannot run
   size_t budget = 0;
   DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals, wvals;
   HostBuf h_items, h_groups, h_chunks, h_in, h_out;
@@ -203,12 +205,16 @@ static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
   if (p->leaves_dirty || !p->structure_uploaded)
     for (int i : p->vertex_leaves) h.leaves[i].w = p->weights[h.leaves[i].label];
   if (!p->structure_uploaded) {
-    void* before[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
+    void* before[6] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p};
     CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
     CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
     CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
     CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
-    void* after[4] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p};
+    if (h.small_ok) {
+      CU(up(p->d_small, h.small.empty() ? nullptr : h.small.data(), h.small.size() * sizeof(SmallNode)));
+      CU(up(p->d_small_leaf, h.small_leaf.data(), h.small_leaf.size() * sizeof(int32_t)));
+    }
+    void* after[6] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p};
     // captured graphs hold these device pointers: a move invalidates them
     if (std::memcmp(before, after, sizeof(before)) != 0) p->version = ++p->ctx->plan_counter;
     p->structure_uploaded = true;
@@ -287,6 +293,14 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     it.done_base = done_base;
     it.n_steps = (int)p->h.steps.size();
     it.fin = p->h.fin;
+    if (p->h.small_ok) {
+      it.small = reinterpret_cast<const SmallNode*>(p->d_small.p);
+      it.small_leaf = reinterpret_cast<const int32_t*>(p->d_small_leaf.p);
+      it.n_small = (int32_t)p->h.small.size();
+      it.small_root = p->h.small_root;
+      it.small_root_log2 = p->h.small_root_log2;
+      it.small_words = p->h.small_words;
+    }
     done_base += it.n_steps;
     hi[i] = it;
   }
@@ -394,7 +408,10 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
   const float* rv = reinterpret_cast<const float*>(c->rvals.p);
   const int smem = max_stream_smem_bytes();
   CU(cudaMemsetAsync(c->misc.p, 0, 64, s));
-  if (mode == TB_MODE_BATCHED) {
+  if (mode == TB_MODE_FUSED) {
+    CU(launch_small<T>((unsigned)n, c->small_smem, s, items, n, out_item, rv));
+    launches++;
+  } else if (mode == TB_MODE_BATCHED) {
     CU(cudaMemsetAsync(c->done.p, 0, sizeof(int) * done_words, s));
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
     int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
@@ -441,6 +458,14 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if (plans[i]->ctx != c) return fail(TB_ERR_INVALID, "plan belongs to another context");
     if (!plans[i]->h.has_weights) return fail(TB_ERR_INVALID, "plan has no bound weights (tb_plan_bind_mis)");
     if ((st = upload_plan(plans[i], false))) return st;
+  }
+  if (mode == TB_MODE_FUSED) {
+    int words = 0;
+    for (int i = 0; i < n; i++) {
+      if (!plans[i]->h.small_ok) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: a plan has no small form");
+      words = std::max(words, plans[i]->h.small_words);
+    }
+    c->small_smem = (int)(std::max(words, 1) * sizeof(T));
   }
   // weights of each distinct plan, staged once per call
   std::vector<int64_t> w_off(n);
@@ -522,11 +547,13 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     CU(cudaEventSynchronize(c->ev1));
   } else {
     // arenas of all items side by side; waves when over budget
-    std::vector<int64_t> aoff(n);
+    std::vector<int64_t> aoff(n, 0);
     int64_t tot = 0;
-    for (int i = 0; i < n; i++) {
-      aoff[i] = tot;
-      tot = align_up(tot + plans[i]->h.arena_elems, 64);
+    if (mode != TB_MODE_FUSED) {  // the fused form keeps every tensor in shared memory
+      for (int i = 0; i < n; i++) {
+        aoff[i] = tot;
+        tot = align_up(tot + plans[i]->h.arena_elems, 64);
+      }
     }
     size_t bytes = (size_t)tot * sizeof(T) + 256;
     if (bytes > c->budget) {
@@ -727,6 +754,18 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : best_cps * c->sms;
   c->chunk_div = best_div;
+  c->tune_fallback = best_mode;
+  // 3. the fused small form, when every plan has one
+  bool all_small = true;
+  for (tb_plan* p : uniq) all_small = all_small && p->h.small_ok;
+  if (all_small) {
+    if ((st = time_batch(c, n, plans, sv, r, TB_MODE_FUSED, ms))) return st;
+    res.n_tried++;
+    if (ms < best) {
+      best = ms;
+      best_mode = TB_MODE_FUSED;
+    }
+  }
   res.mode = best_mode;
   res.tile_bits = best_bits;
   res.ctas_per_sm = c->persistent_ctas / std::max(1, c->sms);
@@ -893,6 +932,7 @@ tb_status tb_plan_stats_get(const tb_plan* p, tb_plan_stats* o) {
   o->n_open = (int32_t)p->h.open.size();
   o->n_sliced = (int32_t)p->h.sliced.size();
   o->n_tiles = (int32_t)std::min<int64_t>(p->h.total_tiles, 0x7fffffff);
+  o->small_words = p->h.small_ok ? p->h.small_words : 0;
   return TB_OK;
 }
 
@@ -1014,7 +1054,8 @@ tb_status tb_solve_batch(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8
                          float* out_item, float* out_max, int32_t mode) {
   if (!c) return fail(TB_ERR_INVALID, "null context");
   if (n <= 0 || !plans) return fail(TB_ERR_INVALID, "empty batch");
-  if (mode != TB_MODE_PLAIN && mode != TB_MODE_BATCHED && mode != TB_MODE_LAYERED && mode != TB_MODE_AUTO)
+  if (mode != TB_MODE_PLAIN && mode != TB_MODE_BATCHED && mode != TB_MODE_LAYERED && mode != TB_MODE_AUTO &&
+      mode != TB_MODE_FUSED)
     return fail(TB_ERR_INVALID, "unknown mode");
   std::lock_guard<std::mutex> lk(c->mu);
   try {
@@ -1024,6 +1065,12 @@ tb_status tb_solve_batch(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8
         if (st) return st;
       }
       mode = c->tuned ? c->tune.mode : TB_MODE_BATCHED;
+      if (mode == TB_MODE_FUSED)
+        for (int32_t i = 0; i < n; i++)
+          if (plans[i] && !plans[i]->h.small_ok) {
+            mode = c->tune_fallback;
+            break;
+          }
     }
     if (c->opt.dtype == TB_DTYPE_F32) return solve_batch_t<float>(c, n, plans, slice_vals, r, out_item, out_max, mode);
     return solve_batch_t<int32_t>(c, n, plans, slice_vals, r, out_item, out_max, mode);
@@ -1283,6 +1330,41 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
       rec.a = op.a_off; rec.b = op.b_off; rec.c = op.c_off; rec.M = op.M; rec.N = op.N; rec.K = op.K; rec.batch = op.batch;
       std::memcpy(p, &rec, sizeof(rec)); p += sizeof(rec);
     }
+  *blob = b;
+  *blob_bytes = (int64_t)bytes;
+  return TB_OK;
+}
+
+// The fused small form of a plan (host only, for the CPU emulator): blob =
+//   int32 {small_ok, n_small, n_leaves, words, root_off, root_log2};
+//   SmallNode nodes[n_small]; int32 leaf_off[n_leaves]
+extern "C" int32_t tbi_plan_small(int32_t n_labels, int32_t n_tensors, const int32_t* ix_off, const int32_t* ix_lab,
+                                  int32_t n_iy, const int32_t* iy, int32_t n_nodes, const int32_t* children,
+                                  int32_t n_sliced, const int32_t* sliced, void** blob, int64_t* blob_bytes,
+                                  char* err, int32_t err_cap) {
+  PlanInput in;
+  in.n_labels = n_labels; in.n_tensors = n_tensors; in.ix_off = ix_off; in.ix_lab = ix_lab;
+  in.n_iy = n_iy; in.iy = iy; in.n_nodes = n_nodes; in.children = children;
+  in.n_sliced = n_sliced; in.sliced = sliced;
+  PlanHost h;
+  std::string e = compile_plan(in, h, 4);
+  if (!e.empty()) {
+    if (err && err_cap > 0) {
+      std::strncpy(err, e.c_str(), err_cap - 1);
+      err[err_cap - 1] = 0;
+    }
+    return TB_ERR_INVALID;
+  }
+  const size_t bytes = 6 * 4 + h.small.size() * sizeof(SmallNode) + h.small_leaf.size() * 4;
+  char* b = (char*)std::malloc(bytes);
+  if (!b) return TB_ERR_OOM;
+  int32_t hdr[6] = {h.small_ok ? 1 : 0, (int32_t)h.small.size(), (int32_t)h.small_leaf.size(), h.small_words,
+                    h.small_root, h.small_root_log2};
+  char* q = b;
+  std::memcpy(q, hdr, sizeof(hdr)); q += sizeof(hdr);
+  if (!h.small.empty()) std::memcpy(q, h.small.data(), h.small.size() * sizeof(SmallNode));
+  q += h.small.size() * sizeof(SmallNode);
+  if (!h.small_leaf.empty()) std::memcpy(q, h.small_leaf.data(), h.small_leaf.size() * 4);
   *blob = b;
   *blob_bytes = (int64_t)bytes;
   return TB_OK;

@@ -648,7 +648,103 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
   }
   p.plain_elems = fused_end + scratch;
   p.arena_elems = extra;  // the plain path never touches the K-part partials
+  compile_small(p);
   return "";
+}
+
+void compile_small(PlanHost& p) {
+  p.small_ok = false;
+  p.small.clear();
+  p.small_leaf.clear();
+  const int T = p.n_tensors;
+  const int total = T + p.n_nodes;
+  for (int i = 0; i < total; i++)
+    if ((int)p.labels[i].size() > kSmallMaxRank) return;
+  for (int i = 0; i < T; i++)
+    if (p.leaf_raw[i].empty() || p.leaf_raw[i].size() > 2) return;  // vertex and edge tensors only
+  std::vector<int32_t> off(total, -1);
+  int32_t end = 0;
+  for (int i = 0; i < T; i++) {
+    off[i] = end;
+    end += 1 << p.labels[i].size();
+  }
+  // first fit over free blocks (start, size), kept sorted and coalesced
+  std::vector<std::pair<int32_t, int32_t>> fl;
+  auto alloc = [&](int32_t n) -> int32_t {
+    for (size_t k = 0; k < fl.size(); k++) {
+      if (fl[k].second < n) continue;
+      const int32_t o = fl[k].first;
+      fl[k].first += n;
+      fl[k].second -= n;
+      if (fl[k].second == 0) fl.erase(fl.begin() + (long)k);
+      return o;
+    }
+    if (!fl.empty() && fl.back().first + fl.back().second == end) {
+      const int32_t o = fl.back().first;
+      fl.pop_back();
+      end = o + n;
+      return o;
+    }
+    const int32_t o = end;
+    end += n;
+    return o;
+  };
+  auto release = [&](int32_t o, int32_t n) {
+    const size_t k = (size_t)(std::lower_bound(fl.begin(), fl.end(), std::make_pair(o, 0)) - fl.begin());
+    fl.insert(fl.begin() + (long)k, {o, n});
+    if (k + 1 < fl.size() && fl[k].first + fl[k].second == fl[k + 1].first) {
+      fl[k].second += fl[k + 1].second;
+      fl.erase(fl.begin() + (long)k + 1);
+    }
+    if (k > 0 && fl[k - 1].first + fl[k - 1].second == fl[k].first) {
+      fl[k - 1].second += fl[k].second;
+      fl.erase(fl.begin() + (long)k);
+    }
+  };
+  std::vector<SmallNode> nodes;
+  for (int j = 0; j < p.n_nodes; j++) {
+    const int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
+    if (a == b) return;
+    const std::vector<int32_t>& A = p.labels[a];
+    const std::vector<int32_t>& B = p.labels[b];
+    const std::vector<int32_t>& C = p.labels[me];
+    std::vector<int32_t> R;
+    for (const std::vector<int32_t>* v : {&A, &B})
+      for (int32_t x : *v)
+        if (index_of(C, x) < 0 && index_of(R, x) < 0) R.push_back(x);
+    for (int32_t x : C)
+      if (index_of(A, x) < 0 && index_of(B, x) < 0) return;  // an output label no operand holds
+    const int nc = (int)C.size(), nk = (int)R.size();
+    if (nc + nk > kSmallMaxL) return;
+    SmallNode nd;
+    std::memset(&nd, 0, sizeof(nd));
+    nd.a_off = off[a];
+    nd.b_off = off[b];
+    nd.c_off = alloc(1 << nc);
+    nd.nc_nk = nc | (nk << 8);
+    for (int i = 0; i < 16; i++) {
+      uint32_t qa = 15, qb = 15;
+      if (i < nc + nk) {
+        const int32_t x = i < nc ? C[i] : R[i - nc];
+        const int ia = index_of(A, x), ib = index_of(B, x);
+        if (ia >= 0) qa = (uint32_t)ia;
+        if (ib >= 0) qb = (uint32_t)ib;
+      }
+      nd.pa[i >> 3] |= qa << (4 * (i & 7));
+      nd.pb[i >> 3] |= qb << (4 * (i & 7));
+    }
+    off[me] = nd.c_off;
+    nodes.push_back(nd);
+    if (a >= T) release(off[a], 1 << A.size());
+    if (b >= T) release(off[b], 1 << B.size());
+  }
+  if (end > kSmallMaxWords) return;
+  p.small = std::move(nodes);
+  p.small_leaf.assign(off.begin(), off.begin() + T);
+  p.small_words = end;
+  p.small_root = off[p.root];
+  p.small_root_log2 = (int32_t)p.labels[p.root].size();
+  p.small_ok = true;
 }
 
 std::string retile_plan(PlanHost& p, int bits) {

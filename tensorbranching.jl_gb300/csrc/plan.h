@@ -69,7 +69,19 @@ struct PlanHost {
   std::vector<int32_t> step_node;              // node a step contracts (-1: leaves, final); a split-K
                                                // reduce step holds -2 - node
   std::vector<int64_t> split_off;              // per node: arena offset of its K-part partials (-1)
+
+  // fused small form (compile_small): every tensor in the reported label
+  // order, leaves packed first, intermediates placed by first fit and freed
+  // after their parent
+  bool small_ok = false;
+  std::vector<SmallNode> small;
+  std::vector<int32_t> small_leaf;
+  int32_t small_words = 0, small_root = 0, small_root_log2 = 0;
 };
+
+// Build the fused small form of a compiled plan when it fits the limits of
+// tb_internal.h; sets small_ok.
+void compile_small(PlanHost& p);
 
 // Compile; returns "" on success or an error message.
 std::string compile_plan(const PlanInput& in, PlanHost& out, int gemm_min_log2);

@@ -93,6 +93,25 @@ struct FinalDesc {
   int32_t pad_;
 };
 
+// Fused small-network form: one warp contracts a whole network in shared
+// memory.  Limits: tensors of at most kSmallMaxRank labels, nodes of at most
+// kSmallMaxL labels (outputs + reduced), kSmallMaxWords shared words.
+constexpr int kSmallMaxRank = 13;
+constexpr int kSmallMaxL = 16;
+constexpr int kSmallMaxWords = 12288;
+
+// One contraction C = max_R A + B of the fused small form.  Bit i of the
+// index x = o | k << nc (o: output index, k: reduced index) selects bit
+// pos_a(i) of A's index and pos_b(i) of B's, packed 4 bits per position in
+// pa / pb (15: the label is not in that operand).  Offsets are shared-memory
+// words.
+struct SmallNode {
+  int32_t a_off, b_off, c_off;
+  int32_t nc_nk;  // nc | nk << 8
+  uint32_t pa[2], pb[2];
+};
+static_assert(sizeof(SmallNode) == 32, "SmallNode layout");
+
 // One batch item as the persistent executor sees it.
 template <typename T>
 struct ItemDev {
@@ -109,6 +128,13 @@ struct ItemDev {
   int32_t done_base;   // offset of this item's step counters
   int32_t n_steps;
   FinalDesc fin;
+  // fused small form (null when the plan has none)
+  const SmallNode* small;
+  const int32_t* small_leaf;  // shared-memory word offset of each leaf
+  int32_t n_small;
+  int32_t small_root;         // shared-memory offset of the root tensor
+  int32_t small_root_log2;
+  int32_t small_words;
 };
 
 // A group = all tiles of one (item, step); groups are listed in dependency

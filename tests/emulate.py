@@ -456,3 +456,104 @@ def run_plain(desc, weights, slice_vals=()):
     off, rank = desc["off"], desc["rank"]
     nodes = [arena[off[T + k]:off[T + k] + (1 << rank[T + k])].copy() for k in range(desc["n_nodes"])]
     return arena[fin.root_off:fin.root_off + (1 << fin.root_log2)].copy(), nodes
+
+
+# ---------------------------------------------------------------------------
+# fused small form (k_small): one warp, the whole network in shared memory
+# ---------------------------------------------------------------------------
+class SmallNode(ctypes.Structure):
+    _fields_ = [("a_off", c_int32), ("b_off", c_int32), ("c_off", c_int32), ("nc_nk", c_int32),
+                ("pa", ctypes.c_uint32 * 2), ("pb", ctypes.c_uint32 * 2)]
+
+
+def describe_small(lib, code, sliced=()):
+    """The plan's small form through ``tbi_plan_small`` (host only)."""
+    lib.tbi_plan_small.restype = c_int32
+    lib.tbi_plan_small.argtypes = [c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_void_p,
+                                   c_int32, c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_int64),
+                                   ctypes.c_char_p, c_int32]
+    lib.tbi_free.argtypes = [c_void_p]
+    off, lab = code.csr()
+    iy = np.array(code.iy if code.iy else [0], np.int32)
+    ch = code.children if code.n_nodes else np.zeros((1, 2), np.int32)
+    sl = np.array(list(sliced) if len(sliced) else [0], np.int32)
+    blob, nbytes = c_void_p(), c_int64()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.tbi_plan_small(code.n_labels, code.n_tensors, off.ctypes.data, lab.ctypes.data, len(code.iy),
+                            iy.ctypes.data, code.n_nodes, ch.ctypes.data, len(sliced), sl.ctypes.data,
+                            ctypes.byref(blob), ctypes.byref(nbytes), err, 512)
+    if rc:
+        raise ValueError(err.value.decode())
+    raw = ctypes.string_at(blob, nbytes.value)
+    lib.tbi_free(blob)
+    ok, n_small, n_leaves, words, root_off, root_log2 = [int(x) for x in np.frombuffer(raw, np.int32, 6, 0)]
+    p = 24
+    nodes = []
+    for _ in range(n_small):
+        nodes.append(SmallNode.from_buffer_copy(raw[p:p + 32]))
+        p += 32
+    leaf_off = np.frombuffer(raw, np.int32, n_leaves, p).copy()
+    p += 4 * n_leaves
+    assert p == len(raw)
+    return dict(ok=bool(ok), nodes=nodes, leaf_off=leaf_off, words=words, root_off=root_off, root_log2=root_log2)
+
+
+def _small_stride(pw, i):
+    q = (int(pw[i >> 3]) >> (4 * (i & 7))) & 15
+    return (1 << q) & 0x7FFF
+
+
+def run_small(sd, leaves, children, weights, slice_vals=(), r=0.0):
+    """Replay k_small for one item: the leaf builder into shared memory, every
+    node's lane loops (all outputs o, all reduced k) and the root max.  Every
+    shared access must stay inside the item's words, every operand word must
+    still hold the tensor the node reads (first-fit reuse never overwrote a
+    live tensor), and no node may write over its own operands."""
+    words = sd["words"]
+    assert 0 < words <= 12288
+    sm = np.full(words, np.nan, np.float64)
+    owner = np.full(words, -1, np.int64)
+    T = len(leaves)
+    for i, ld in enumerate(leaves):
+        w = float(weights[ld.label]) if ld.label >= 0 else float(ld.w)
+        base = int(sd["leaf_off"][i])
+        for e in range(1 << ld.n_out):
+            best = -np.inf
+            for raw in range(1 << ld.nraw):
+                ok = True
+                for k in range(ld.nraw):
+                    x = (raw >> k) & 1
+                    if ld.slice_idx[k] >= 0:
+                        ok &= x == int(slice_vals[ld.slice_idx[k]])
+                    else:
+                        ok &= ((e >> ld.out_bit[k]) & 1) == x
+                if ok:
+                    best = max(best, (w if raw & 1 else 0.0) if ld.nraw == 1 else (-np.inf if raw == 3 else 0.0))
+            assert 0 <= base + e < words
+            sm[base + e] = best
+            owner[base + e] = i
+    for j, nd in enumerate(sd["nodes"]):
+        a, b = int(children[j][0]), int(children[j][1])
+        nc, nk = nd.nc_nk & 0xFF, (nd.nc_nk >> 8) & 0xFF
+        assert nc + nk <= 16
+        o = np.arange(1 << nc)
+        k = np.arange(1 << nk)
+        ao = sum(((o >> i) & 1) * _small_stride(nd.pa, i) for i in range(nc)) if nc else np.zeros(1, np.int64)
+        bo = sum(((o >> i) & 1) * _small_stride(nd.pb, i) for i in range(nc)) if nc else np.zeros(1, np.int64)
+        ak = sum(((k >> i) & 1) * _small_stride(nd.pa, nc + i) for i in range(nk)) if nk else np.zeros(1, np.int64)
+        bk = sum(((k >> i) & 1) * _small_stride(nd.pb, nc + i) for i in range(nk)) if nk else np.zeros(1, np.int64)
+        ia = nd.a_off + np.asarray(ao)[:, None] + np.asarray(ak)[None, :]
+        ib = nd.b_off + np.asarray(bo)[:, None] + np.asarray(bk)[None, :]
+        ic = nd.c_off + o
+        for idx, want in ((ia, a), (ib, b)):
+            assert idx.min() >= 0 and idx.max() < words, "operand read out of the item's shared words"
+            assert np.all(owner[idx] == want), f"node {j} reads words not holding tensor {want}"
+        assert ic.min() >= 0 and ic.max() < words, "output out of the item's shared words"
+        assert not (set(ic.tolist()) & (set(ia.ravel().tolist()) | set(ib.ravel().tolist()))), \
+            f"node {j} writes over its operands"
+        sm[ic] = np.max(sm[ia] + sm[ib], axis=1)
+        owner[ic] = T + j
+    root_id = T + len(sd["nodes"]) - 1 if sd["nodes"] else 0
+    ir = sd["root_off"] + np.arange(1 << sd["root_log2"])
+    assert ir.min() >= 0 and ir.max() < words and np.all(owner[ir] == root_id)
+    return float(np.max(sm[ir])) + r

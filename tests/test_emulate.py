@@ -125,3 +125,64 @@ def test_tile_sizes_of_the_autotuner(tb, orc, lib, bits):
     n8 = sum(s.n_tiles for s in emulate.describe(lib, code, tile_bits=8)["steps"])
     n10 = sum(s.n_tiles for s in emulate.describe(lib, code, tile_bits=10)["steps"])
     assert n8 > n10
+
+
+# ---------------------------------------------------------------------------
+# fused small form (TB_MODE_FUSED): one warp per network, shared memory only
+# ---------------------------------------------------------------------------
+def _check_small(lib, orc, code, w, sliced=(), sv=(), r=0.0):
+    sd = emulate.describe_small(lib, code, sliced)
+    assert sd["ok"]
+    desc = emulate.describe(lib, code, sliced)
+    ch = code.children if code.n_nodes else np.zeros((0, 2), np.int32)
+    got = emulate.run_small(sd, desc["leaves"], ch, w, sv, r)
+    ref = orc.execute(code, w, sliced=sliced, slice_vals=sv)
+    assert got == float(np.max(ref)) + r
+    return sd
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_small_form_rr(tb, orc, lib, seed):
+    g, w, code = rr_case(tb, 24 + 6 * seed, seed, weighted=bool(seed % 2))
+    sd = _check_small(lib, orc, code, w, r=1.5 * seed)
+    assert sd["words"] >= sum(1 << len(set(ix)) for ix in code.ixs)
+
+
+def test_small_form_slices_open_labels_and_corners(tb, orc, lib):
+    g, w, code = rr_case(tb, 24, 11)
+    for a in (0, 1):
+        for b in (0, 1):
+            _check_small(lib, orc, code, w, [0, 5], (a, b))
+    opened = tb.CompressedEinsum(code.ixs, [2, 9], code.children, n_labels=code.n_labels)
+    _check_small(lib, orc, opened, w)
+    _check_small(lib, orc, opened, w, [4], (1,))
+    for name, g, w, code in corner_cases(tb):
+        _check_small(lib, orc, code, w)
+    g, w, code = ksg_case(tb, 5, 1, weighted=True)
+    _check_small(lib, orc, code, w)
+
+
+def test_small_form_limits(tb, lib):
+    """Networks past the shared-memory budget or the rank limit have no
+    small form (TB_MODE_FUSED refuses them)."""
+    g, w, code = rr_case(tb, 120, 3)
+    assert code.complexity()[1] > 13
+    assert not emulate.describe_small(lib, code)["ok"]
+    g, w, code = rr_case(tb, 40, 3)
+    assert code.complexity()[1] <= 13 and emulate.describe_small(lib, code)["ok"]
+
+
+def test_small_form_branch_batch(tb, orc, lib):
+    """Branches of the reference's rule (sc <= 8) all have a small form and
+    replay to the oracle's values."""
+    g = tb.random_regular_graph(60, 3, 5)
+    w = np.ones(g.n, np.float32)
+    kr = tb.kernelize(g, w)
+    code = tb.initialize_code(kr.g, tb.GreedyMethod(5))
+    branches = tb.slice(tb.MISProblem(kr.g, kr.weights), code, kr.r,
+                        tb.ContractionTreeSlicer(sc_target=8, refine=False,
+                                                 region_selector=tb.ScoreRS(n_max=12)))
+    for b in branches:
+        if b.code is None or b.p.g.n == 0:
+            continue
+        _check_small(lib, orc, b.code, b.p.weight_array(), r=b.r)

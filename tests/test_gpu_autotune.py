@@ -33,7 +33,7 @@ def test_autotune_then_auto_mode(tb, orc):
     eng, plans, svs, rs, refs = _batch(tb, orc)
     try:
         res = eng.autotune(plans, slice_vals=svs, r=rs)
-        assert res["mode"] in ("batched", "layered")
+        assert res["mode"] in ("batched", "layered", "fused")
         assert 8 <= res["tile_bits"] <= 11
         assert res["ctas_per_sm"] >= 1 and res["chunk_div"] in (1, 4, 16)
         assert res["n_tried"] >= 5 and 0 < res["ms"] <= res["ms_default"]
