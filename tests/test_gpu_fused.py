@@ -16,7 +16,7 @@ def _uneven(tb, orc, engine, n=16):
         if seed % 3 == 0:
             g, w, code = ksg_case(tb, 4 + seed % 4, seed, weighted=bool(seed % 2))
         else:
-            g, w, code = rr_case(tb, 12 + 3 * seed, seed, weighted=bool(seed % 2))
+            g, w, code = rr_case(tb, 12 + 4 * seed, seed, weighted=bool(seed % 2))
         plans.append(engine.plan(code, w))
         refs.append(orc.solve(code, w))
         rs.append(0.5 * seed)
@@ -35,7 +35,7 @@ def test_fused_uneven_batch(tb, orc, engine):
 def test_fused_int32(tb, orc, engine_i32):
     plans, refs = [], []
     for seed in range(6):
-        g, w, code = rr_case(tb, 30 + 5 * seed, seed)
+        g, w, code = rr_case(tb, 30 + 4 * seed, seed)
         plans.append(engine_i32.plan(code, w))
         refs.append(orc.solve(code, w, dtype=np.int32))
     out, mx = engine_i32.solve_batch(plans, mode="fused")
