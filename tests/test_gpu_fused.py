@@ -10,7 +10,7 @@ from cases import corner_cases, ksg_case, rr_case
 pytestmark = pytest.mark.gpu
 
 
-def _uneven(tb, orc, engine, n=16):
+def _uneven(tb, orc, engine, n=13):
     plans, refs, rs = [], [], []
     for seed in range(n):
         if seed % 3 == 0:
