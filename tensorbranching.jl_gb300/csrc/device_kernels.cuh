@@ -166,6 +166,13 @@ __global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, int n_ite
   const int item = blockIdx.x;
   if (item >= n_items) return;
   const ItemDev<T>& it = items[item];
+  // the node records go to shared memory behind the tensors, so each node
+  // reads its record at shared-memory latency
+  int4* sdesc = reinterpret_cast<int4*>(tb_smem + small_desc_word(it.small_words));
+  {
+    const int4* g = reinterpret_cast<const int4*>(it.small);
+    for (int i = lane; i < 2 * it.n_small; i += 32) sdesc[i] = g[i];
+  }
   for (int i = lane; i < it.n_leaves; i += 32) {
     const LeafDesc ld = it.leaves[i];
     const T w = Trop<T>::from_w(it.w && ld.label >= 0 ? it.w[ld.label] : ld.w);
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, int n_ite
   }
   __syncwarp();
   for (int j = 0; j < it.n_small; j++) {
-    const SmallNode nd = it.small[j];
+    const SmallNode nd = reinterpret_cast<const SmallNode*>(sdesc)[j];
     const int nc = nd.nc_nk & 0xff, nk = (nd.nc_nk >> 8) & 0xff;
     const T* A = sm + nd.a_off;
     const T* B = sm + nd.b_off;
@@ -264,6 +271,12 @@ inline cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t 
 template <typename T>
 cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, int n, float* out_item,
                          const float* r) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
   k_small<T><<<grid, 32, smem, s>>>(items, n, out_item, r);
   return cudaGetLastError();
 }

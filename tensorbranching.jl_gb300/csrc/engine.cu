@@ -96,6 +96,8 @@ struct tb_plan {
   bool mis_checked = false;    // leaves checked to be vertex / edge tensors
   std::vector<int> vertex_leaves;
   uint64_t version = 0;        // bumps when device buffers move
+  uint64_t seen_call = 0;      // last solve call that staged this plan's weights
+  int64_t seen_off = 0;        // where that call staged them
 };
 
 struct GraphKey {
@@ -118,6 +120,7 @@ struct tb_ctx {
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   int small_smem = 0;   // shared bytes per item of the fused small form (this batch)
+  uint64_t call_counter = 0;  // solve calls (stamps plans seen in a call)
   int tune_fallback = TB_MODE_BATCHED;  // tuned mode for batches the fused form cannot run
   size_t budget = 0;
   DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals, wvals;
@@ -202,7 +205,9 @@ static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
     return cudaSuccess;
   };
   PlanHost& h = p->h;
-  if (p->leaves_dirty || !p->structure_uploaded)
+  // LeafDesc::w matters only to the paths that build leaves from it (the
+  // batched and plain solves pass a per-call weight array instead)
+  if (!p->structure_uploaded || (leaf_weights && p->leaves_dirty))
     for (int i : p->vertex_leaves) h.leaves[i].w = p->weights[h.leaves[i].label];
   if (!p->structure_uploaded) {
     void* before[6] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p};
@@ -460,29 +465,34 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if ((st = upload_plan(plans[i], false))) return st;
   }
   if (mode == TB_MODE_FUSED) {
-    int words = 0;
+    // tensors (in 4-byte words of T) then the staged node records
+    int bytes = 16;
     for (int i = 0; i < n; i++) {
-      if (!plans[i]->h.small_ok) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: a plan has no small form");
-      words = std::max(words, plans[i]->h.small_words);
+      const PlanHost& h = plans[i]->h;
+      if (!h.small_ok) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: a plan has no small form");
+      bytes = std::max(bytes, (int)(small_desc_word(h.small_words * (int)(sizeof(T) / 4)) * 4 +
+                                    h.small.size() * sizeof(SmallNode)));
     }
-    c->small_smem = (int)(std::max(words, 1) * sizeof(T));
+    if (bytes > 227 * 1024) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: network too large for shared memory");
+    c->small_smem = bytes;
   }
   // weights of each distinct plan, staged once per call
   std::vector<int64_t> w_off(n);
   std::vector<char> w_first(n, 0);
   int64_t w_total = 0;
   {
-    std::unordered_map<const tb_plan*, int64_t> seen;
-    seen.reserve((size_t)n * 2);
+    // first sighting of a plan in this call: its stamp is older than the call
+    const uint64_t call = ++c->call_counter;
     for (int i = 0; i < n; i++) {
-      auto it = seen.find(plans[i]);
-      if (it != seen.end()) {
-        w_off[i] = it->second;
+      tb_plan* p = plans[i];
+      if (p->seen_call == call) {
+        w_off[i] = p->seen_off;
       } else {
         w_off[i] = w_total;
         w_first[i] = 1;
-        seen.emplace(plans[i], w_total);
-        w_total += align_up(std::max<int64_t>(plans[i]->h.n_labels, 1), 4);
+        p->seen_call = call;
+        p->seen_off = w_total;
+        w_total += align_up(std::max<int64_t>(p->h.n_labels, 1), 4);
       }
     }
   }

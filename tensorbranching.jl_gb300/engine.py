@@ -64,6 +64,7 @@ class Plan:
         if getattr(self, "handle", None):
             self.engine.lib.tb_plan_destroy(self.handle)
             self.handle = None
+            self.engine._plans_closed = getattr(self.engine, "_plans_closed", 0) + 1
 
     def __del__(self):
         try:
@@ -115,13 +116,16 @@ class Engine:
             offs = offsets
             if flat.dtype != np.float32 or not flat.flags.c_contiguous or offs.dtype != np.int64 or len(offs) != n:
                 raise ValueError("flat weights must be contiguous float32 with one int64 offset per plan")
+        key = tuple(plans)
         cached = getattr(self, "_bind_cache", None)
-        if cached is not None and len(cached[0]) == n and all(a is b and a.handle for a, b in zip(cached[0], plans)):
+        if cached is not None and cached[3] == getattr(self, "_plans_closed", 0) and cached[0] == key:
             arr, n_labels = cached[1], cached[2]
         else:
+            if not all(p.handle for p in plans):
+                raise ValueError("a plan of the batch is closed")
             arr = (c_void_p * max(n, 1))(*[p.handle for p in plans])
             n_labels = np.array([p.code.n_labels for p in plans], np.int64)
-            self._bind_cache = (list(plans), arr, n_labels)
+            self._bind_cache = (key, arr, n_labels, getattr(self, "_plans_closed", 0))
         if offsets is not None and n and (np.any(offs < 0) or np.any(offs + n_labels > flat.shape[0])):
             raise ValueError("weights out of range")
         _native.check(self.lib.tb_plan_bind_mis_batch(n, ctypes.cast(arr, c_void_p), flat.ctypes.data,
@@ -131,12 +135,16 @@ class Engine:
         n = len(plans)
         # the handle array is kept with the plans it holds (so none of them
         # can be freed while cached) and reused when the same plans come again
+        # (a closed plan invalidates every cached array)
+        key = tuple(plans)
         cached = getattr(self, "_arr_cache", None)
-        if cached is not None and len(cached[0]) == n and all(a is b and a.handle for a, b in zip(cached[0], plans)):
+        if cached is not None and cached[2] == getattr(self, "_plans_closed", 0) and cached[0] == key:
             arr = cached[1]
         else:
+            if not all(p.handle for p in plans):
+                raise ValueError("a plan of the batch is closed")
             arr = (c_void_p * n)(*[p.handle for p in plans])
-            self._arr_cache = (list(plans), arr)
+            self._arr_cache = (key, arr, getattr(self, "_plans_closed", 0))
         sv = None
         if slice_vals is not None and isinstance(slice_vals, (list, tuple)) and all(len(x) == 0 for x in slice_vals):
             slice_vals = None
