@@ -96,6 +96,7 @@ struct tb_plan {
   bool mis_checked = false;    // leaves checked to be vertex / edge tensors
   std::vector<int> vertex_leaves;
   uint64_t version = 0;        // bumps when device buffers move
+  bool vertex_dense = false;   // vertex leaf k has label k
   uint64_t seen_call = 0;      // last solve call that staged this plan's weights
   int64_t seen_off = 0;        // where that call staged them
 };
@@ -596,6 +597,8 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     GraphKey key;
     key.mode = mode;
     key.sched = c->persistent_ctas * 64 + c->chunk_div;
+    key.plans.reserve(n);
+    key.versions.reserve(n);
     for (int i = 0; i < n; i++) {
       key.plans.push_back(plans[i]);
       key.versions.push_back(plans[i]->version);
@@ -963,24 +966,37 @@ tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
         return fail(TB_ERR_INVALID, "independent-set leaves have one (vertex) or two (edge) labels");
       if (p->h.leaves[i].nraw == 1) p->vertex_leaves.push_back(i);
     }
+    // the usual layout: vertex leaf k carries label k
+    p->vertex_dense = true;
+    for (size_t k = 0; k < p->vertex_leaves.size(); k++)
+      p->vertex_dense = p->vertex_dense && p->h.leaves[p->vertex_leaves[k]].label == (int32_t)k;
     p->mis_checked = true;
   }
   const bool is_int = p->ctx->opt.dtype == TB_DTYPE_I32;
   // every finite tensor value is an integer in [0, 8191] when the weights
   // are integers >= 0 summing below 8192: the GEMM tiles may then add and max
-  // them as packed int16 exactly
+  // them as packed int16 exactly.  One pass without branches (contiguous in
+  // the usual layout), the errors after it.
   double sum = 0;
-  bool ok16 = true;
-  for (int i : p->vertex_leaves) {
-    const float x = w[p->h.leaves[i].label];
-    if (!std::isfinite(x)) return fail(TB_ERR_INVALID, "weights must be finite");
-    const bool integral = x == std::floor(x);
-    if (is_int && (!integral || std::fabs(x) > 1e8f))
-      return fail(TB_ERR_INVALID, "int32 weights must be integers of magnitude below 1e8");
-    if (x < 0 || !integral) ok16 = false;
+  bool finite = true, integral = true, nonneg = true;
+  float maxabs = 0.0f;
+  auto scan = [&](float x) {
+    finite &= std::isfinite(x);
+    integral &= x == std::trunc(x);
+    nonneg &= x >= 0.0f;
+    maxabs = std::max(maxabs, std::fabs(x));
     sum += x;
+  };
+  if (p->vertex_dense) {
+    const int nv = (int)p->vertex_leaves.size();
+    for (int k = 0; k < nv; k++) scan(w[k]);
+  } else {
+    for (int i : p->vertex_leaves) scan(w[p->h.leaves[i].label]);
   }
-  ok16 = ok16 && sum < 8192;
+  if (!finite) return fail(TB_ERR_INVALID, "weights must be finite");
+  if (is_int && (!integral || maxabs > 1e8f))
+    return fail(TB_ERR_INVALID, "int32 weights must be integers of magnitude below 1e8");
+  const bool ok16 = integral && nonneg && sum < 8192;
   // the weights travel with each solve (one staged copy for the whole
   // batch); LeafDesc::w is refreshed only for the paths that read it
   p->weights.assign(w, w + p->h.n_labels);
