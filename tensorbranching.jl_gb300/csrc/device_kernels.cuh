@@ -158,21 +158,14 @@ __device__ __forceinline__ int small_stride(uint32_t p0, uint32_t p1, int i) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, int n_items, float* out_item,
-                                              const float* r) {
+__global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, const int32_t* order, int n_items,
+                                              float* out_item, const float* r) {
   extern __shared__ int tb_smem[];
   T* sm = reinterpret_cast<T*>(tb_smem);
   const int lane = threadIdx.x;
-  const int item = blockIdx.x;
-  if (item >= n_items) return;
+  if ((int)blockIdx.x >= n_items) return;
+  const int item = order[blockIdx.x];
   const ItemDev<T>& it = items[item];
-  // the node records go to shared memory behind the tensors, so each node
-  // reads its record at shared-memory latency
-  int4* sdesc = reinterpret_cast<int4*>(tb_smem + small_desc_word(it.small_words));
-  {
-    const int4* g = reinterpret_cast<const int4*>(it.small);
-    for (int i = lane; i < 2 * it.n_small; i += 32) sdesc[i] = g[i];
-  }
   for (int i = lane; i < it.n_leaves; i += 32) {
     const LeafDesc ld = it.leaves[i];
     const T w = Trop<T>::from_w(it.w && ld.label >= 0 ? it.w[ld.label] : ld.w);
@@ -197,8 +190,13 @@ __global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, int n_ite
     }
   }
   __syncwarp();
+  // node records come from global memory (L1/L2); the next one is loaded
+  // while this one runs
+  SmallNode nxt;
+  if (it.n_small > 0) nxt = it.small[0];
   for (int j = 0; j < it.n_small; j++) {
-    const SmallNode nd = reinterpret_cast<const SmallNode*>(sdesc)[j];
+    const SmallNode nd = nxt;
+    if (j + 1 < it.n_small) nxt = it.small[j + 1];
     const int nc = nd.nc_nk & 0xff, nk = (nd.nc_nk >> 8) & 0xff;
     const T* A = sm + nd.a_off;
     const T* B = sm + nd.b_off;
@@ -269,15 +267,15 @@ inline cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t 
 // launch wrappers (declared in launch.h)
 // ---------------------------------------------------------------------------
 template <typename T>
-cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, int n, float* out_item,
-                         const float* r) {
+cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const int32_t* order,
+                         int n, float* out_item, const float* r) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_small<T><<<grid, 32, smem, s>>>(items, n, out_item, r);
+  k_small<T><<<grid, 32, smem, s>>>(items, order, n, out_item, r);
   return cudaGetLastError();
 }
 

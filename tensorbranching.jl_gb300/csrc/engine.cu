@@ -101,6 +101,12 @@ struct tb_plan {
   int64_t seen_off = 0;        // where that call staged them
 };
 
+// One launch of the fused small form: items small_order[first, first + count),
+// each block asking for smem bytes.
+struct SmallGroup {
+  int first, count, smem;
+};
+
 struct GraphKey {
   std::vector<const tb_plan*> plans;
   std::vector<uint64_t> versions;
@@ -120,7 +126,9 @@ struct tb_ctx {
   int persistent_ctas = 0;
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
-  int small_smem = 0;   // shared bytes per item of the fused small form (this batch)
+  std::vector<int32_t> small_order;   // fused small form: items by shared need, largest first
+  std::vector<SmallGroup> small_groups;  // launches over small_order
+  DevBuf small_order_dev;
   uint64_t call_counter = 0;  // solve calls (stamps plans seen in a call)
   int tune_fallback = TB_MODE_BATCHED;  // tuned mode for batches the fused form cannot run
   size_t budget = 0;
@@ -415,8 +423,11 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
   const int smem = max_stream_smem_bytes();
   CU(cudaMemsetAsync(c->misc.p, 0, 64, s));
   if (mode == TB_MODE_FUSED) {
-    CU(launch_small<T>((unsigned)n, c->small_smem, s, items, n, out_item, rv));
-    launches++;
+    const int32_t* order = reinterpret_cast<const int32_t*>(c->small_order_dev.p);
+    for (const SmallGroup& g : c->small_groups) {
+      CU(launch_small<T>((unsigned)g.count, g.smem, s, items, order + g.first, g.count, out_item, rv));
+      launches++;
+    }
   } else if (mode == TB_MODE_BATCHED) {
     CU(cudaMemsetAsync(c->done.p, 0, sizeof(int) * done_words, s));
     unsigned long long* ticket = reinterpret_cast<unsigned long long*>(c->misc.p);
@@ -466,16 +477,28 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if ((st = upload_plan(plans[i], false))) return st;
   }
   if (mode == TB_MODE_FUSED) {
-    // tensors (in 4-byte words of T) then the staged node records
-    int bytes = 16;
+    // items by shared-memory need, largest first, in up to four launches whose
+    // blocks ask for their own group's largest need (small networks are not
+    // held to the largest network's footprint)
+    std::vector<int> need(n);
     for (int i = 0; i < n; i++) {
       const PlanHost& h = plans[i]->h;
       if (!h.small_ok) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: a plan has no small form");
-      bytes = std::max(bytes, (int)(small_desc_word(h.small_words * (int)(sizeof(T) / 4)) * 4 +
-                                    h.small.size() * sizeof(SmallNode)));
+      need[i] = std::max(16, (int)(h.small_words * sizeof(T)));
     }
-    if (bytes > 227 * 1024) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: network too large for shared memory");
-    c->small_smem = bytes;
+    c->small_order.resize(n);
+    for (int i = 0; i < n; i++) c->small_order[i] = i;
+    std::stable_sort(c->small_order.begin(), c->small_order.end(),
+                     [&](int a, int b) { return need[a] > need[b]; });
+    c->small_groups.clear();
+    for (int g0 = 0; g0 < n;) {
+      const int top = need[c->small_order[g0]];
+      int g1 = g0 + 1;
+      if (c->small_groups.size() == 3) g1 = n;
+      while (g1 < n && (int64_t)need[c->small_order[g1]] * 4 >= (int64_t)top * 3) g1++;
+      c->small_groups.push_back({g0, g1 - g0, top});
+      g0 = g1;
+    }
   }
   // weights of each distinct plan, staged once per call
   std::vector<int64_t> w_off(n);
@@ -613,6 +636,11 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
       }
       c->have_key = false;
       if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, false, &w_off))) return st;
+      if (mode == TB_MODE_FUSED) {
+        CU(c->small_order_dev.ensure(sizeof(int32_t) * n));
+        CU(cudaMemcpyAsync(c->small_order_dev.p, c->small_order.data(), sizeof(int32_t) * n,
+                           cudaMemcpyHostToDevice, c->stream));
+      }
       CU(cudaStreamSynchronize(c->stream));
       c->key = key;
       c->have_key = true;

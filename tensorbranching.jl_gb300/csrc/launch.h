@@ -17,10 +17,10 @@ template <typename T>
 cudaError_t launch_tile(unsigned grid, int smem, cudaStream_t s, const TileDesc& d, T* arena, int64_t chunk);
 template <typename T>
 cudaError_t launch_final(cudaStream_t s, const FinalDesc& f, const T* arena, float r, float* out);
-// fused small form: one warp per item, grid = items
+// fused small form: one warp per item; block b runs item order[b] (b < n)
 template <typename T>
-cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, int n, float* out_item,
-                         const float* r);
+cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const int32_t* order,
+                         int n, float* out_item, const float* r);
 template <typename T>
 cudaError_t launch_k1_any(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
                           cudaStream_t s);

@@ -664,10 +664,6 @@ void compile_small(PlanHost& p) {
     if (p.leaf_raw[i].empty() || p.leaf_raw[i].size() > 2) return;  // vertex and edge tensors only
   std::vector<int32_t> off(total, -1);
   int32_t end = 0;
-  for (int i = 0; i < T; i++) {
-    off[i] = end;
-    end += 1 << p.labels[i].size();
-  }
   // first fit over free blocks (start, size), kept sorted and coalesced
   std::vector<std::pair<int32_t, int32_t>> fl;
   auto alloc = [&](int32_t n) -> int32_t {
@@ -701,6 +697,8 @@ void compile_small(PlanHost& p) {
       fl.erase(fl.begin() + (long)k);
     }
   };
+  // leaves first (packed from 0); each is freed after the node that reads it
+  for (int i = 0; i < T; i++) off[i] = alloc(1 << p.labels[i].size());
   std::vector<SmallNode> nodes;
   for (int j = 0; j < p.n_nodes; j++) {
     const int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
@@ -735,8 +733,8 @@ void compile_small(PlanHost& p) {
     }
     off[me] = nd.c_off;
     nodes.push_back(nd);
-    if (a >= T) release(off[a], 1 << A.size());
-    if (b >= T) release(off[b], 1 << B.size());
+    release(off[a], 1 << A.size());
+    release(off[b], 1 << B.size());
   }
   if (end > kSmallMaxWords) return;
   p.small = std::move(nodes);

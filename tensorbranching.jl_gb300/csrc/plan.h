@@ -71,8 +71,8 @@ struct PlanHost {
   std::vector<int64_t> split_off;              // per node: arena offset of its K-part partials (-1)
 
   // fused small form (compile_small): every tensor in the reported label
-  // order, leaves packed first, intermediates placed by first fit and freed
-  // after their parent
+  // order, leaves packed first, intermediates placed by first fit, every
+  // tensor freed after the node that reads it
   bool small_ok = false;
   std::vector<SmallNode> small;
   std::vector<int32_t> small_leaf;

@@ -112,14 +112,6 @@ struct SmallNode {
 };
 static_assert(sizeof(SmallNode) == 32, "SmallNode layout");
 
-#ifdef __CUDACC__
-#define TB_HOST_DEVICE __host__ __device__
-#else
-#define TB_HOST_DEVICE
-#endif
-// First shared-memory word of an item's staged node records in the fused
-// small form: 16-byte aligned, after the item's tensors.
-TB_HOST_DEVICE inline int small_desc_word(int tensor_words) { return (tensor_words + 3) & ~3; }
 
 // One batch item as the persistent executor sees it.
 template <typename T>
