@@ -71,7 +71,7 @@ typedef int32_t tb_status;
 #define TB_MODE_AUTO 3    /* the schedule tb_autotune chose for this context
                              (tuned on first use when tb_options.autotune is 1;
                              TB_MODE_BATCHED before any tuning) */
-#define TB_MODE_FUSED 4   /* one warp per item contracts the whole network in
+#define TB_MODE_FUSED 4   /* one block per item contracts the whole network in
                              shared memory, one launch for the batch; every
                              plan must have the small form (tensors of at most
                              2^13 entries, at most 48 KiB live per network,

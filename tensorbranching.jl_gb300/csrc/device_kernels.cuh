@@ -147,26 +147,28 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
   }
 }
 
-// Fused small form: block b (one warp) contracts item b's whole network in
-// shared memory (leaves, every node in post-order, the root max) and writes
-// one value.  Node j: lane l computes outputs o = l, l + 32, ...; the
-// addresses of A and B follow from the bits of o (and of the reduced index
-// k) through the node's 4-bit label positions.
+// Fused small form: block b contracts item order[b]'s whole network in
+// shared memory (leaves, every node in post-order with a block barrier
+// between nodes, the root max) and writes one value.  Node j: thread t
+// computes outputs o = t, t + kSmallThreads, ...; the addresses of A and B
+// follow from the bits of o (and of the reduced index k) through the node's
+// 4-bit label positions.
 __device__ __forceinline__ int small_stride(uint32_t p0, uint32_t p1, int i) {
   const uint32_t q = ((i < 8 ? p0 : p1) >> (4 * (i & 7))) & 15u;
   return (int)((1u << q) & 0x7fffu);  // position 15: not in this operand
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, const int32_t* order, int n_items,
-                                              float* out_item, const float* r) {
+__global__ void __launch_bounds__(kSmallThreads) k_small(const ItemDev<T>* items, const int32_t* order, int n_items,
+                                                         float* out_item, const float* r) {
   extern __shared__ int tb_smem[];
+  __shared__ float s_max[kSmallThreads / 32];
   T* sm = reinterpret_cast<T*>(tb_smem);
-  const int lane = threadIdx.x;
+  const int tid = threadIdx.x;
   if ((int)blockIdx.x >= n_items) return;
   const int item = order[blockIdx.x];
   const ItemDev<T>& it = items[item];
-  for (int i = lane; i < it.n_leaves; i += 32) {
+  for (int i = tid; i < it.n_leaves; i += kSmallThreads) {
     const LeafDesc ld = it.leaves[i];
     const T w = Trop<T>::from_w(it.w && ld.label >= 0 ? it.w[ld.label] : ld.w);
     T* dst = sm + it.small_leaf[i];
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, const int
       dst[e] = best;
     }
   }
-  __syncwarp();
+  __syncthreads();
   // node records come from global memory (L1/L2); the next one is loaded
   // while this one runs
   SmallNode nxt;
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, const int
     const T* A = sm + nd.a_off;
     const T* B = sm + nd.b_off;
     T* C = sm + nd.c_off;
-    for (int o = lane; o < (1 << nc); o += 32) {
+    for (int o = tid; o < (1 << nc); o += kSmallThreads) {
       int ao = 0, bo = 0;
       for (int i = 0; i < nc; i++) {
         if ((o >> i) & 1) {
@@ -222,13 +224,19 @@ __global__ void __launch_bounds__(32) k_small(const ItemDev<T>* items, const int
       }
       C[o] = acc;
     }
-    __syncwarp();
+    __syncthreads();
   }
   T m = Trop<T>::neg();
-  for (int i = lane; i < (1 << it.small_root_log2); i += 32) m = Trop<T>::mx(m, sm[it.small_root + i]);
+  for (int i = tid; i < (1 << it.small_root_log2); i += kSmallThreads) m = Trop<T>::mx(m, sm[it.small_root + i]);
   float v = Trop<T>::to_f(m);
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  if (lane == 0) out_item[item] = v + (r ? r[item] : 0.0f);
+  if ((tid & 31) == 0) s_max[tid >> 5] = v;
+  __syncthreads();
+  if (tid == 0) {
+    float b = s_max[0];
+    for (int w = 1; w < kSmallThreads / 32; w++) b = fmaxf(b, s_max[w]);
+    out_item[item] = b + (r ? r[item] : 0.0f);
+  }
 }
 
 template <typename T, int BM, int BN>
@@ -275,7 +283,7 @@ cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_small<T><<<grid, 32, smem, s>>>(items, order, n, out_item, r);
+  k_small<T><<<grid, kSmallThreads, smem, s>>>(items, order, n, out_item, r);
   return cudaGetLastError();
 }
 

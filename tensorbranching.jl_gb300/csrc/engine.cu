@@ -107,6 +107,17 @@ struct SmallGroup {
   int first, count, smem;
 };
 
+// Issue-slot estimate of one item of the fused small form: per node, each
+// lane's outputs times (address bits + reduced terms), plus a fixed cost.
+static double small_cost(const PlanHost& h) {
+  double c = 0;
+  for (const SmallNode& nd : h.small) {
+    const int nc = nd.nc_nk & 0xff, nk = (nd.nc_nk >> 8) & 0xff;
+    c += std::max(1.0, std::ldexp(1.0, nc - 5)) * (nc + 4.0 * std::ldexp(1.0, nk)) + 24.0;
+  }
+  return c;
+}
+
 struct GraphKey {
   std::vector<const tb_plan*> plans;
   std::vector<uint64_t> versions;
@@ -477,28 +488,22 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if ((st = upload_plan(plans[i], false))) return st;
   }
   if (mode == TB_MODE_FUSED) {
-    // items by shared-memory need, largest first, in up to four launches whose
-    // blocks ask for their own group's largest need (small networks are not
-    // held to the largest network's footprint)
-    std::vector<int> need(n);
+    // one launch, items longest first (blocks start roughly in index order,
+    // so the longest networks, which bound the launch, start first); every
+    // block asks for the largest shared-memory need of the batch
+    std::vector<double> cost(n);
+    int smem = 16;
     for (int i = 0; i < n; i++) {
       const PlanHost& h = plans[i]->h;
       if (!h.small_ok) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: a plan has no small form");
-      need[i] = std::max(16, (int)(h.small_words * sizeof(T)));
+      smem = std::max(smem, (int)(h.small_words * sizeof(T)));
+      cost[i] = small_cost(h);
     }
     c->small_order.resize(n);
     for (int i = 0; i < n; i++) c->small_order[i] = i;
     std::stable_sort(c->small_order.begin(), c->small_order.end(),
-                     [&](int a, int b) { return need[a] > need[b]; });
-    c->small_groups.clear();
-    for (int g0 = 0; g0 < n;) {
-      const int top = need[c->small_order[g0]];
-      int g1 = g0 + 1;
-      if (c->small_groups.size() == 3) g1 = n;
-      while (g1 < n && (int64_t)need[c->small_order[g1]] * 4 >= (int64_t)top * 3) g1++;
-      c->small_groups.push_back({g0, g1 - g0, top});
-      g0 = g1;
-    }
+                     [&](int a, int b) { return cost[a] > cost[b]; });
+    c->small_groups.assign(1, SmallGroup{0, n, smem});
   }
   // weights of each distinct plan, staged once per call
   std::vector<int64_t> w_off(n);

@@ -17,7 +17,7 @@ template <typename T>
 cudaError_t launch_tile(unsigned grid, int smem, cudaStream_t s, const TileDesc& d, T* arena, int64_t chunk);
 template <typename T>
 cudaError_t launch_final(cudaStream_t s, const FinalDesc& f, const T* arena, float r, float* out);
-// fused small form: one warp per item; block b runs item order[b] (b < n)
+// fused small form: one block per item; block b runs item order[b] (b < n)
 template <typename T>
 cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const int32_t* order,
                          int n, float* out_item, const float* r);

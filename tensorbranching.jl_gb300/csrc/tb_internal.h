@@ -93,12 +93,13 @@ struct FinalDesc {
   int32_t pad_;
 };
 
-// Fused small-network form: one warp contracts a whole network in shared
+// Fused small-network form: one block contracts a whole network in shared
 // memory.  Limits: tensors of at most kSmallMaxRank labels, nodes of at most
 // kSmallMaxL labels (outputs + reduced), kSmallMaxWords shared words.
 constexpr int kSmallMaxRank = 13;
 constexpr int kSmallMaxL = 16;
 constexpr int kSmallMaxWords = 12288;
+constexpr int kSmallThreads = 128;  // threads of one item's block
 
 // One contraction C = max_R A + B of the fused small form.  Bit i of the
 // index x = o | k << nc (o: output index, k: reduced index) selects bit

@@ -459,7 +459,7 @@ def run_plain(desc, weights, slice_vals=()):
 
 
 # ---------------------------------------------------------------------------
-# fused small form (k_small): one warp, the whole network in shared memory
+# fused small form (k_small): one block, the whole network in shared memory
 # ---------------------------------------------------------------------------
 class SmallNode(ctypes.Structure):
     _fields_ = [("a_off", c_int32), ("b_off", c_int32), ("c_off", c_int32), ("nc_nk", c_int32),
@@ -505,7 +505,7 @@ def _small_stride(pw, i):
 
 def run_small(sd, leaves, children, weights, slice_vals=(), r=0.0):
     """Replay k_small for one item: the leaf builder into shared memory, every
-    node's lane loops (all outputs o, all reduced k) and the root max.  Every
+    node's thread loops (all outputs o, all reduced k) and the root max.  Every
     shared access must stay inside the item's words, every operand word must
     still hold the tensor the node reads (first-fit reuse never overwrote a
     live tensor), and no node may write over its own operands."""

@@ -128,7 +128,7 @@ def test_tile_sizes_of_the_autotuner(tb, orc, lib, bits):
 
 
 # ---------------------------------------------------------------------------
-# fused small form (TB_MODE_FUSED): one warp per network, shared memory only
+# fused small form (TB_MODE_FUSED): one block per network, shared memory only
 # ---------------------------------------------------------------------------
 def _check_small(lib, orc, code, w, sliced=(), sv=(), r=0.0):
     sd = emulate.describe_small(lib, code, sliced)

@@ -1,4 +1,4 @@
-"""TB_MODE_FUSED (one warp per network, every tensor in shared memory) on
+"""TB_MODE_FUSED (one block per network, every tensor in shared memory) on
 the GPU: bit-exact against the oracle for uneven branch batches, sliced
 items, open labels, r offsets, f32 and int32; plans past its limits are
 refused; TB_MODE_AUTO falls back to the tuned tile schedule for them."""
