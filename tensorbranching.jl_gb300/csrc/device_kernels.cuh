@@ -277,11 +277,11 @@ inline cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t 
 template <typename T>
 cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const int32_t* order,
                          int n, float* out_item, const float* r) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  static int attr = 0;  // dynamic shared bytes the kernel is opted in for
+  if (smem > attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr = smem;
   }
   k_small<T><<<grid, kSmallThreads, smem, s>>>(items, order, n, out_item, r);
   return cudaGetLastError();
