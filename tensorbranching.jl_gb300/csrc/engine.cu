@@ -107,16 +107,6 @@ struct SmallGroup {
   int first, count, smem;
 };
 
-// Issue-slot estimate of one item of the fused small form: per node, each
-// lane's outputs times (address bits + reduced terms), plus a fixed cost.
-static double small_cost(const PlanHost& h) {
-  double c = 0;
-  for (const SmallNode& nd : h.small) {
-    const int nc = nd.nc_nk & 0xff, nk = (nd.nc_nk >> 8) & 0xff;
-    c += std::max(1.0, std::ldexp(1.0, nc - 5)) * (nc + 4.0 * std::ldexp(1.0, nk)) + 24.0;
-  }
-  return c;
-}
 
 struct GraphKey {
   std::vector<const tb_plan*> plans;
@@ -488,21 +478,14 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     if ((st = upload_plan(plans[i], false))) return st;
   }
   if (mode == TB_MODE_FUSED) {
-    // one launch, items longest first (blocks start roughly in index order,
-    // so the longest networks, which bound the launch, start first); every
-    // block asks for the largest shared-memory need of the batch
-    std::vector<double> cost(n);
+    // one launch; every block asks for the largest shared-memory need of the
+    // batch (the item order is built with the batch upload)
     int smem = 16;
     for (int i = 0; i < n; i++) {
       const PlanHost& h = plans[i]->h;
       if (!h.small_ok) return fail(TB_ERR_UNSUPPORTED, "TB_MODE_FUSED: a plan has no small form");
       smem = std::max(smem, (int)(h.small_words * sizeof(T)));
-      cost[i] = small_cost(h);
     }
-    c->small_order.resize(n);
-    for (int i = 0; i < n; i++) c->small_order[i] = i;
-    std::stable_sort(c->small_order.begin(), c->small_order.end(),
-                     [&](int a, int b) { return cost[a] > cost[b]; });
     c->small_groups.assign(1, SmallGroup{0, n, smem});
   }
   // weights of each distinct plan, staged once per call
@@ -642,6 +625,12 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
       c->have_key = false;
       if ((st = upload_batch<T>(c, n, plans, aoff, sv_off, false, &w_off))) return st;
       if (mode == TB_MODE_FUSED) {
+        // items longest first: blocks start roughly in index order, and the
+        // longest networks bound the launch
+        c->small_order.resize(n);
+        for (int i = 0; i < n; i++) c->small_order[i] = i;
+        std::stable_sort(c->small_order.begin(), c->small_order.end(),
+                         [&](int a, int b) { return plans[a]->h.small_cost > plans[b]->h.small_cost; });
         CU(c->small_order_dev.ensure(sizeof(int32_t) * n));
         CU(cudaMemcpyAsync(c->small_order_dev.p, c->small_order.data(), sizeof(int32_t) * n,
                            cudaMemcpyHostToDevice, c->stream));

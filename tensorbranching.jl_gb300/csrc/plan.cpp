@@ -742,6 +742,13 @@ void compile_small(PlanHost& p) {
   p.small_words = end;
   p.small_root = off[p.root];
   p.small_root_log2 = (int32_t)p.labels[p.root].size();
+  // per node: each thread's outputs times (address bits + reduced terms),
+  // plus a fixed cost for the record and the barrier
+  p.small_cost = 0;
+  for (const SmallNode& nd : p.small) {
+    const int nc = nd.nc_nk & 0xff, nk = (nd.nc_nk >> 8) & 0xff;
+    p.small_cost += std::max(1.0, std::ldexp(1.0, nc - 7)) * (nc + 4.0 * std::ldexp(1.0, nk)) + 24.0;
+  }
   p.small_ok = true;
 }
 

@@ -77,6 +77,7 @@ struct PlanHost {
   std::vector<SmallNode> small;
   std::vector<int32_t> small_leaf;
   int32_t small_words = 0, small_root = 0, small_root_log2 = 0;
+  double small_cost = 0;                       // issue-slot estimate of one item (launch order)
 };
 
 // Build the fused small form of a compiled plan when it fits the limits of
