@@ -124,6 +124,8 @@ void tb_options_default(tb_options* opt);
 
 /* Create / destroy a context bound to CUDA device `device`. */
 tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out);
+/* Plans created on ctx may still be passed to tb_plan_destroy afterwards
+ * (and to nothing else). */
 void tb_ctx_destroy(tb_ctx* ctx);
 const char* tb_last_error(const tb_ctx* ctx);
 /* Library version string, e.g. "tb 0.1 sm_103a". */

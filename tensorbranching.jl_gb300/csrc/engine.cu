@@ -21,6 +21,7 @@
 #include <string>
 #include <type_traits>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/tb.h"
@@ -131,6 +132,8 @@ struct tb_ctx {
   std::vector<SmallGroup> small_groups;  // launches over small_order
   DevBuf small_order_dev;
   uint64_t call_counter = 0;  // solve calls (stamps plans seen in a call)
+  std::mutex plans_mu;        // guards live_plans
+  std::unordered_set<tb_plan*> live_plans;  // plans created on this context and not destroyed
   int tune_fallback = TB_MODE_BATCHED;  // tuned mode for batches the fused form cannot run
   size_t budget = 0;
   DevBuf arena, items, groups, chunks, done, misc, slice_vals, out_item, rvals, wvals;
@@ -891,6 +894,12 @@ tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
 
 void tb_ctx_destroy(tb_ctx* c) {
   if (!c) return;
+  {
+    // plans that outlive their context keep only their own buffers
+    std::lock_guard<std::mutex> lk(c->plans_mu);
+    for (tb_plan* p : c->live_plans) p->ctx = nullptr;
+    c->live_plans.clear();
+  }
   cudaSetDevice(c->device);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->stream) cudaStreamSynchronize(c->stream);
@@ -937,18 +946,28 @@ tb_status tb_plan_create(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const
   for (auto& lab : p->h.labels)
     if (lab.size() > 30) return fail(TB_ERR_UNSUPPORTED, "a tensor of rank > 30 (over 4 GiB)");
   p->version = ++ctx->plan_counter;
+  {
+    std::lock_guard<std::mutex> lk(ctx->plans_mu);
+    ctx->live_plans.insert(p.get());
+  }
   *out = p.release();
   return TB_OK;
 }
 
 void tb_plan_destroy(tb_plan* p) {
   if (!p) return;
-  if (p->ctx && p->ctx->have_key) {
-    for (auto* q : p->ctx->key.plans)
-      if (q == p) {
-        p->ctx->have_key = false;
-        break;
-      }
+  if (p->ctx) {
+    {
+      std::lock_guard<std::mutex> lk(p->ctx->plans_mu);
+      p->ctx->live_plans.erase(p);
+    }
+    if (p->ctx->have_key) {
+      for (auto* q : p->ctx->key.plans)
+        if (q == p) {
+          p->ctx->have_key = false;
+          break;
+        }
+    }
   }
   delete p;
 }
@@ -982,6 +1001,7 @@ tb_status tb_plan_node_labels(const tb_plan* p, int32_t node, int32_t cap, int32
 
 tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   if (!p || !w) return fail(TB_ERR_INVALID, "null argument");
+  if (!p->ctx) return fail(TB_ERR_INVALID, "the plan's context was destroyed");
   if (!p->mis_checked) {
     for (int i = 0; i < p->h.n_tensors; i++) {
       if (p->h.leaves[i].nraw < 1 || p->h.leaves[i].nraw > 2)
@@ -1569,7 +1589,7 @@ extern "C" int32_t tbi_measure_maxplus_peak_i16(int32_t device, double* ops_per_
 // Re-tile a plan's stream steps (tile size), as the autotuner does; for
 // tests that pin one configuration.
 extern "C" int32_t tbi_plan_retile(tb_plan* p, int32_t bits) {
-  if (!p) return TB_ERR_INVALID;
+  if (!p || !p->ctx) return TB_ERR_INVALID;
   std::lock_guard<std::mutex> lk(p->ctx->mu);
   std::string e = retile_plan(p->h, bits);
   if (!e.empty()) return fail(TB_ERR_INVALID, e);

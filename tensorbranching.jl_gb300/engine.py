@@ -253,6 +253,9 @@ class Engine:
 
     def close(self):
         if getattr(self, "ctx", None):
+            # cached handle arrays hold plans; drop them with the context
+            self._arr_cache = None
+            self._bind_cache = None
             self.lib.tb_ctx_destroy(self.ctx)
             self.ctx = None
 

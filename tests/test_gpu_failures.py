@@ -50,3 +50,21 @@ def test_host_side_errors_are_status_codes(tb, native):
         assert e.value.status == native.TB_ERR_INVALID
     finally:
         eng.close()
+
+
+def test_plans_outliving_their_context(tb):
+    """Destroying a context before its plans leaves the plans destroyable
+    (and refused by everything else), in any order the garbage collector
+    picks."""
+    import numpy as np
+
+    eng = tb.Engine()
+    g = tb.random_regular_graph(20, 3, 1)
+    code = tb.initialize_code(g, tb.GreedyMethod(1))
+    plans = [eng.plan(code, np.ones(g.n, np.float32)) for _ in range(3)]
+    eng.solve_batch(plans, mode="fused")
+    eng.close()
+    with pytest.raises(tb._native.TbError):
+        tb._native.check(eng.lib.tb_plan_bind_mis(plans[0].handle, np.ones(g.n, np.float32).ctypes.data), None)
+    for p in plans:
+        p.close()
