@@ -472,7 +472,8 @@ def main():
         "peak_source": f"simt: measured f32 max-plus probe on this GPU ({simt / 1e12:.2f} Tops); packed-int16 "
                        f"max-plus probe {simt_i16 / 1e12:.2f} Tops (the GEMM tiles' ceiling when they run that "
                        f"form; used per node in attainable_frac); hbm: {peak_kind} copy bandwidth ({hbm:.0f} GB/s)",
-        "note": "dominant kernel k_persistent (batched) / k_level (layered) runs the whole step; achieved = "
+        "note": "dominant kernel k_persistent (batched) / k_level (layered) / k_small (fused: tensors stay in "
+                "shared memory, so the HBM fraction is nominal) runs the whole step; achieved = "
                 "algorithmic tropical ops 2*2^|L| (max and add; SIMT, no tensor cores) or bytes "
                 "4(|A|+|B|+|C|) summed over nodes / device time of the step; a node's compute ceiling is the "
                 "measured f32 max-plus rate, or the packed-int16 rate for GEMM nodes run in that form; "
