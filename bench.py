@@ -193,6 +193,8 @@ def make_items(engine, wl, tb, max_items=0):
             svs.append(np.zeros(0, np.int8))
             rs.append(b.r)
     wl["step_fraction"] = frac
+    if all(len(x) == 0 for x in svs):
+        svs = None  # no sliced plan: a caller passes no slice values
     return plans, svs, np.array(rs, np.float32)
 
 
@@ -428,7 +430,7 @@ def main():
     # e2e: bind weights from host (H2D) + solve + result read-back (D2H), wall clock
     uplans = list(uniq.values())
     # per step: the bound weights of every distinct plan, r and slice values
-    h2d = sum(4 * p.code.n_labels for p in uplans) + 4 * len(plans) + sum(len(x) for x in svs)
+    h2d = sum(4 * p.code.n_labels for p in uplans) + 4 * len(plans) + (sum(len(x) for x in svs) if svs else 0)
     d2h = 4 * (len(plans) + 1)
     host_w = [np.ascontiguousarray(_weights_of(wl, p), np.float32) for p in uplans]
     w_offs = np.zeros(len(uplans), np.int64)
