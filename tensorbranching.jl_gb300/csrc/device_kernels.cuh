@@ -203,19 +203,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_small(const ItemDev<T>* items
     const T* A = sm + nd.a_off;
     const T* B = sm + nd.b_off;
     T* C = sm + nd.c_off;
-    // the low 7 bits of every output this thread computes are its own index
-    // bits: their part of the addresses is summed once per node
-    static_assert(kSmallThreads == 128, "thread bits below");
-    int alo = 0, blo = 0;
-    for (int i = 0; i < (nc < 7 ? nc : 7); i++) {
-      if ((tid >> i) & 1) {
-        alo += small_stride(nd.pa[0], nd.pa[1], i);
-        blo += small_stride(nd.pb[0], nd.pb[1], i);
-      }
-    }
     for (int o = tid; o < (1 << nc); o += kSmallThreads) {
-      int ao = alo, bo = blo;
-      for (int i = 7; i < nc; i++) {
+      int ao = 0, bo = 0;
+      for (int i = 0; i < nc; i++) {
         if ((o >> i) & 1) {
           ao += small_stride(nd.pa[0], nd.pa[1], i);
           bo += small_stride(nd.pb[0], nd.pb[1], i);
