@@ -154,48 +154,17 @@ def load_workload(tb, name):
     return workloads.load(name)
 
 
-OPEN_BITS = 4          # sliced labels kept open per item (2^4 slices per item)
-SLICED_ITEMS_PER_STEP = 64
-
-
 def make_items(engine, wl, tb, max_items=0):
-    """Plans and per-item inputs of one step of the workload.  Index-sliced
-    workloads group 2^OPEN_BITS slices per item (those labels stay open in the
-    root tensor) and a step runs SLICED_ITEMS_PER_STEP of the items."""
-    plans, svs, rs = [], [], []
-    sliced = wl["sliced"]
-    frac = 1.0
-    for b in wl["branches"]:
-        if b.code is None:
-            continue
-        wmap = wl.setdefault("plan_weights", {})
-        if sliced:
-            ob = wl.get("open_bits", OPEN_BITS)
-            opened = sliced[:ob]
-            fixed = sliced[ob:]
-            code = tb.CompressedEinsum(b.code.ixs, list(opened), b.code.children, n_labels=b.code.n_labels)
-            p = engine.plan(code, b.p.weight_array(), sliced=fixed)
-            wmap[id(p)] = b.p.weight_array()
-            k = len(fixed)
-            total = 1 << k
-            take = min(total, max_items or SLICED_ITEMS_PER_STEP)
-            frac = take / total
-            idx = np.linspace(0, total - 1, take).astype(np.int64)
-            vals = ((idx[:, None] >> np.arange(k)[None, :]) & 1).astype(np.int8)
-            for row in vals:
-                plans.append(p)
-                svs.append(row)
-                rs.append(b.r)
-        else:
-            p = engine.plan(b.code, b.p.weight_array())
-            wmap[id(p)] = b.p.weight_array()
-            plans.append(p)
-            svs.append(np.zeros(0, np.int8))
-            rs.append(b.r)
-    wl["step_fraction"] = frac
-    if all(len(x) == 0 for x in svs):
-        svs = None  # no sliced plan: a caller passes no slice values
-    return plans, svs, np.array(rs, np.float32)
+    """Plans and per-item inputs of one step of the workload
+    (``workloads.step_items``): one plan per branch, shared by its slices."""
+    from tensorbranching_gb300 import workloads
+
+    items = workloads.step_items(wl, max_items)
+    plans, svs, rs = workloads.plans_for(engine, items)
+    wmap = wl.setdefault("plan_weights", {})
+    for it, p in zip(items, plans):
+        wmap[id(p)] = it["weights"]
+    return plans, svs, rs
 
 
 def expected_answer(wl):
@@ -237,11 +206,12 @@ def _subtree(tb, code, labs, j):
                                node_iy=niy, n_labels=code.n_labels), nodes
 
 
-def run_cpu_baseline(tb, orc, wl, budget_s: float):
-    """The oracle port (GEMM lowering, OpenMP on every host core) on a bounded
-    sample: the largest subtree of the first network whose contraction fits
-    the time budget, extrapolated by algorithmic ops to whole steps."""
-    threads = os.cpu_count() or 1
+def run_cpu_baseline(tb, orc, wl, budget_s: float, threads: int = 0):
+    """The oracle port (GEMM lowering, OpenMP on `threads` host cores, 0:
+    every core) on a bounded sample: the largest subtree of the first network
+    whose contraction fits the time budget, extrapolated by algorithmic ops
+    to whole steps."""
+    threads = orc.set_threads(threads)
     sliced = wl["sliced"]
     total_ops = 0.0
     for br in wl["branches"]:
@@ -305,6 +275,197 @@ def run_cpu_baseline(tb, orc, wl, budget_s: float):
             "ops_per_s": sops / dt}
 
 
+ANSWERS = os.path.join(ROOT, "tests", "golden", "workload_answers.json")
+EXTRA_CONFIGS = "rr100_ob10,ksg32_ob20,ksg32_b20,ksg32_dom20,rr300w_s22,rr220w_s22"
+PLAIN_MAX_ITEMS = 256
+
+
+def stored_answers(name):
+    """The oracle's item values for this workload (tests/golden/
+    workload_answers.json, made by tests/golden/make_answers.py), or None."""
+    if not os.path.exists(ANSWERS):
+        return None
+    with open(ANSWERS) as f:
+        return json.load(f).get(name)
+
+
+def check_answer(name, out, max_items):
+    """Every item value of a step against the stored oracle values."""
+    ans = stored_answers(name)
+    if ans is None:
+        return False, "no stored oracle answer for this workload"
+    ref = ans["items"]
+    if max_items:
+        ref = ref[: len(out)] if not ans["sliced"] else None
+        if ref is None:
+            return False, "a --max-items run of a sliced workload samples other slices"
+    if len(ref) != len(out):
+        return False, f"{len(out)} items, {len(ref)} stored"
+    bad = int(np.sum(np.asarray(out, np.float64) != np.asarray(ref, np.float64)))
+    if bad:
+        raise AssertionError(f"{name}: {bad} of {len(out)} item values differ from the oracle's")
+    return True, f"all {len(out)} item values equal the oracle's (tests/golden/workload_answers.json)"
+
+
+def workload_config(wl, name):
+    """The workload as both arms describe it (no engine settings)."""
+    br = next(x for x in wl["branches"] if x.code is not None)
+    code = br.code.remove_labels(wl["sliced"]) if wl["sliced"] else br.code
+    tc, sc, rwc = code.complexity()
+    from tensorbranching_gb300 import workloads
+
+    items = workloads.step_items(wl)
+    return {"workload": name, "detail": _desc(name), "items_per_step": len(items),
+            "graphs_per_step": expected_answer(wl), "tc": tc, "sc": sc, "rwc": rwc,
+            "sliced_labels": len(wl["sliced"]), "l2": "flushed between steps (256 MiB write)"}
+
+
+def level_roofline(prof, simt, hbm, simt_i16=None):
+    """Per-kernel roofline from a per-launch profile: the GEMM-tile launches
+    (k_level<float, 2>) against the SIMT max-plus peak of their form, the
+    stream-tile launches (k_level<float, 1>) against HBM; the dominant kernel
+    is the one with the larger share of device time."""
+    tot = sum(p["ms"] for p in prof) or 1e-9
+    out = {}
+    for kind, name in (("gemm", "k_level<float,2> (GEMM tiles)"), ("stream", "k_level<float,1> (stream tiles)")):
+        ps = [p for p in prof if p["kind"] == kind]
+        if not ps:
+            continue
+        t = sum(p["ms"] for p in ps) / 1000.0
+        o = sum(p["ops"] for p in ps)
+        b = sum(p["bytes"] for p in ps)
+        if kind == "gemm":
+            peak = simt_i16 if simt_i16 else simt
+            out[kind] = {"kernel": name, "launches": len(ps), "share": t * 1000.0 / tot, "bound": "simt",
+                         "achieved": o / t / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                         "frac": o / t / peak, "ms": t * 1000.0, "algorithmic_ops": o}
+        else:
+            out[kind] = {"kernel": name, "launches": len(ps), "share": t * 1000.0 / tot, "bound": "hbm",
+                         "achieved": b / t / 1e9, "peak": hbm, "unit": "GB/s", "frac": b / t / (hbm * 1e9),
+                         "ms": t * 1000.0, "algorithmic_bytes": b}
+    return out
+
+
+def measure(tb, eng, wl, name, args, steps, warmup, plain_steps, flush, dev, ws, simt, simt_i16, hbm, peak_kind,
+            with_profile=True):
+    """Time one workload on one engine: the device-timed step (inputs
+    resident, L2 flushed between steps), the end-to-end step through the
+    public API (host weights bound, results read back), the per-launch
+    roofline and the plain drop-in path on the same items."""
+    import torch
+
+    plans, svs, rs = make_items(eng, wl, tb, args.max_items)
+    units = expected_answer(wl)
+    if args.tile_bits:
+        for p in {id(p): p for p in plans}.values():
+            eng.retile(p, args.tile_bits)
+    uniq = {id(p): p for p in plans}
+    ops = sum(p.stats()["ops"] for p in plans)
+    tuned = eng.autotune(plans, slice_vals=svs, r=rs) if args.mode == "auto" else None
+    mode = tuned["mode"] if tuned else args.mode
+    out0, mx0 = eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
+    checked, note = check_answer(name, out0, args.max_items)
+
+    def step():
+        return eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
+
+    for _ in range(warmup):
+        step()
+    dev_ms, launches = [], 0
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            o, m = step()
+            ms, nl = eng.last_timing()
+            dev_ms.append(ms)
+            launches += nl
+            if not np.array_equal(o, out0):
+                raise AssertionError(f"{name}: a timed step's item values changed")
+    torch.cuda.synchronize()
+    t_dev = sum(dev_ms) / 1000.0
+    # e2e: bind weights from host (H2D) + solve + result read-back (D2H), wall clock
+    uplans = list(uniq.values())
+    h2d = sum(4 * p.code.n_labels for p in uplans) + 4 * len(plans) + (sum(len(x) for x in svs) if svs else 0)
+    d2h = 4 * (len(plans) + 1)
+    host_w = [np.ascontiguousarray(_weights_of(wl, p), np.float32) for p in uplans]
+    w_offs = np.zeros(len(uplans), np.int64)
+    if len(uplans) > 1:
+        w_offs[1:] = np.cumsum([len(w) for w in host_w[:-1]])
+    w_flat = np.ascontiguousarray(np.concatenate(host_w), np.float32)  # the caller's host buffer
+    if ws > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        eng.bind_batch(uplans, w_flat, w_offs)
+        o, m = step()
+        if not np.array_equal(o, out0):
+            raise AssertionError(f"{name}: an end-to-end step's item values changed")
+    t_e2e = time.perf_counter() - t0
+    if ws > 1:
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    ms_per_step = 1000.0 * t_dev / steps
+    t_step = ms_per_step / 1000.0
+    i16 = eng.gemm_arith == "i16x2" and _gemm_arith(wl) != "f32"
+    r_ops, r_bytes, t_simt, t_hbm, t_bound = roofline(plans, t_step, simt, hbm, simt_i16 if i16 else None)
+    res = {"value": ws * steps * units / t_dev, "unit": "solves/s", "ms_per_step": ms_per_step,
+           "dtype": "int16x2 (exact: integer weights >= 0 summing below 8192)" if i16 else "f32",
+           "mode": mode, "autotune": tuned, "answer": mx0, "answer_checked": checked, "answer_note": note,
+           "tropical_gops": ops / t_step / 1e9, "gpu_launches": launches,
+           "items_per_s": ws * steps * len(plans) / t_dev,
+           "e2e": {"value": ws * steps * units / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h},
+           "clocks": clk.summary()}
+    # the step as a whole against the node-weighted roofline
+    step_roof = {"attainable_frac": t_bound / t_step, "algorithmic_ops": r_ops, "algorithmic_bytes": r_bytes}
+    if t_simt >= t_hbm:
+        step_roof.update({"bound": "simt", "achieved": r_ops / t_step / 1e12, "peak": r_ops / t_simt / 1e12,
+                          "unit": "TFLOP/s", "frac": t_simt / t_step})
+    else:
+        step_roof.update({"bound": "hbm", "achieved": r_bytes / t_step / 1e9, "peak": hbm, "unit": "GB/s",
+                          "frac": r_bytes / t_step / (hbm * 1e9)})
+    res["step_roofline"] = step_roof
+    if with_profile and mode == "layered":
+        # per-launch device times of the same schedule (CUDA events on the
+        # engine's stream, L2 flushed before each of three runs)
+        runs = []
+        for _ in range(3):
+            flush.zero_()
+            torch.cuda.synchronize()
+            runs.append(eng.profile_levels(plans, slice_vals=svs, r=rs))
+        prof = [dict(p, ms=float(np.mean([r[k]["ms"] for r in runs]))) for k, p in enumerate(runs[0])]
+        res["kernels"] = level_roofline(prof, simt, hbm, simt_i16 if i16 else None)
+    if plain_steps > 0:
+        # the drop-in path on the same items: one item at a time, per-node
+        # launches (permute + K1 GEMM + permute), a result read-back per item.
+        # It runs the items one after another, so a strided sample of at most
+        # PLAIN_MAX_ITEMS of them, scaled by the item count, times the step.
+        n = len(plans)
+        stride = -(-n // PLAIN_MAX_ITEMS)
+        idx = list(range(0, n, stride))
+        p_s = [plans[i] for i in idx]
+        sv_s = [svs[i] for i in idx] if svs is not None else None
+        pl_ms = 0.0
+        for _ in range(plain_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            o, m = eng.solve_batch(p_s, slice_vals=sv_s, r=rs[idx], mode="plain")
+            if not np.array_equal(o, out0[idx]):
+                raise AssertionError(f"{name}: the plain path's item values differ")
+            pl_ms += eng.last_timing()[0] * n / len(idx)
+        pv = plain_steps * units / (pl_ms / 1000.0)
+        res["plain"] = {"value": pv, "unit": "solves/s", "ms_per_step": pl_ms / plain_steps, "steps": plain_steps,
+                        "items_timed": len(idx), "items": n, "speedup_vs_plain": res["value"] / pv,
+                        "note": "items timed one after another, the per-item device time scaled to the step's "
+                                "item count" if len(idx) < n else "every item of the step"}
+    return res, plans
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -314,9 +475,15 @@ def main():
     ap.add_argument("--config", default="rr220")
     ap.add_argument("--mode", default="auto", choices=["auto", "batched", "layered", "plain", "fused"],
                     help="auto: tb_autotune picks tile size and schedule before the warm-up (untimed)")
+    ap.add_argument("--gemm-arith", default="f32", choices=["f32", "i16x2"],
+                    help="arithmetic of the headline's GEMM tiles (f32: the reference's Float32)")
+    ap.add_argument("--configs", default=EXTRA_CONFIGS,
+                    help="further workloads timed in the same run and reported under 'configs' ('' for none)")
+    ap.add_argument("--config-steps", type=int, default=5)
+    ap.add_argument("--no-i16", action="store_true", help="skip the packed-int16 GEMM form of the headline")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain drop-in comparison")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--compare-plain", action="store_true")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--make", nargs="*")
     ap.add_argument("--max-items", type=int, default=0,
@@ -346,6 +513,8 @@ def main():
     wl = load_workload(tb, args.config)
     if args.max_items and not wl["sliced"]:
         wl["truncated"] = True  # a subset of the branches answers no whole solve
+        wl["branches"] = [b for b in wl["branches"] if b.code is not None][: args.max_items]
+    cfg = workload_config(wl, args.config)
     units = expected_answer(wl)
 
     if args.impl == "reference":
@@ -362,10 +531,9 @@ def main():
         out = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * units / v,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-               "data": "synthetic (seeded graphs)",
-               "config": {"workload": args.config, "detail": _desc(args.config)},
+               "data": "synthetic (seeded graphs, weights as described)", "config": cfg,
                "cpu_baseline": {"value": v, "unit": "solves/s", "cores": r["cores"], "kind": "port",
-                                "sample": r["sample"]},
+                                "sample": r["sample"], "cpu": _cpu_model()},
                "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return
@@ -379,145 +547,103 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
-    eng = tb.Engine(device=dev, use_graphs=not args.no_graphs)
-    if args.max_items:
-        wl["branches"] = [b for b in wl["branches"] if b.code is not None][: args.max_items]
-    plans, svs, rs = make_items(eng, wl, tb, args.max_items)
-    units = expected_answer(wl)
-    if args.tile_bits:
-        for p in {id(p): p for p in plans}.values():
-            eng.retile(p, args.tile_bits)
-    st = plans[0].stats()
-    uniq = {id(p): p for p in plans}
-    ops = sum(uniq[k].stats()["ops"] for k in uniq) if not wl["sliced"] else st["ops"] * len(plans)
-    byts = sum(uniq[k].stats()["bytes"] for k in uniq) if not wl["sliced"] else st["bytes"] * len(plans)
-    tuned = None
-    if args.mode == "auto":
-        tuned = eng.autotune(plans, slice_vals=svs, r=rs)
-    # check the answer once
-    out0, mx0 = eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
-    from tensorbranching_gb300.engine import measure_maxplus_peak
+    from tensorbranching_gb300.engine import measure_maxplus_peak, measure_maxplus_peak_i16
 
     simt = measure_maxplus_peak(dev)
-    from tensorbranching_gb300.engine import measure_maxplus_peak_i16
-
     simt_i16 = measure_maxplus_peak_i16(dev)
+    hbm, peak_kind = _peaks()
     # L2 flush buffer (larger than the 129 MB L2)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")
-
-    def step():
-        return eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
-
-    for _ in range(args.warmup):
-        step()
-    # device-timed region: inputs resident, L2 flushed between steps
-    dev_ms = []
-    launches = 0
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            o, m = step()
-            ms, nl = eng.last_timing()
-            dev_ms.append(ms)
-            launches += nl
-            assert m == mx0
-    torch.cuda.synchronize()
-    t_dev = sum(dev_ms) / 1000.0
-    # e2e: bind weights from host (H2D) + solve + result read-back (D2H), wall clock
-    uplans = list(uniq.values())
-    # per step: the bound weights of every distinct plan, r and slice values
-    h2d = sum(4 * p.code.n_labels for p in uplans) + 4 * len(plans) + (sum(len(x) for x in svs) if svs else 0)
-    d2h = 4 * (len(plans) + 1)
-    host_w = [np.ascontiguousarray(_weights_of(wl, p), np.float32) for p in uplans]
-    w_offs = np.zeros(len(uplans), np.int64)
-    if len(uplans) > 1:
-        w_offs[1:] = np.cumsum([len(w) for w in host_w[:-1]])
-    w_flat = np.ascontiguousarray(np.concatenate(host_w), np.float32)  # the caller's host buffer
-    if ws > 1:
-        torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        eng.bind_batch(uplans, w_flat, w_offs)
-        o, m = step()
-        assert m == mx0
-    t_e2e = time.perf_counter() - t0
-    if ws > 1:
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=f"cuda:{dev}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    eng = tb.Engine(device=dev, use_graphs=not args.no_graphs, gemm_arith=args.gemm_arith)
+    head, plans = measure(tb, eng, wl, args.config, args, args.steps, args.warmup,
+                          0 if args.no_plain or args.mode == "plain" else min(args.steps, 3), flush, dev, ws, simt,
+                          simt_i16, hbm, peak_kind)
+    extra = {}
+    if rank == 0 and not args.no_i16 and args.gemm_arith == "f32" and _gemm_arith(wl) != "f32":
+        # the same workload with the exact packed-int16 GEMM tiles
+        eng16 = tb.Engine(device=dev, use_graphs=not args.no_graphs, gemm_arith="i16x2")
+        r16, _ = measure(tb, eng16, load_workload(tb, args.config) if not args.max_items else wl, args.config, args,
+                         args.steps, args.warmup, 0, flush, dev, 1, simt, simt_i16, hbm, peak_kind)
+        eng16.close()
+        extra["i16x2"] = {k: r16[k] for k in ("value", "unit", "ms_per_step", "dtype", "answer_checked", "e2e",
+                                               "step_roofline", "kernels", "mode") if k in r16}
+    configs = {}
+    if rank == 0 and ws == 1 and args.configs and not args.max_items:
+        for nm in [x for x in args.configs.split(",") if x and x != args.config]:
+            try:
+                wl2 = load_workload(tb, nm)
+            except FileNotFoundError as ex:
+                configs[nm] = {"unavailable": str(ex)}
+                continue
+            e2 = tb.Engine(device=dev, use_graphs=not args.no_graphs, gemm_arith=args.gemm_arith)
+            r2, _ = measure(tb, e2, wl2, nm, args, args.config_steps, 3, 0 if args.no_plain else 1, flush, dev, 1,
+                            simt, simt_i16, hbm, peak_kind)
+            e2.close()
+            r2["config"] = workload_config(wl2, nm)
+            r2.pop("clocks", None)
+            configs[nm] = r2
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
-    value = ws * args.steps * units / t_dev
-    ms_per_step = 1000.0 * t_dev / args.steps
-    hbm, peak_kind = _peaks()
-    t_step = ms_per_step / 1000.0
-    gemm_arith = _gemm_arith(wl)
-    r_ops, r_bytes, t_simt, t_hbm, t_bound = roofline(plans, t_step, simt, hbm,
-                                                      simt_i16 if gemm_arith != "f32" else None)
-    traffic = _profiled_traffic(args.config, args.mode)
-    if t_simt >= t_hbm:
-        # peak = the ops-weighted ceiling of the step's nodes: the measured f32
-        # max-plus rate, or the packed-int16 one for GEMM nodes in that form
-        roof = {"bound": "simt", "achieved": r_ops / t_step / 1e12, "peak": r_ops / t_simt / 1e12,
-                "unit": "TFLOP/s", "frac": t_simt / t_step, "peak_f32": simt / 1e12}
+    gk = head.get("kernels", {})
+    dom = max(gk.values(), key=lambda k: k["share"]) if gk else None
+    if dom is not None:
+        roof = {k: dom[k] for k in ("bound", "achieved", "peak", "unit", "frac")}
+        roof.update({"kernel": dom["kernel"], "share_of_step": dom["share"]})
     else:
-        roof = {"bound": "hbm", "achieved": r_bytes / t_step / 1e9, "peak": hbm, "unit": "GB/s",
-                "frac": r_bytes / t_step / (hbm * 1e9)}
-    roof.update({
-        "peak_i16x2": simt_i16 / 1e12,
-        "traffic": traffic, "attainable_frac": t_bound / t_step,
-        "peak_source": f"simt: measured f32 max-plus probe on this GPU ({simt / 1e12:.2f} Tops); packed-int16 "
-                       f"max-plus probe {simt_i16 / 1e12:.2f} Tops (the GEMM tiles' ceiling when they run that "
-                       f"form; used per node in attainable_frac); hbm: {peak_kind} copy bandwidth ({hbm:.0f} GB/s)",
-        "note": "dominant kernel k_persistent (batched) / k_level (layered) / k_small (fused: tensors stay in "
-                "shared memory, so the HBM fraction is nominal) runs the whole step; achieved = "
-                "algorithmic tropical ops 2*2^|L| (max and add; SIMT, no tensor cores) or bytes "
-                "4(|A|+|B|+|C|) summed over nodes / device time of the step; a node's compute ceiling is the "
-                "measured f32 max-plus rate, or the packed-int16 rate for GEMM nodes run in that form; "
-                "attainable_frac = sum over nodes of max(ops/P_node, bytes/BW) / device time"})
+        sr = head["step_roofline"]
+        roof = {k: sr[k] for k in ("bound", "achieved", "peak", "unit", "frac")}
+        roof["kernel"] = {"fused": "k_small", "batched": "k_persistent"}.get(head["mode"], head["mode"])
+        roof["share_of_step"] = 1.0
+    roof["traffic"], roof["traffic_source"] = _profiled_traffic(args.config, head["mode"], head["dtype"])
+    roof["peak_source"] = (f"simt: measured f32 max-plus probe on this GPU ({simt / 1e12:.2f} Tops; the packed-int16 "
+                           f"probe {simt_i16 / 1e12:.2f} Tops is the ceiling of int16x2 GEMM tiles); hbm: "
+                           f"{peak_kind} copy bandwidth ({hbm:.0f} GB/s)")
+    roof["note"] = ("achieved = algorithmic tropical ops 2*2^|L| (max and add; SIMT, no tensor cores) or bytes "
+                    "4(|A|+|B|+|C|) of the nodes the kernel's launches run / their device time (CUDA events per "
+                    "launch on the engine's stream); kernels: every kernel of the step with its share")
     res = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded graphs, weights as described)",
-        "config": {"workload": args.config, "detail": _desc(args.config), "mode": args.mode,
-                   "items_per_step": len(plans), "graphs_per_step": units, "tc": st["tc"], "sc": st["sc"],
-                   "rwc": st["rwc"], "l2": "flushed between steps (256 MiB write)",
-                   "answer": mx0, "parallelism": f"replicas x{ws}", "autotune": tuned,
-                   "gemm_arithmetic": gemm_arith,
-                   "resident_ctas": eng.info()},
-        "tropical_gops": ops / (ms_per_step / 1000.0) / 1e9,
-        "roofline": roof,
-        "e2e": {"value": ws * args.steps * units / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "metric": METRIC, "value": head["value"], "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": head["dtype"], "data": "synthetic (seeded graphs, weights as described)",
+        "config": cfg,
+        "engine": {"mode": head["mode"], "autotune": head["autotune"], "gemm_arithmetic": head["dtype"],
+                   "resident_ctas": eng.info(), "parallelism": f"replicas x{ws}"},
+        "answer": head["answer"], "answer_checked": head["answer_checked"], "answer_note": head["answer_note"],
+        "tropical_gops": head["tropical_gops"],
+        "roofline": roof, "kernels": gk, "step_roofline": head["step_roofline"],
+        "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
     }
-    if args.compare_plain and args.mode != "plain":
-        # the drop-in path on the same items: one item at a time, per-node launches
-        t0 = time.perf_counter()
-        n_pl = max(1, min(args.steps, 3))
-        pl_ms = 0.0
-        for _ in range(n_pl):
-            flush.zero_()
-            torch.cuda.synchronize()
-            o, m = eng.solve_batch(plans, slice_vals=svs, r=rs, mode="plain")
-            assert m == mx0
-            pl_ms += eng.last_timing()[0]
-        plain_value = n_pl * units / (pl_ms / 1000.0)
-        res["plain"] = {"value": plain_value, "unit": "solves/s", "ms_per_step": pl_ms / n_pl,
-                        "speedup_vs_plain": value / plain_value}
+    if "plain" in head:
+        res["plain"] = head["plain"]
+        res["speedup_vs_plain"] = head["plain"]["speedup_vs_plain"]
+    res.update(extra)
+    if configs:
+        res["configs"] = configs
     if not args.no_cpu_baseline:
         orc = _ge.load_oracle()
         orc.build()
-        res["cpu_baseline"] = run_cpu_baseline(tb, orc, wl, args.cpu_budget)
+        cb = run_cpu_baseline(tb, orc, wl, args.cpu_budget)
+        cb1 = run_cpu_baseline(tb, orc, wl, args.cpu_budget / 2, threads=1)
+        orc.set_threads(0)
+        cb["cpu"] = _cpu_model()
+        cb["single_thread"] = {"value": cb1["value"], "cores": 1, "sample": cb1["sample"]}
+        res["cpu_baseline"] = cb
     print(json.dumps(res))
+    eng.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip() + f" ({os.cpu_count()} cores)"
+    except Exception:
+        pass
+    return f"{os.cpu_count()} cores"
 
 
 def run_serve(tb, args):
@@ -577,15 +703,19 @@ def _weights_of(wl, plan):
     return wl["plan_weights"][id(plan)]
 
 
-def _profiled_traffic(config, mode):
+def _profiled_traffic(config, mode, dtype):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary, if one exists for this workload (line 'traffic_bytes_per_step: X')."""
-    p = os.path.join(ROOT, "profiles", f"traffic_{config}_{mode}.txt")
+    summary for this workload and form (profiles/traffic_<config>_<mode>
+    [_i16].txt, line 'traffic_bytes_per_launch: X'), and the file's name;
+    (None, reason) when no capture exists."""
+    sfx = "_i16" if dtype.startswith("int16") else ""
+    nm = f"traffic_{config}_{mode}{sfx}.txt"
+    p = os.path.join(ROOT, "profiles", nm)
     if os.path.exists(p):
         for line in open(p):
-            if line.startswith("traffic_bytes_per_step:"):
-                return float(line.split(":")[1])
-    return None
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1]), f"profiles/{nm}"
+    return None, f"no ncu capture committed as profiles/{nm}"
 
 
 def _desc(name):

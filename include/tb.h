@@ -88,7 +88,13 @@ typedef struct tb_options {
   int32_t timeout_ms;       /* bound on every device-side wait (default 20000) */
   int32_t autotune;         /* 1: the first TB_MODE_AUTO solve runs tb_autotune */
   int32_t persistent_ctas;  /* CTAs of the persistent executor; 0 = 2 per SM */
-  int32_t reserved[9];
+  int32_t gemm_i16;         /* 0 (default): every contraction computes in the
+                               context's dtype.  1 (TB_DTYPE_F32 only): GEMM tiles
+                               of a plan whose bound weights are integers >= 0
+                               summing below 8192 compute in packed int16 pairs
+                               (exact for such values: same results, twice the
+                               SIMT rate); other plans stay f32 */
+  int32_t reserved[8];
 } tb_options;
 
 typedef struct tb_plan_stats {

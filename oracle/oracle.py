@@ -48,6 +48,10 @@ def lib():
             f = getattr(_lib, f"or_einsum_gemm_{sfx}")
             f.restype = c_int
             f.argtypes = [c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+            _lib.or_set_threads.restype = None
+            _lib.or_set_threads.argtypes = [c_int]
+            _lib.or_get_threads.restype = c_int
+            _lib.or_get_threads.argtypes = []
             f = getattr(_lib, f"or_execute_{sfx}")
             f.restype = c_int
             f.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int,
@@ -56,6 +60,13 @@ def lib():
 
 
 I32_NEG = -536870912
+
+
+def set_threads(n: int = 0) -> int:
+    """OpenMP threads of later oracle calls (0: every host core); returns the
+    count now in effect."""
+    lib().or_set_threads(int(n))
+    return int(lib().or_get_threads())
 
 
 def _i(a):

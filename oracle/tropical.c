@@ -35,6 +35,7 @@
  * accumulator starting at the sentinel, so sums never overflow).
  */
 #include <math.h>
+#include <omp.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -366,3 +367,10 @@ fail:
   free(buf); free(labs); free(nlab); free(refs);
   return rc;
 }
+
+#ifndef OR_I32
+/* OpenMP threads of every later call (the benchmark's single-thread and
+ * all-core CPU baselines); n <= 0 restores every host core. */
+void or_set_threads(int n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
+int or_get_threads(void) { return omp_get_max_threads(); }
+#endif

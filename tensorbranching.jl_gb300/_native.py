@@ -38,7 +38,8 @@ class TbOptions(ctypes.Structure):
         ("timeout_ms", c_int32),
         ("autotune", c_int32),
         ("persistent_ctas", c_int32),
-        ("reserved", c_int32 * 9),
+        ("gemm_i16", c_int32),
+        ("reserved", c_int32 * 8),
     ]
 
 

@@ -79,8 +79,11 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
       if ((KINDS & 1) && st.kind == STEP_TILE) {
         stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err);
       } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
-        gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err,
-                          (it.flags & 1) != 0);
+        // a timed-out copy wait (err set) may leave copies in flight into this
+        // CTA's shared memory: use it no further
+        if (!gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err,
+                               (it.flags & 1) != 0))
+          return;
       } else {
         for (int64_t x = tk; x < g_end; x++) run_small_step<T>(it, st, x - g.first, out_item, r, g.item);
       }
@@ -137,7 +140,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
     if (st.kind == STEP_TILE) {
       stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
     } else if (st.kind == STEP_GEMM) {
-      gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0);
+      if (!gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0))
+        return;  // err is set; copies may still be landing in this CTA's shared memory
     } else {
       for (int64_t x = ch.t0; x < ch.t1; x++) run_small_step<T>(it, st, x, out_item, r, g.item);
     }
@@ -243,11 +247,8 @@ template <typename T, int BM, int BN>
 inline cudaError_t launch_k1(const T* A, const T* B, T* C, int64_t M, int64_t N, int64_t K, int64_t batch,
                              cudaStream_t s) {
   using Cfg = K1Cfg<T, BM, BN>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(gemm_k1<T, BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES);
-    attr = true;
-  }
+  cudaError_t e = smem_optin(reinterpret_cast<const void*>(gemm_k1<T, BM, BN>), Cfg::SMEM_BYTES);
+  if (e != cudaSuccess) return e;
   int64_t tiles_mn = (M / BM) * (N / BN);
   int64_t grid = tiles_mn * batch;
   if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
@@ -277,12 +278,8 @@ inline cudaError_t dispatch_k1(const T* A, const T* B, T* C, int64_t M, int64_t 
 template <typename T>
 cudaError_t launch_small(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const int32_t* order,
                          int n, float* out_item, const float* r) {
-  static int attr = 0;  // dynamic shared bytes the kernel is opted in for
-  if (smem > attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = smem;
-  }
+  cudaError_t e = smem_optin(reinterpret_cast<const void*>(k_small<T>), smem);
+  if (e != cudaSuccess) return e;
   k_small<T><<<grid, kSmallThreads, smem, s>>>(items, order, n, out_item, r);
   return cudaGetLastError();
 }
@@ -296,13 +293,8 @@ cudaError_t launch_leaves(unsigned grid, cudaStream_t s, const LeafDesc* leaves,
 
 template <typename T>
 cudaError_t launch_tile(unsigned grid, int smem, cudaStream_t s, const TileDesc& d, T* arena, int64_t chunk) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         stream_smem_words_max() * 4);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = smem_optin(reinterpret_cast<const void*>(k_tile<T>), stream_smem_words_max() * 4);
+  if (e != cudaSuccess) return e;
   k_tile<T><<<grid, kThreads, smem, s>>>(d, arena, chunk);
   return cudaGetLastError();
 }
@@ -321,13 +313,7 @@ cudaError_t launch_k1_any(const T* A, const T* B, T* C, int64_t M, int64_t N, in
 
 template <typename T, int KINDS>
 static cudaError_t level_attr(int smem) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_level<T, KINDS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  return cudaSuccess;
+  return smem_optin(reinterpret_cast<const void*>(k_level<T, KINDS>), smem);
 }
 
 template <typename T, int KINDS>
@@ -349,13 +335,7 @@ cudaError_t occupancy_level(int* per_sm, int smem) {
 
 template <typename T>
 static cudaError_t persistent_attr(int smem) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  return cudaSuccess;
+  return smem_optin(reinterpret_cast<const void*>(k_persistent<T>), smem);
 }
 
 template <typename T>

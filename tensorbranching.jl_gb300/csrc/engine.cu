@@ -172,6 +172,21 @@ static tb_status fail(tb_status s, const std::string& msg) {
 namespace tb {
 // Lets other translation units of the library report through tb_last_error.
 void set_last_error(const std::string& msg) { g_err = msg; }
+
+cudaError_t smem_optin(const void* fn, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> opted;  // (kernel, device) -> bytes
+  std::lock_guard<std::mutex> lk(mu);
+  int& have = opted[{fn, dev}];
+  if (bytes <= have) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  have = bytes;
+  return cudaSuccess;
+}
 }  // namespace tb
 
 #define CU(x)                                                                                   \
@@ -303,9 +318,9 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
     it.slice_vals = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
     it.w = w_off ? reinterpret_cast<const float*>(c->wvals.p) + (*w_off)[i] : nullptr;
-    // exact packed-int16 GEMM tiles only where the per-call weights are the
-    // plan's bound ones (the batched solves)
-    it.flags = (w_off && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
+    // exact packed-int16 GEMM tiles only when the context allows them and
+    // the per-call weights are the plan's bound ones (the batched solves)
+    it.flags = (c->opt.gemm_i16 && w_off && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = done_base;
@@ -417,6 +432,29 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   return TB_OK;
 }
 
+// One launch of the per-level schedule: every tile of one (tree level,
+// kind) of the uploaded batch.
+template <typename T>
+static tb_status enqueue_level(tb_ctx* c, const tb_ctx::LevelRange& lr) {
+  const ItemDev<T>* items = reinterpret_cast<const ItemDev<T>*>(c->items.p);
+  const Group* groups = reinterpret_cast<const Group*>(c->groups.p);
+  float* out_item = reinterpret_cast<float*>(c->out_item.p);
+  const float* rv = reinterpret_cast<const float*>(c->rvals.p);
+  int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
+  if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
+  if (lr.kinds == 2) {
+    const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
+    CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, groups, c->n_groups, lr.first,
+                           lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv, err)));
+  } else {
+    const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
+    CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, groups, c->n_groups, lr.first,
+                           lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv, err)));
+  }
+  CU(cudaGetLastError());
+  return TB_OK;
+}
+
 template <typename T>
 static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int64_t& launches) {
   cudaStream_t s = c->stream;
@@ -444,21 +482,9 @@ static tb_status enqueue_batched(tb_ctx* c, int n, int mode, int done_words, int
     CU(cudaGetLastError());
     launches++;
   } else {
-    int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
     for (auto& lr : c->level_ranges) {
-      if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
-      if (lr.kinds == 2) {
-        const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-        CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), s, 
-            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv,
-            err)));
-      } else {
-        const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-        CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, 
-            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv,
-            err)));
-      }
-      CU(cudaGetLastError());
+      tb_status st = enqueue_level<T>(c, lr);
+      if (st) return st;
       launches++;
     }
   }
@@ -1551,6 +1577,85 @@ extern "C" int32_t tbi_timeout_probe(tb_ctx* c, tb_plan* p, int32_t timeout_ms) 
   c->have_key = false;
   if (e == TB_ERR_TIMEOUT) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
   return e ? fail(TB_ERR_CUDA, "unexpected device error word") : TB_OK;
+}
+
+// Per-launch profile of the per-level schedule (for the benchmark's
+// roofline): solves the batch once in TB_MODE_LAYERED, then runs its level
+// launches again without a graph, with a CUDA event after each, on the
+// context's stream.  Per launch k < *n_out: device milliseconds, kind (1
+// stream tiles with leaves / final steps, 2 GEMM tiles) and the algorithmic
+// tropical ops (2 2^|L| per node) and bytes (4 (|A|+|B|+|C|) per node) of the
+// contraction steps it runs (K-split max steps count none).  The batch must
+// fit the context's budget in one wave.
+template <typename T>
+static tb_status profile_levels_t(tb_ctx* c, int n, tb_plan* const* plans, const int8_t* sv, const float* r,
+                                  int cap, double* ms, int32_t* kinds, double* ops, double* bytes, int32_t* n_out) {
+  tb_status st = solve_batch_t<T>(c, n, plans, sv, r, nullptr, nullptr, TB_MODE_LAYERED);
+  if (st) return st;
+  if (!c->have_key || c->n_items != n) return fail(TB_ERR_UNSUPPORTED, "the batch ran in waves");
+  const int L = (int)c->level_ranges.size();
+  if (L > cap) return fail(TB_ERR_INVALID, "more level launches than cap");
+  std::vector<cudaEvent_t> ev(L + 1, nullptr);
+  auto destroy = [&]() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  };
+  for (auto& e : ev) {
+    cudaError_t ce = cudaEventCreate(&e);
+    if (ce != cudaSuccess) {
+      destroy();
+      return fail(TB_ERR_CUDA, cudaGetErrorString(ce));
+    }
+  }
+  cudaError_t ce = cudaMemsetAsync(c->misc.p, 0, 64, c->stream);
+  if (ce == cudaSuccess) ce = cudaEventRecord(ev[0], c->stream);
+  for (int k = 0; k < L && ce == cudaSuccess && st == TB_OK; k++) {
+    st = enqueue_level<T>(c, c->level_ranges[k]);
+    if (st == TB_OK) ce = cudaEventRecord(ev[k + 1], c->stream);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+  if (st || ce != cudaSuccess) {
+    destroy();
+    return st ? st : fail(TB_ERR_CUDA, cudaGetErrorString(ce));
+  }
+  const Group* hg = reinterpret_cast<const Group*>(c->h_groups.p);
+  int g = 0;
+  for (int k = 0; k < L; k++) {
+    const auto& lr = c->level_ranges[k];
+    float t = 0;
+    cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+    ms[k] = t;
+    kinds[k] = lr.kinds;
+    ops[k] = bytes[k] = 0;
+    for (; g < c->n_groups && hg[g].first < lr.first + lr.count; g++) {
+      const PlanHost& h = plans[hg[g].item]->h;
+      const int sn = h.step_node[hg[g].step];
+      if (sn >= 0) {
+        ops[k] += h.node_ops[sn];
+        bytes[k] += h.node_bytes[sn];
+      }
+    }
+  }
+  destroy();
+  *n_out = L;
+  int err = 0;
+  CU(cudaMemcpy(&err, reinterpret_cast<char*>(c->misc.p) + 16, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
+  return TB_OK;
+}
+
+extern "C" int32_t tbi_profile_levels(tb_ctx* c, int32_t n, tb_plan* const* plans, const int8_t* sv,
+                                      const float* r, int32_t cap, double* ms, int32_t* kinds, double* ops,
+                                      double* bytes, int32_t* n_out) {
+  if (!c || n <= 0 || !plans || !ms || !kinds || !ops || !bytes || !n_out) return fail(TB_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  try {
+    return c->opt.dtype == TB_DTYPE_F32
+               ? profile_levels_t<float>(c, n, plans, sv, r, cap, ms, kinds, ops, bytes, n_out)
+               : profile_levels_t<int32_t>(c, n, plans, sv, r, cap, ms, kinds, ops, bytes, n_out);
+  } catch (const std::exception& ex) {
+    return fail(TB_ERR_INVALID, std::string("internal: ") + ex.what());
+  }
 }
 
 // Measured packed-int16 max-plus rate (ops/s, a max and an add per MAC).

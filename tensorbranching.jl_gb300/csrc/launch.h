@@ -10,6 +10,11 @@
 
 namespace tb {
 
+// Opt kernel `fn` in to `bytes` of dynamic shared memory on the current
+// device.  The attribute is per device, so the state is kept per (kernel,
+// device) and raised when a launch asks for more; thread-safe (engine.cu).
+cudaError_t smem_optin(const void* fn, int bytes);
+
 template <typename T>
 cudaError_t launch_leaves(unsigned grid, cudaStream_t s, const LeafDesc* leaves, int n, const int8_t* sv, T* arena,
                           const float* w);

@@ -389,6 +389,8 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
   p.arena_elems = fused_end;
   // complexity model
   p.tc = -INFINITY; p.sc = 0; p.rwc = -INFINITY; p.ops = 0; p.bytes = 0;
+  p.node_ops.assign(in.n_nodes, 0.0);
+  p.node_bytes.assign(in.n_nodes, 0.0);
   for (int i = 0; i < total; i++) p.sc = std::max(p.sc, (double)p.labels[i].size());
   for (int j = 0; j < in.n_nodes; j++) {
     int me = T + j, a = p.children[2 * j], b = p.children[2 * j + 1];
@@ -400,9 +402,11 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
     double rw = log2sumexp2(log2sumexp2((double)p.labels[a].size(), (double)p.labels[b].size()),
                             (double)p.labels[me].size());
     p.rwc = log2sumexp2(p.rwc, rw);
-    p.ops += 2.0 * std::exp2(t);
-    p.bytes += 4.0 * (std::exp2((double)p.labels[a].size()) + std::exp2((double)p.labels[b].size()) +
-                      std::exp2((double)p.labels[me].size()));
+    p.node_ops[j] = 2.0 * std::exp2(t);
+    p.node_bytes[j] = 4.0 * (std::exp2((double)p.labels[a].size()) + std::exp2((double)p.labels[b].size()) +
+                             std::exp2((double)p.labels[me].size()));
+    p.ops += p.node_ops[j];
+    p.bytes += p.node_bytes[j];
   }
   if (in.n_nodes == 0) {
     p.tc = (double)p.labels[0].size();

@@ -63,6 +63,7 @@ struct PlanHost {
   std::vector<std::vector<PlainOp>> plain;     // per node, in post-order
 
   double tc = 0, sc = 0, rwc = 0, ops = 0, bytes = 0;
+  std::vector<double> node_ops, node_bytes;    // algorithmic work of each node: 2 2^|L|, 4 (|A|+|B|+|C|)
   int64_t total_tiles = 0;
   int32_t tile_bits = 9;                       // stream tiles grow to 2^tile_bits outputs
   int32_t gemm_ctas = 304;                     // resident GEMM CTAs the K split balances for

@@ -30,6 +30,7 @@
 
 #include "../../include/tb.h"
 #include "kernels.cuh"
+#include "launch.h"
 #include "plan.h"
 
 namespace tb {
@@ -76,8 +77,7 @@ template <int BM, int BN>
 cudaError_t ks_k1(const float* A, const float* B, float* C, int64_t M, int64_t N, int64_t K, int64_t batch,
                   cudaStream_t s) {
   using Cfg = K1Cfg<float, BM, BN>;
-  cudaError_t e = cudaFuncSetAttribute(gemm_k1<float, BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       Cfg::SMEM_BYTES);
+  cudaError_t e = smem_optin(reinterpret_cast<const void*>(gemm_k1<float, BM, BN>), Cfg::SMEM_BYTES);
   if (e != cudaSuccess) return e;
   int64_t tiles_mn = (M / BM) * (N / BN);
   int64_t grid = tiles_mn * batch;
@@ -166,8 +166,8 @@ extern "C" tb_status tb_solve_static(int32_t n_labels, int32_t n_tensors, const 
   LeafDesc* d_leaves = reinterpret_cast<LeafDesc*>(b + arena_bytes);
   float* d_out = reinterpret_cast<float*>(b + arena_bytes + leaf_bytes);
   SCU(cudaMemcpyAsync(d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc), cudaMemcpyHostToDevice, s));
-  const int sm_bytes = (kSmemFloats + 3 * 512 + 2 * 256 + kThreads) * 4;
-  SCU(cudaFuncSetAttribute(ks_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_bytes));
+  // every stream tile the plan compiler emits fits stream_smem_words_max()
+  SCU(smem_optin(reinterpret_cast<const void*>(ks_tile), stream_smem_words_max() * 4));
   ks_leaves<<<(h.n_tensors + kThreads - 1) / kThreads, kThreads, 0, s>>>(d_leaves, h.n_tensors, nullptr, arena);
   SCU(cudaGetLastError());
   if (h.n_nodes == 0) {

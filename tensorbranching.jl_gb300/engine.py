@@ -77,7 +77,12 @@ class Engine:
     """A tb_ctx on one CUDA device."""
 
     def __init__(self, device: int = 0, dtype: str = "f32", use_graphs: bool = True,
-                 max_device_bytes: int = 0, timeout_ms: int = 20000, persistent_ctas: int = 0):
+                 max_device_bytes: int = 0, timeout_ms: int = 20000, persistent_ctas: int = 0,
+                 gemm_arith: str = "f32"):
+        """gemm_arith "f32" (default): every contraction computes in f32 (or
+        in int32 for dtype "i32"); "i16x2": GEMM tiles of plans whose weights
+        are integers >= 0 summing below 8192 compute in exact packed int16
+        pairs (tb_options.gemm_i16)."""
         self.lib = _native.engine_lib()
         opt = _native.TbOptions()
         self.lib.tb_options_default(ctypes.byref(opt))
@@ -86,7 +91,9 @@ class Engine:
         opt.max_device_bytes = int(max_device_bytes)
         opt.timeout_ms = int(timeout_ms)
         opt.persistent_ctas = int(persistent_ctas)
+        opt.gemm_i16 = {"f32": 0, "i16x2": 1}[gemm_arith]
         self.dtype = dtype
+        self.gemm_arith = gemm_arith
         h = c_void_p()
         _native.check(self.lib.tb_ctx_create(device, ctypes.byref(opt), ctypes.byref(h)), None)
         self.ctx = h
@@ -240,6 +247,29 @@ class Engine:
                                             ctypes.cast(ptrs, c_void_p), _native.MODES[mode])
         _native.check(st, self.ctx)
         return outs
+
+    def profile_levels(self, plans, slice_vals=None, r=None) -> list[dict]:
+        """Per launch of the per-level schedule of this batch (run without a
+        graph, a CUDA event after each launch; tbi_profile_levels, an internal
+        engine symbol): device ms, kind ("stream" tiles with leaves and final
+        steps, or "gemm" tiles) and the algorithmic ops and bytes it runs."""
+        f = self.lib.tbi_profile_levels
+        f.restype = c_int32
+        f.argtypes = [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                      c_void_p, POINTER(c_int32)]
+        n, arr, sv, rr = self._batch_args(plans, slice_vals, r)
+        cap = 4096
+        ms = np.zeros(cap)
+        kinds = np.zeros(cap, np.int32)
+        ops = np.zeros(cap)
+        byts = np.zeros(cap)
+        nout = c_int32()
+        st = f(self.ctx, n, ctypes.cast(arr, c_void_p), None if sv is None else sv.ctypes.data,
+               None if rr is None else rr.ctypes.data, cap, ms.ctypes.data, kinds.ctypes.data, ops.ctypes.data,
+               byts.ctypes.data, ctypes.byref(nout))
+        _native.check(st, self.ctx)
+        return [{"ms": float(ms[k]), "kind": "gemm" if kinds[k] == 2 else "stream", "ops": float(ops[k]),
+                 "bytes": float(byts[k])} for k in range(nout.value)]
 
     def last_timing(self) -> tuple[float, int]:
         ms = c_double()

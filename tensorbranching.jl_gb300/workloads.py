@@ -11,11 +11,18 @@ Each workload follows one configuration of the benchmark plan:
               branches
   rr220       random 3-regular n=220, unit weights, one contraction, no slicing
   rr220w_s22  the rr220 graph and tree with integer weights U{1..10}; index
-              slicing until every slice has sc <= 22; 2^k slices (the sliced
-              batch configuration at n=220: at n=300 the host order search
-              reaches sc 42-45, which needs 2^20 slices and ~4.5e15 ops)
+              slicing until every slice has sc <= 22: 2^6 slices, all of them
+              in one step
+  rr300w_s22  the sliced batch configuration at its stated size: random
+              3-regular n=300, weights U{1..10}, index-sliced to sc <= 22
+              (2^22 slices of tc ~28); a step contracts evenly spaced slices
+              and the rate is extrapolated by the share of slices covered
   ksg32_b20   King's subgraph L=32, filling 0.8, unit weights; kernelize +
-              branch until sc <= 20
+              branch until sc <= 20 by the two-way vertex rule
+  ksg32_ob20  the same King's subgraph branched by the reference's default
+              rule (ScoreRS + GreedyBrancher) to sc <= 20: 186 branches
+  ksg32_dom20 the same with the domination reduction as well: it leaves a
+              416-vertex kernel of sc 16, so no branching (one network)
 
 Contraction trees come from simulated annealing, whose floating-point
 acceptance tests can differ between machines, so each workload's trees are
@@ -45,8 +52,14 @@ WORKLOADS = {
                   "optimal branching rule (ScoreRS sc_score regions, GreedyBrancher)",
     "rr220": "random 3-regular n=220 (seed 1), unit weights, one contraction, no slicing",
     "rr220w_s22": "random 3-regular n=220 (seed 1), weights U{1..10} (seed 1), rr220's tree index-sliced to sc<=22",
+    "rr300w_s22": "random 3-regular n=300 (seed 1), weights U{1..10} (seed 1), index-sliced to sc<=22 "
+                  "(2^k slices; a step contracts evenly spaced slices of them)",
     "ksg32_b20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, isolated/pendant reductions, "
-                 "branched to sc<=20",
+                 "branched to sc<=20 by the two-way vertex rule",
+    "ksg32_ob20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, isolated/pendant reductions, "
+                  "branched to sc<=20 by the optimal branching rule (ScoreRS sc_score regions, GreedyBrancher)",
+    "ksg32_dom20": "King's subgraph L=32 filling 0.8 (seed 1), unit weights, every exact reduction (domination "
+                   "included: 416 vertices left, sc 16), so the optimal branching rule at sc<=20 makes no branches",
 }
 
 
@@ -102,6 +115,36 @@ def build_rr220w_s22() -> dict:
     sliced, cc = _order.greedy_slice(code, 22, 40)
     return {"name": "rr220w_s22", "graph": {"n": g.n, "edges": [list(e) for e in g.edges]}, "seed": base["seed"],
             "weights": w.tolist(), "code": base["code"], "cc": list(code.complexity()), "sliced": sliced,
+            "sliced_cc": list(cc)}
+
+
+def build_rr300w_s22() -> dict:
+    """3-regular n=300 (seed 1), weights U{1..10} (seed 1), index-sliced to
+    sc <= 22.  The tree: min-fill, annealed at falling space targets, then
+    the sliced labels chosen greedily and the tree annealed again with them
+    removed (each slice's network is what runs), twice."""
+    g = random_regular_graph(300, 3, 1)
+    w = random_weights(300, 1)
+    ixs, iy = rawcode(g)
+    code = _order.initialize_code(g, _order.GreedyMethod(2))
+    for rnd, (tgt, lo, hi, nit) in enumerate([(40, 0.1, 15.0, 100), (36, 0.5, 20.0, 200), (34, 1.0, 25.0, 300),
+                                             (34, 1.0, 30.0, 600)]):
+        c2 = _order.treesa(code, _order.TreeSA(sc_target=tgt, betas=np.arange(lo, hi, 0.05), ntrials=8, niters=nit,
+                                               seed=rnd, rw_weight=0.2))
+        if (c2.complexity()[1], c2.complexity()[0]) < (code.complexity()[1], code.complexity()[0]):
+            code = c2
+    sliced, cc = _order.greedy_slice(code, 22, 40)
+    for rnd in range(3):
+        cs = _order.treesa(code.remove_labels(sliced),
+                           _order.TreeSA(sc_target=22, betas=np.arange(1.0, 30.0, 0.05), ntrials=8, niters=200,
+                                         seed=10 + rnd, rw_weight=0.2))
+        code = CompressedEinsum(ixs, iy, cs.children, n_labels=g.n)
+        s2, c2 = _order.greedy_slice(code, 22, 40)
+        if len(s2) + c2[0] < len(sliced) + cs.complexity()[0]:
+            sliced = s2
+    cc = code.remove_labels(sliced).complexity()
+    return {"name": "rr300w_s22", "graph": {"n": g.n, "edges": [list(e) for e in g.edges]}, "seed": 1,
+            "weights": w.tolist(), "code": _code_json(code), "cc": list(code.complexity()), "sliced": sliced,
             "sliced_cc": list(cc)}
 
 
@@ -184,11 +227,34 @@ def build_ksg32_b20() -> dict:
     return _pack_branches(brs)
 
 
-BUILDERS = {"rr220": build_rr220, "rr220w_s22": build_rr220w_s22, "rr100_b10": build_rr100_b10,
-            "rr100_ob10": build_rr100_ob10, "ksg32_b20": build_ksg32_b20}
+def build_ksg32_ob20() -> dict:
+    # the reference's default branching rule (ScoreRS regions, GreedyBrancher
+    # set cover) with the isolated / pendant reductions: 186 uneven branches
+    from .branching import GreedyBrancher
+
+    g = random_ksg(32, 0.8, 1)
+    kr, brs = _branch_set(g, np.ones(g.n, np.float32), 20, 1, 20, _mis.REDUCTIONS_BASIC, GreedyBrancher())
+    return _pack_branches(brs)
 
 
-NPZ = {"rr100_b10", "rr100_ob10", "ksg32_b20"}
+def build_ksg32_dom20() -> dict:
+    # every exact reduction, domination included: it leaves 416 of the 804
+    # vertices, whose network already has sc <= 20, so the rule makes no
+    # branches (one network)
+    from .branching import GreedyBrancher
+
+    g = random_ksg(32, 0.8, 1)
+    kr, brs = _branch_set(g, np.ones(g.n, np.float32), 20, 1, 20, _mis.REDUCTIONS_ALL, GreedyBrancher())
+    return _pack_branches(brs)
+
+
+BUILDERS = {"rr220": build_rr220, "rr220w_s22": build_rr220w_s22, "rr300w_s22": build_rr300w_s22,
+            "rr100_b10": build_rr100_b10,
+            "rr100_ob10": build_rr100_ob10, "ksg32_b20": build_ksg32_b20, "ksg32_ob20": build_ksg32_ob20,
+            "ksg32_dom20": build_ksg32_dom20}
+
+
+NPZ = {"rr100_b10", "rr100_ob10", "ksg32_b20", "ksg32_ob20", "ksg32_dom20"}
 MULTI = {"rr100_b10", "rr100_ob10"}  # 32 graphs per step
 
 
@@ -282,6 +348,69 @@ def _gemm_workload(name: str) -> dict:
     return {"name": name, "graph": g, "branches": [b], "sliced": [], "slice_values": None}
 
 
+SLICED_ITEMS_PER_STEP = 64  # slices of an index-sliced workload one benchmark step contracts
+
+
+def step_items(wl: dict, max_items: int = 0) -> list[dict]:
+    """The contraction items of one benchmark step, in order.
+
+    A branch with a network is one item; a branch of an index-sliced workload
+    gives evenly spaced slices (``SLICED_ITEMS_PER_STEP``, or ``max_items``),
+    each fixing the sliced labels to the bits of its slice index (the first
+    ``open_bits`` sliced labels stay open in the root instead).  Branches
+    without a network (empty graph, value r) are not items.  Each item is a
+    dict: ``branch`` (index into wl["branches"]), ``code`` (the network, open
+    labels included), ``weights``, ``fixed`` (labels fixed per item),
+    ``values`` (int8 row for them), ``index`` (slice index, -1 when not
+    sliced) and ``r``.  Sets wl["step_fraction"], the share of all slices a
+    step covers (1 when not sliced).
+    """
+    items = []
+    sliced = wl["sliced"]
+    frac = 1.0
+    for bi, b in enumerate(wl["branches"]):
+        if b.code is None:
+            continue
+        if sliced:
+            ob = wl.get("open_bits", 0)
+            opened, fixed = list(sliced[:ob]), list(sliced[ob:])
+            code = CompressedEinsum(b.code.ixs, opened, b.code.children, n_labels=b.code.n_labels)
+            k = len(fixed)
+            total = 1 << k
+            take = min(total, max_items or wl.get("items_per_step", SLICED_ITEMS_PER_STEP))
+            frac = take / total
+            idx = np.linspace(0, total - 1, take).astype(np.int64)
+            vals = ((idx[:, None] >> np.arange(k)[None, :]) & 1).astype(np.int8)
+            for i, row in zip(idx.tolist(), vals):
+                items.append({"branch": bi, "code": code, "weights": b.p.weight_array(), "fixed": fixed,
+                              "values": row, "index": int(i), "r": float(b.r)})
+        else:
+            items.append({"branch": bi, "code": b.code, "weights": b.p.weight_array(), "fixed": [],
+                          "values": np.zeros(0, np.int8), "index": -1, "r": float(b.r)})
+            if max_items and len(items) >= max_items:
+                break
+    wl["step_fraction"] = frac
+    return items
+
+
+def plans_for(engine, items: list[dict]):
+    """Plans and per-item inputs of ``step_items``' items on an Engine: one
+    plan per branch, shared by its slices.  Returns (plans, slice values per
+    item or None when nothing is sliced, r as float32)."""
+    by_branch = {}
+    plans, svs, rs = [], [], []
+    for it in items:
+        p = by_branch.get(it["branch"])
+        if p is None:
+            p = by_branch[it["branch"]] = engine.plan(it["code"], it["weights"], sliced=it["fixed"])
+        plans.append(p)
+        svs.append(it["values"])
+        rs.append(it["r"])
+    if all(len(x) == 0 for x in svs):
+        svs = None
+    return plans, svs, np.array(rs, np.float32)
+
+
 def load(name: str) -> dict:
     """Workload as host objects:
       branches     list of SlicedBranch (one per network to contract)
@@ -299,15 +428,16 @@ def load(name: str) -> dict:
         code = CompressedEinsum(ixs, iy, np.array(d["code"]["children"], np.int32).reshape(-1, 2), n_labels=g.n)
         b = SlicedBranch(MISProblem(g, np.ones(g.n, np.float32)), code, 0.0)
         return {"name": name, "graph": g, "branches": [b], "sliced": [], "slice_values": None}
-    if name == "rr220w_s22":
-        g = random_regular_graph(220, 3, d["seed"])
+    if name in ("rr220w_s22", "rr300w_s22"):
+        g = random_regular_graph(d["graph"]["n"], 3, d["seed"])
         assert [list(e) for e in g.edges] == d["graph"]["edges"], "graph generator changed"
         w = np.array(d["weights"], np.float32)
         ixs, iy = rawcode(g)
         code = CompressedEinsum(ixs, iy, np.array(d["code"]["children"], np.int32).reshape(-1, 2), n_labels=g.n)
         b = SlicedBranch(MISProblem(g, w), code, 0.0)
+        # rr300w_s22's slices are small (tc ~28): a step takes more of them
         return {"name": name, "graph": g, "branches": [b], "sliced": list(d["sliced"]), "slice_values": None,
-                "open_bits": 0}
+                "open_bits": 0, "items_per_step": 1024 if name == "rr300w_s22" else SLICED_ITEMS_PER_STEP}
     if name in MULTI:
         brs, gs = [], []
         for s in range(1, 33):
@@ -318,9 +448,10 @@ def load(name: str) -> dict:
             brs.append(_unpack_branches(kr.g, kr.weights, sub))
         return {"name": name, "graphs": gs, "branch_sets": brs, "branches": [b for bs in brs for b in bs],
                 "sliced": [], "slice_values": None}
-    if name == "ksg32_b20":
+    if name in ("ksg32_b20", "ksg32_ob20", "ksg32_dom20"):
         g = random_ksg(32, 0.8, 1)
-        kr = _mis.kernelize(g, np.ones(g.n, np.float32), rules=_mis.REDUCTIONS_BASIC)
+        rules = _mis.REDUCTIONS_ALL if name == "ksg32_dom20" else _mis.REDUCTIONS_BASIC
+        kr = _mis.kernelize(g, np.ones(g.n, np.float32), rules=rules)
         brs = _unpack_branches(kr.g, kr.weights, d)
         return {"name": name, "graph": g, "branches": brs, "sliced": [], "slice_values": None}
     raise KeyError(name)

@@ -52,3 +52,11 @@ def engine_i32(tb):
     eng = tb.Engine(dtype="i32")
     yield eng
     eng.close()
+
+
+@pytest.fixture(scope="session")
+def engine_i16(tb):
+    """An f32 context whose GEMM tiles may run the exact packed-int16 form."""
+    eng = tb.Engine(gemm_arith="i16x2")
+    yield eng
+    eng.close()

@@ -154,23 +154,27 @@ def test_rebinding_weights_between_solves(tb, orc, engine):
     assert list(out) == [np.float32(orc.solve(code, w3)), np.float32(orc.solve(code, w3[::-1].copy()))]
 
 
+@pytest.mark.parametrize("arith", ["f32", "i16x2"])
 @pytest.mark.parametrize("kind", ["small_int", "large_int", "fractional"])
-def test_gemm_arithmetic_forms(tb, orc, engine, kind):
-    """GEMM tiles run exact packed-int16 arithmetic when the weights are
-    integers >= 0 summing below 8192, f32 otherwise; both equal the oracle."""
+def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
+    """By default GEMM tiles compute in f32; a context opened with
+    gemm_arith="i16x2" runs exact packed-int16 GEMM tiles when the weights
+    are integers >= 0 summing below 8192, f32 otherwise; all equal the
+    oracle."""
     from cases import gemm_case
 
+    eng = engine if arith == "f32" else engine_i16
     for shape in ((7, 7, 6, 1), (8, 7, 5, 1), (7, 6, 8, 0)):
         g, w, code = gemm_case(tb, *shape)
         if kind == "large_int":
             w = (w * 300).astype(np.float32)           # sum > 8192
         elif kind == "fractional":
             w = (w + 0.5).astype(np.float32)
-        plan = engine.plan(code, w)
+        plan = eng.plan(code, w)
         ref, dumps = orc.execute(code, w, node_iy=plan.all_node_labels(), dump=True)
         for mode in ("batched", "layered"):
-            out, mx = engine.solve_batch([plan, plan], r=[0.0, 2.0], mode=mode)
-            assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode)
+            out, mx = eng.solve_batch([plan, plan], r=[0.0, 2.0], mode=mode)
+            assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode, arith)
 
 
 @pytest.mark.parametrize("bits", [8, 10, 11])

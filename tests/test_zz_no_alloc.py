@@ -24,7 +24,8 @@ def _solve_static(native, code, w):
 
 
 def test_static_matches_solve_batch_twice(tb, native, engine):
-    cases = [rr_case(tb, 60, 1), rr_case(tb, 44, 2, weighted=False)]
+    # rr100 seed 3 has stream tiles that need more than 48 KiB of shared memory
+    cases = [rr_case(tb, 60, 1), rr_case(tb, 44, 2, weighted=False), rr_case(tb, 100, 3)]
     for g, w, code in cases:  # two calls in a row, different networks
         st, v, msg = _solve_static(native, code, w)
         assert st == 0, msg
