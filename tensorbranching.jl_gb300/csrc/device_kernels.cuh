@@ -67,27 +67,47 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
     // keeps one copy pipeline across its tiles
     int64_t tk = first_ticket + (int64_t)blockIdx.x * chunk;
     const int64_t end = tk + chunk < last_ticket ? tk + chunk : last_ticket;
+    if (tk >= end) return;
+    // the first group by binary search, then the following ones in order
+    // (the index lives in shared memory, not across the tile code's registers)
+    if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
+    __syncthreads();
     while (tk < end) {
-      __syncthreads();
-      if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
-      __syncthreads();
       const int gi = s_g;
-      const Group g = groups[gi];
-      const int64_t g_end = gi + 1 < n_groups && groups[gi + 1].first < end ? groups[gi + 1].first : end;
-      const ItemDev<T>& it = items[g.item];
-      const Step& st = it.steps[g.step];
-      if ((KINDS & 1) && st.kind == STEP_TILE) {
-        stream_tiles<T>(it.tiles[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err);
-      } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
-        // a timed-out copy wait (err set) may leave copies in flight into this
-        // CTA's shared memory: use it no further
-        if (!gemm_tiles_any<T>(it.gemms[st.desc], tk - g.first, g_end - g.first, it.arena, tb_smem, err,
-                               (it.flags & 1) != 0))
-          return;
+      const Group& g = groups[gi];
+      int next = gi + 1;
+      if ((KINDS & 1) && g.tiny) {
+        // a run of tiny steps (one tile each, listed first in their level):
+        // warp w takes the run's tiles w, w + 8, ...
+        int n = 1;
+        while (gi + n < n_groups && groups[gi + n].first < end && groups[gi + n].tiny) n++;
+        for (int q = threadIdx.x >> 5; q < n; q += kThreads / 32) {
+          const Group& gq = groups[gi + q];
+          tiny_node<T>(gq.tile, items[gq.item].arena);
+        }
+        next = gi + n;
+        tk = next < n_groups && groups[next].first < end ? groups[next].first : end;
       } else {
-        for (int64_t x = tk; x < g_end; x++) run_small_step<T>(it, st, x - g.first, out_item, r, g.item);
+        const int64_t g_end = gi + 1 < n_groups && groups[gi + 1].first < end ? groups[gi + 1].first : end;
+        const ItemDev<T>& it = items[g.item];
+        const Step& st = it.steps[g.step];
+        const int64_t g_first = g.first;
+        if ((KINDS & 1) && st.kind == STEP_TILE) {
+          stream_tiles<T>(it.tiles[st.desc], tk - g_first, g_end - g_first, it.arena, tb_smem, err);
+        } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
+          // a timed-out copy wait (err set) may leave copies in flight into
+          // this CTA's shared memory: use it no further
+          if (!gemm_tiles_any<T>(it.gemms[st.desc], tk - g_first, g_end - g_first, it.arena, tb_smem, err,
+                                 (it.flags & 1) != 0))
+            return;
+        } else {
+          for (int64_t x = tk; x < g_end; x++) run_small_step<T>(it, st, x - g_first, out_item, r, g.item);
+        }
+        tk = g_end;
       }
-      tk = g_end;
+      __syncthreads();  // every thread has read s_g
+      if (threadIdx.x == 0) s_g = next;
+      __syncthreads();
     }
   }
 }

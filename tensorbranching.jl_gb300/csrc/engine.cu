@@ -146,7 +146,8 @@ struct tb_ctx {
   int64_t n_chunks = 0;
   struct LevelRange {
     int64_t first, count;
-    int kinds;  // 1 stream-like, 2 GEMM
+    int kinds;   // 1 stream-like, 2 GEMM
+    int g0, g1;  // its groups [g0, g1) (contiguous: groups are sorted by level and kind)
   };
   std::vector<LevelRange> level_ranges;
   size_t sv_bytes = 0;
@@ -197,6 +198,13 @@ cudaError_t smem_optin(const void* fn, int bytes) {
   } while (0)
 
 static int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+// A stream step one warp of the level kernel runs from global memory
+// (tiny_node): one tile, no reduction loop or split, small enough.
+static bool tiny_step(const TileDesc& d) {
+  return d.n_tiles == 1 && d.n_loop == 0 && d.split_log2 == 0 && d.n_tc <= kTinyOut && d.n_tr <= kTinyRed &&
+         d.n_tc + d.n_tr <= 10;
+}
 
 template <typename T>
 static size_t elem() { return sizeof(T); }
@@ -337,19 +345,22 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     done_base += it.n_steps;
     hi[i] = it;
   }
-  // groups sorted by (level, item, step)
-  struct GK { int level, kinds, item, step; };
+  // groups sorted by (level, kind, tiny first, item, step)
+  struct GK { int level, kinds, tiny, item, step; };
   std::vector<GK> gk;
   for (int i = 0; i < n; i++) {
     const PlanHost& h = plans[i]->h;
     for (int s = 0; s < (int)h.steps.size(); s++) {
-      if (skip_leaves && h.steps[s].kind == STEP_LEAVES) continue;
-      gk.push_back({h.steps[s].level, h.steps[s].kind == STEP_GEMM ? 2 : 1, i, s});
+      const Step& st = h.steps[s];
+      if (skip_leaves && st.kind == STEP_LEAVES) continue;
+      gk.push_back({st.level, st.kind == STEP_GEMM ? 2 : 1, st.kind == STEP_TILE && tiny_step(h.tiles[st.desc]),
+                    i, s});
     }
   }
   std::stable_sort(gk.begin(), gk.end(), [](const GK& a, const GK& b) {
     if (a.level != b.level) return a.level < b.level;
     if (a.kinds != b.kinds) return a.kinds < b.kinds;
+    if (a.tiny != b.tiny) return a.tiny > b.tiny;
     if (a.item != b.item) return a.item < b.item;
     return a.step < b.step;
   });
@@ -362,14 +373,20 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     hg[g].item = gk[g].item;
     hg[g].step = gk[g].step;
     hg[g].first = tk;
+    hg[g].tiny = gk[g].tiny;
+    hg[g].pad_ = 0;
+    hg[g].tile = gk[g].tiny ? reinterpret_cast<const TileDesc*>(plans[gk[g].item]->d_tiles.p) +
+                                  plans[gk[g].item]->h.steps[gk[g].step].desc
+                            : nullptr;
     if (gk[g].level != cur_level || gk[g].kinds != cur_kinds) {
-      c->level_ranges.push_back({tk, 0, gk[g].kinds});
+      c->level_ranges.push_back({tk, 0, gk[g].kinds, (int)g, (int)g});
       cur_level = gk[g].level;
       cur_kinds = gk[g].kinds;
     }
     int64_t nt = plans[gk[g].item]->h.steps[gk[g].step].n_tiles;
     tk += nt;
     c->level_ranges.back().count += nt;
+    c->level_ranges.back().g1 = (int)g + 1;
   }
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
@@ -442,14 +459,17 @@ static tb_status enqueue_level(tb_ctx* c, const tb_ctx::LevelRange& lr) {
   const float* rv = reinterpret_cast<const float*>(c->rvals.p);
   int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
   if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
+  // the kernel searches only this level's groups (their tickets are absolute)
+  const Group* lg = groups + lr.g0;
+  const int ng = lr.g1 - lr.g0;
   if (lr.kinds == 2) {
     const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-    CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, groups, c->n_groups, lr.first,
-                           lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv, err)));
+    CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
+                           (lr.count + grid - 1) / grid, out_item, rv, err)));
   } else {
     const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-    CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, groups, c->n_groups, lr.first,
-                           lr.first + lr.count, (lr.count + grid - 1) / grid, out_item, rv, err)));
+    CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
+                           (lr.count + grid - 1) / grid, out_item, rv, err)));
   }
   CU(cudaGetLastError());
   return TB_OK;
@@ -1244,14 +1264,12 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
     for (auto& lr : c->level_ranges) {
       if (lr.kinds == 2) {
         const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-        CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, 
-            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr,
-            err)));
+        CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
+                               lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
       } else {
         const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-        CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, 
-            items, groups, c->n_groups, lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr,
-            err)));
+        CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
+                               lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
       }
       CU(cudaGetLastError());
     }

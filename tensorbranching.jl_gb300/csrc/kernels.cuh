@@ -23,6 +23,23 @@ namespace tb {
 // ---------------------------------------------------------------------------
 // semiring
 // ---------------------------------------------------------------------------
+// packed f32 pair add (one FADD2 for two sums) and three-input max
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ float max3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float lo32(uint64_t x) { return __uint_as_float((uint32_t)x); }
+__device__ __forceinline__ float hi32(uint64_t x) { return __uint_as_float((uint32_t)(x >> 32)); }
+__device__ __forceinline__ uint64_t pack2(float x, float y) {
+  return (uint64_t)__float_as_uint(x) | ((uint64_t)__float_as_uint(y) << 32);
+}
+
 template <typename T>
 struct Trop;
 
@@ -30,6 +47,11 @@ template <>
 struct Trop<float> {
   static __device__ __forceinline__ float neg() { return __int_as_float(0xff800000); }
   static __device__ __forceinline__ float mac(float acc, float a, float b) { return fmaxf(acc, a + b); }
+  // two terms: max(acc, a0 + b0, a1 + b1) as one packed add and one 3-input max
+  static __device__ __forceinline__ float mac2(float acc, float a0, float a1, float b0, float b1) {
+    const uint64_t s = add2(pack2(a0, a1), pack2(b0, b1));
+    return max3(acc, lo32(s), hi32(s));
+  }
   static __device__ __forceinline__ float mx(float a, float b) { return fmaxf(a, b); }
   static __device__ __forceinline__ float from_w(float w) { return w; }
   static __device__ __forceinline__ float to_f(float v) { return v; }
@@ -41,6 +63,9 @@ struct Trop<int32_t> {
   // DPX: max(a + b, acc) in one instruction
   static __device__ __forceinline__ int32_t mac(int32_t acc, int32_t a, int32_t b) {
     return __viaddmax_s32(a, b, acc);
+  }
+  static __device__ __forceinline__ int32_t mac2(int32_t acc, int32_t a0, int32_t a1, int32_t b0, int32_t b1) {
+    return __viaddmax_s32(a1, b1, __viaddmax_s32(a0, b0, acc));
   }
   static __device__ __forceinline__ int32_t mx(int32_t a, int32_t b) { return max(a, b); }
   static __device__ __forceinline__ int32_t from_w(float w) { return (int32_t)w; }
@@ -286,17 +311,23 @@ struct StreamRun {
 // outputs per thread and NTR in-tile reduction terms, all compile-time.
 // One barrier per item: after it, item `it` is visible to every thread and
 // every thread is done with item it - 1, whose buffer the refill reuses.
+// In-tile reduction offsets are XORs of one basis offset per reduced bit
+// (the swizzle is linear over GF(2)): the terms are visited in Gray-code
+// order, one XOR per step, so only log2(NTR) offsets per operand stay in
+// registers; they are taken in pairs (one packed add and a 3-input max).
 template <typename T, int OPT, int NTR>
 __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
-  int iar[NTR], ibr[NTR];
+  constexpr int LTR = NTR >= 16 ? 4 : NTR >= 8 ? 3 : NTR >= 4 ? 2 : NTR >= 2 ? 1 : 0;
+  static_assert((1 << LTR) == NTR, "NTR is a power of two");
+  int ba[LTR > 0 ? LTR : 1], bb[LTR > 0 ? LTR : 1];
 #pragma unroll
-  for (int r = 0; r < NTR; r++) {
-    iar[r] = R.IAr[r];
-    ibr[r] = R.IBr[r];
+  for (int b = 0; b < LTR; b++) {
+    ba[b] = R.IAr[1 << b];
+    bb[b] = R.IBr[1 << b];
   }
-  T acc[kMaxOpt];
+  T acc[OPT];
 #pragma unroll
-  for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+  for (int i = 0; i < OPT; i++) acc[i] = Trop<T>::neg();
   const int last = R.nloop - 1;
   for (int64_t it = 0; it < R.n_items; it++) {
     cp_async_wait_n(R.S - 2);
@@ -308,16 +339,35 @@ __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
     if (R.act) {
 #pragma unroll
       for (int i = 0; i < OPT; i++) {
-        T a = acc[i];
+        int xa = R.iah[i], xb = R.ibh[i];  // term 0: the reduced bits' offsets are 0
+        if constexpr (NTR == 1) {
+          acc[i] = Trop<T>::mac(acc[i], As[xa], Bs[xb]);
+        } else {
+          // two independent chains for NTR >= 4
+          T a0 = acc[i], a1 = Trop<T>::neg();
 #pragma unroll
-        for (int r = 0; r < NTR; r++) a = Trop<T>::mac(a, As[R.iah[i] ^ iar[r]], Bs[R.ibh[i] ^ ibr[r]]);
-        acc[i] = a;
+          for (int r = 0; r < NTR; r += 2) {
+            // the pair (g, g ^ bit 0) of Gray-code terms
+            const T x0 = As[xa], y0 = Bs[xb];
+            const T x1 = As[xa ^ ba[0]], y1 = Bs[xb ^ bb[0]];
+            if (NTR >= 4 && (r & 2)) a1 = Trop<T>::mac2(a1, x0, x1, y0, y1);
+            else a0 = Trop<T>::mac2(a0, x0, x1, y0, y1);
+            if (r + 2 < NTR) {
+              // pair index m = r / 2 moves to m + 1: flip reduced bit
+              // 1 + ctz(m + 1) = ctz(r + 2)
+              const int k = __ffs(r + 2) - 1;
+              xa ^= ba[k];
+              xb ^= bb[k];
+            }
+          }
+          acc[i] = NTR >= 4 ? Trop<T>::mx(a0, a1) : a0;
+        }
       }
     }
     if (R.rl == last) {
       if (R.act) R.template store<OPT>(acc);
 #pragma unroll
-      for (int i = 0; i < kMaxOpt; i++) acc[i] = Trop<T>::neg();
+      for (int i = 0; i < OPT; i++) acc[i] = Trop<T>::neg();
       R.next_tile();
       R.rl = 0;
     } else {
@@ -532,24 +582,32 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   R.oc = gc;
   R.cb = 0;
   R.rl = 0;
-  const bool fixed = R.hasB && R.split == 0 && ntr <= 4;
-  const int shape = R.opt * 8 + ntr;
+  const bool fixed = R.hasB && R.split == 0 && ntr <= 16;
+  const int shape = R.opt * 32 + ntr;
   __syncthreads();  // tables ready
   // prologue: items 0 .. S-2, one commit group each (empty past the end)
   for (int k = 0; k < R.S - 1; k++) R.refill();
   if (fixed) {
     switch (shape) {
-      case 1 * 8 + 1: stream_loop_fixed<T, 1, 1>(R); break;
-      case 1 * 8 + 2: stream_loop_fixed<T, 1, 2>(R); break;
-      case 1 * 8 + 4: stream_loop_fixed<T, 1, 4>(R); break;
-      case 2 * 8 + 1: stream_loop_fixed<T, 2, 1>(R); break;
-      case 2 * 8 + 2: stream_loop_fixed<T, 2, 2>(R); break;
-      case 2 * 8 + 4: stream_loop_fixed<T, 2, 4>(R); break;
-      case 4 * 8 + 1: stream_loop_fixed<T, 4, 1>(R); break;
-      case 4 * 8 + 2: stream_loop_fixed<T, 4, 2>(R); break;
-      case 4 * 8 + 4: stream_loop_fixed<T, 4, 4>(R); break;
-      case 8 * 8 + 1: stream_loop_fixed<T, 8, 1>(R); break;
-      case 8 * 8 + 2: stream_loop_fixed<T, 8, 2>(R); break;
+      case 1 * 32 + 1: stream_loop_fixed<T, 1, 1>(R); break;
+      case 1 * 32 + 2: stream_loop_fixed<T, 1, 2>(R); break;
+      case 1 * 32 + 4: stream_loop_fixed<T, 1, 4>(R); break;
+      case 1 * 32 + 8: stream_loop_fixed<T, 1, 8>(R); break;
+      case 1 * 32 + 16: stream_loop_fixed<T, 1, 16>(R); break;
+      case 2 * 32 + 1: stream_loop_fixed<T, 2, 1>(R); break;
+      case 2 * 32 + 2: stream_loop_fixed<T, 2, 2>(R); break;
+      case 2 * 32 + 4: stream_loop_fixed<T, 2, 4>(R); break;
+      case 2 * 32 + 8: stream_loop_fixed<T, 2, 8>(R); break;
+      case 2 * 32 + 16: stream_loop_fixed<T, 2, 16>(R); break;
+      case 4 * 32 + 1: stream_loop_fixed<T, 4, 1>(R); break;
+      case 4 * 32 + 2: stream_loop_fixed<T, 4, 2>(R); break;
+      case 4 * 32 + 4: stream_loop_fixed<T, 4, 4>(R); break;
+      case 4 * 32 + 8: stream_loop_fixed<T, 4, 8>(R); break;
+      case 4 * 32 + 16: stream_loop_fixed<T, 4, 16>(R); break;
+      case 8 * 32 + 1: stream_loop_fixed<T, 8, 1>(R); break;
+      case 8 * 32 + 2: stream_loop_fixed<T, 8, 2>(R); break;
+      case 8 * 32 + 4: stream_loop_fixed<T, 8, 4>(R); break;
+      case 8 * 32 + 8: stream_loop_fixed<T, 8, 8>(R); break;
       default:
         if (R.opt == 1) stream_loop_any<T, 1>(R);
         else stream_loop_any<T, kMaxOpt>(R);
@@ -561,6 +619,68 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
     stream_loop_any<T, kMaxOpt>(R);
   }
   cp_async_wait<0>();
+}
+
+// A tiny stream step (Group::tiny) by one warp, straight from global memory
+// (its operands are a few hundred bytes, so staging would cost more than the
+// reads): lane l computes outputs l, l + 32, ...; an output's operand offsets
+// are sums of one power of two per set bit of its index (distinct tensor
+// positions), and the reduced terms are visited in Gray-code order, one XOR
+// per term.
+template <typename T>
+__device__ __noinline__ void tiny_node(const TileDesc* __restrict__ d, T* __restrict__ arena) {
+  const int lane = threadIdx.x & 31;
+  const int n_tc = d->n_tc, n_tr = d->n_tr;
+  const bool hasB = d->b_off >= 0;
+  const T* A = arena + d->a_off;
+  const T* B = arena + (hasB ? d->b_off : 0);
+  T* C = arena + d->c_off;
+  int sa[kTinyOut], sb[kTinyOut], sc[kTinyOut], ra[kTinyRed], rb[kTinyRed];
+#pragma unroll
+  for (int b = 0; b < kTinyOut; b++) {
+    sa[b] = sb[b] = sc[b] = 0;
+    if (b < n_tc) {
+      const int xa = d->tc_a[b], xb = d->tc_b[b];
+      if (xa >= 0) sa[b] = 1 << d->ta_pos[xa];
+      if (xb >= 0) sb[b] = 1 << d->tb_pos[xb];
+      sc[b] = 1 << d->tc_pos[b];
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < kTinyRed; b++) {
+    ra[b] = rb[b] = 0;
+    if (b < n_tr) {
+      const int xa = d->tr_a[b], xb = d->tr_b[b];
+      if (xa >= 0) ra[b] = 1 << d->ta_pos[xa];
+      if (xb >= 0) rb[b] = 1 << d->tb_pos[xb];
+    }
+  }
+  const int nred = 1 << n_tr;
+  for (int c = lane; c < (1 << n_tc); c += 32) {
+    int oa = 0, ob = 0, oc = 0;
+#pragma unroll
+    for (int b = 0; b < kTinyOut; b++)
+      if ((c >> b) & 1) {
+        oa |= sa[b];
+        ob |= sb[b];
+        oc |= sc[b];
+      }
+    T acc = Trop<T>::neg();
+    for (int r = 0; r < nred; r++) {
+      acc = hasB ? Trop<T>::mac(acc, __ldcg(A + oa), __ldcg(B + ob)) : Trop<T>::mx(acc, __ldcg(A + oa));
+      const int k = __ffs(r + 1) - 1;  // Gray code: the next term flips reduced bit k
+      int xa = 0, xb = 0;
+#pragma unroll
+      for (int b = 0; b < kTinyRed; b++)
+        if (b == k) {
+          xa = ra[b];
+          xb = rb[b];
+        }
+      oa ^= xa;
+      ob ^= xb;
+    }
+    C[oc] = acc;
+  }
 }
 
 // One tile (the launch-per-tile form used by the plain path's kernels).
@@ -599,18 +719,6 @@ __device__ void final_tile(const FinalDesc& f, const T* __restrict__ arena, floa
 // keeps k in interleaved pairs, so one 64-bit load yields (x[k], x[k+1]) and
 // the inner step is one add.f32x2 and one three-input max.f32 per two MACs.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ float max3(float a, float b, float c) {
-  float d;
-  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-  return d;
-}
-__device__ __forceinline__ float lo32(uint64_t x) { return __uint_as_float((uint32_t)x); }
-__device__ __forceinline__ float hi32(uint64_t x) { return __uint_as_float((uint32_t)(x >> 32)); }
 
 template <typename T, int BM, int BN>
 struct K1Cfg {

@@ -143,8 +143,17 @@ struct ItemDev {
 // order and tickets index tiles within the concatenation of groups.
 struct Group {
   int32_t item, step;
-  int64_t first;  // first ticket of this group
+  int64_t first;          // first ticket of this group
+  int32_t tiny;           // 1: a one-tile stream step small enough for one warp (tiny_node)
+  int32_t pad_;
+  const TileDesc* tile;   // its descriptor (device), when tiny
 };
+
+// Stream steps one warp runs straight from global memory (tiny_node): one
+// tile, no reduction loop or split, at most 2^kTinyOut outputs and 2^kTinyRed
+// reduced terms.
+constexpr int kTinyOut = 8;
+constexpr int kTinyRed = 5;
 
 // A unit of work of the persistent executor: tiles [t0, t1) of one group.
 // Chunks are listed in dependency order.
