@@ -70,7 +70,8 @@ class TbTuneResult(ctypes.Structure):
         ("ms", c_double),
         ("ms_default", c_double),
         ("n_tried", c_int32),
-        ("reserved", c_int32 * 7),
+        ("stream_ctas_per_sm", c_int32),
+        ("reserved", c_int32 * 6),
     ]
 
 

@@ -55,6 +55,9 @@ __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int
 
 // One launch per tree level: block b runs ticket first_ticket + b.  No
 // waiting: the previous launch on the stream finished every dependency.
+// KINDS bit 0: stream-like steps, bit 1: GEMM steps; 5 is the stream form
+// with two resident CTAs per SM (128 registers a thread instead of 80),
+// which the autotuner may choose.
 template <typename T, int KINDS>
 __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
                                                    int64_t first_ticket, int64_t last_ticket, int64_t chunk,

@@ -127,6 +127,8 @@ struct tb_ctx {
   int sms = 0;
   int persistent_ctas = 0;
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
+  int stream_ctas_wide = 0;  // the same for the 128-register form of the stream level kernel
+  bool stream_wide = false;  // per-level stream launches use that form (tb_autotune)
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   std::vector<int32_t> small_order;   // fused small form: items by shared need, largest first
   std::vector<SmallGroup> small_groups;  // launches over small_order
@@ -200,10 +202,10 @@ cudaError_t smem_optin(const void* fn, int bytes) {
 static int64_t align_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
 // A stream step one warp of the level kernel runs from global memory
-// (tiny_node): one tile, no reduction loop or split, small enough.
+// (tiny_node): one tile, no reduction loop, small enough (a block would split
+// its reduction over threads; a warp does not need to).
 static bool tiny_step(const TileDesc& d) {
-  return d.n_tiles == 1 && d.n_loop == 0 && d.split_log2 == 0 && d.n_tc <= kTinyOut && d.n_tr <= kTinyRed &&
-         d.n_tc + d.n_tr <= 10;
+  return d.n_tiles == 1 && d.n_loop == 0 && d.n_tc <= kTinyOut && d.n_tr <= kTinyRed && d.n_tc + d.n_tr <= 10;
 }
 
 template <typename T>
@@ -465,6 +467,10 @@ static tb_status enqueue_level(tb_ctx* c, const tb_ctx::LevelRange& lr) {
   if (lr.kinds == 2) {
     const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
     CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
+                           (lr.count + grid - 1) / grid, out_item, rv, err)));
+  } else if (c->stream_wide) {
+    const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas_wide);
+    CU((launch_level<T, 5>((unsigned)grid, smem_bytes(1), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
                            (lr.count + grid - 1) / grid, out_item, rv, err)));
   } else {
     const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
@@ -839,7 +845,20 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : best_cps * c->sms;
   c->chunk_div = best_div;
   c->tune_fallback = best_mode;
-  // 3. the fused small form, when every plan has one
+  // 3. per-level launches: the stream level kernel at 80 registers and three
+  // CTAs per SM, or 128 registers and two
+  bool best_wide = c->stream_wide;
+  if (best_mode == TB_MODE_LAYERED) {
+    c->stream_wide = !best_wide;
+    if ((st = time_batch(c, n, plans, sv, r, TB_MODE_LAYERED, ms))) return st;
+    res.n_tried++;
+    if (ms < best) {
+      best = ms;
+      best_wide = c->stream_wide;
+    }
+    c->stream_wide = best_wide;
+  }
+  // 4. the fused small form, when every plan has one
   bool all_small = true;
   for (tb_plan* p : uniq) all_small = all_small && p->h.small_ok;
   if (all_small) {
@@ -854,6 +873,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   res.tile_bits = best_bits;
   res.ctas_per_sm = c->persistent_ctas / std::max(1, c->sms);
   res.chunk_div = best_div;
+  res.stream_ctas_per_sm = (c->stream_wide ? c->stream_ctas_wide : c->stream_ctas) / std::max(1, c->sms);
   res.ms = best;
   c->tune = res;
   c->tuned = true;
@@ -928,6 +948,12 @@ tb_status tb_ctx_create(int32_t device, const tb_options* opt, tb_ctx** out) {
   else
     CU((occupancy_level<int32_t, 1>(&per_sm_stream, smem_bytes(1))));
   c->stream_ctas = std::max(1, per_sm_stream) * c->sms;
+  int per_sm_wide = 0;
+  if (c->opt.dtype == TB_DTYPE_F32)
+    CU((occupancy_level<float, 5>(&per_sm_wide, smem_bytes(1))));
+  else
+    CU((occupancy_level<int32_t, 5>(&per_sm_wide, smem_bytes(1))));
+  c->stream_ctas_wide = std::max(1, per_sm_wide) * c->sms;
   int per_sm_gemm = 0;
   if (c->opt.dtype == TB_DTYPE_F32)
     CU((occupancy_level<float, 2>(&per_sm_gemm, smem_bytes(2))));
@@ -1266,6 +1292,10 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
         const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
         CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
                                lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
+      } else if (c->stream_wide) {
+        const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas_wide);
+        CU((launch_level<T, 5>((unsigned)grid, smem_bytes(1), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
+                               lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
       } else {
         const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
         CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
@@ -1542,6 +1572,15 @@ __global__ void __launch_bounds__(256) k_peak_i16(unsigned* out, int iters, unsi
 
 // Resident CTAs of the context's kernels (stream tiles, GEMM tiles,
 // persistent executor) and its SM count, for reports.
+// Per-level stream launches in the 128-register form (1) or the 80-register
+// form (0), as the autotuner may choose; for tests that pin one.
+extern "C" int32_t tbi_ctx_set_stream_wide(tb_ctx* c, int32_t wide) {
+  if (!c) return TB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->stream_wide = wide != 0;
+  return TB_OK;
+}
+
 extern "C" int32_t tbi_ctx_info(const tb_ctx* c, int32_t* out4) {
   if (!c || !out4) return TB_ERR_INVALID;
   out4[0] = c->stream_ctas;

@@ -314,7 +314,11 @@ struct StreamRun {
 // In-tile reduction offsets are XORs of one basis offset per reduced bit
 // (the swizzle is linear over GF(2)): the terms are visited in Gray-code
 // order, one XOR per step, so only log2(NTR) offsets per operand stay in
-// registers; they are taken in pairs (one packed add and a 3-input max).
+// registers.
+// Terms are packed in pairs (pack2 + add.f32x2 + 3-input max) from this many
+// in-tile reduction terms on; fewer go one add and one max each.
+constexpr int kPairMin = 8;
+
 template <typename T, int OPT, int NTR>
 __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
   constexpr int LTR = NTR >= 16 ? 4 : NTR >= 8 ? 3 : NTR >= 4 ? 2 : NTR >= 2 ? 1 : 0;
@@ -350,8 +354,9 @@ __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
             // the pair (g, g ^ bit 0) of Gray-code terms
             const T x0 = As[xa], y0 = Bs[xb];
             const T x1 = As[xa ^ ba[0]], y1 = Bs[xb ^ bb[0]];
-            if (NTR >= 4 && (r & 2)) a1 = Trop<T>::mac2(a1, x0, x1, y0, y1);
-            else a0 = Trop<T>::mac2(a0, x0, x1, y0, y1);
+            T& a = (NTR >= 4 && (r & 2)) ? a1 : a0;
+            if constexpr (NTR >= kPairMin) a = Trop<T>::mac2(a, x0, x1, y0, y1);
+            else a = Trop<T>::mac(Trop<T>::mac(a, x0, y0), x1, y1);
             if (r + 2 < NTR) {
               // pair index m = r / 2 moves to m + 1: flip reduced bit
               // 1 + ctz(m + 1) = ctz(r + 2)

@@ -150,8 +150,8 @@ struct Group {
 };
 
 // Stream steps one warp runs straight from global memory (tiny_node): one
-// tile, no reduction loop or split, at most 2^kTinyOut outputs and 2^kTinyRed
-// reduced terms.
+// tile, no reduction loop, at most 2^kTinyOut outputs and 2^kTinyRed reduced
+// terms.
 constexpr int kTinyOut = 8;
 constexpr int kTinyRed = 5;
 

@@ -175,6 +175,15 @@ class Engine:
         return {"stream_ctas": int(out[0]), "gemm_ctas": int(out[1]), "persistent_ctas": int(out[2]),
                 "sms": int(out[3])}
 
+    def set_stream_wide(self, wide: bool) -> None:
+        """Per-level stream launches with 128 registers a thread and two CTAs
+        per SM (True) or 80 and three (False), as the autotuner may choose
+        (tbi_ctx_set_stream_wide, an internal engine symbol)."""
+        f = self.lib.tbi_ctx_set_stream_wide
+        f.restype = c_int32
+        f.argtypes = [c_void_p, c_int32]
+        _native.check(f(self.ctx, 1 if wide else 0), self.ctx)
+
     def retile(self, plan: "Plan", bits: int) -> None:
         """Re-plan a plan's stream tiles for up to 2^bits outputs (8..11), as
         the autotuner does (tbi_plan_retile, an internal engine symbol)."""
@@ -211,7 +220,8 @@ class Engine:
         _native.check(st, self.ctx)
         names = {v: k for k, v in _native.MODES.items()}
         return {"mode": names[res.mode], "tile_bits": res.tile_bits, "ctas_per_sm": res.ctas_per_sm,
-                "chunk_div": res.chunk_div, "ms": res.ms, "ms_default": res.ms_default, "n_tried": res.n_tried}
+                "chunk_div": res.chunk_div, "stream_ctas_per_sm": res.stream_ctas_per_sm, "ms": res.ms,
+                "ms_default": res.ms_default, "n_tried": res.n_tried}
 
     def solve_batch(self, plans, slice_vals=None, r=None, mode: str = "batched"):
         """Per-item results (max root + r) and their max."""

@@ -177,10 +177,12 @@ def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
             assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode, arith)
 
 
+@pytest.mark.parametrize("wide", [False, True])
 @pytest.mark.parametrize("bits", [8, 10, 11])
-def test_stream_tile_configurations(tb, orc, engine, bits):
-    """Every stream tile size the autotuner may choose gives the oracle's
-    intermediates in the fused modes."""
+def test_stream_tile_configurations(tb, orc, engine, bits, wide):
+    """Every stream tile size and stream kernel form the autotuner may choose
+    gives the oracle's intermediates in the fused modes."""
+    engine.set_stream_wide(wide)
     import ctypes
 
     lib = engine.lib
@@ -197,3 +199,4 @@ def test_stream_tile_configurations(tb, orc, engine, bits):
         got = engine.dump(plan, mode="layered")
         for a, b in zip(got, dumps):
             assert np.array_equal(a, b)
+    engine.set_stream_wide(False)
