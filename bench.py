@@ -680,7 +680,8 @@ def run_serve(tb, args):
            "data": "synthetic serving mix (seeded)",
            "config": {"workload": "serve", "requests": len(preps),
                       "detail": "Poisson arrivals at 0.8x measured capacity; 3-regular n in [60,200] and KSG L in "
-                                "[10,24] filling 0.8; unit or U{1..10} weights; sc capped at 24 by index slicing",
+                                "[10,36] filling 0.8; unit or U{1..10} weights; sc capped at 24 by index slicing; "
+                                "admitted requests run as cohorts on 4 streams",
                       "arrival_rate_per_s": rate, "capacity_solves_per_s": capacity,
                       "items": int(sum(p.n_items for p in preps)), "host_prep_s": prep_s},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),

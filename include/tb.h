@@ -270,10 +270,13 @@ tb_status tb_gemm_device(tb_ctx* ctx, int64_t M, int64_t N, int64_t K, int64_t b
  * pool_bytes (0: half the context budget) and at most max_items items in
  * flight (0: 4096).  tb_submit queues a request of n items (plans with their
  * slice values and r, as in tb_solve_batch) and returns at once; any thread
- * may submit, poll and wait.  The owner thread admits queued requests as pool
- * memory and item slots free up, and then runs steps: one step executes, for
- * every admitted item, the contraction steps of its current tree level, so
- * requests that arrive while others run overlap with them on the device.  A
+ * may submit, poll and wait.  The owner thread admits queued requests, whole
+ * and in arrival order, as pool memory, item slots and one of four stream
+ * slots free up; the requests admitted together form a cohort, which runs as
+ * one batch of per-level launches on its slot's stream while the owner
+ * thread goes on admitting, so requests that arrive while others run overlap
+ * with them on the device; no step of it waits for the device.  A request
+ * completes when the cohort holding its last item does.  A
  * request's result is the max over its items (as contract_slices + maximum,
  * src/dynamic_ob.jl:24-27).  Plans must outlive their requests and must not
  * be re-bound while a request uses them; while a server runs, call
@@ -290,6 +293,8 @@ tb_status tb_poll(tb_request* req, int32_t* done);
  * latency in milliseconds. */
 tb_status tb_wait(tb_request* req, int32_t timeout_ms, float* out_max, double* latency_ms);
 void tb_request_free(tb_request* req);
+/* Cohorts launched (steps), kernel launches, requests completed and items in
+ * flight. */
 tb_status tb_serve_stats(tb_ctx* ctx, int64_t* steps, int64_t* launches, int64_t* completed, int64_t* active);
 
 /*

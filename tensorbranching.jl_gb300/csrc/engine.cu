@@ -310,6 +310,62 @@ static tb_status plain_item(tb_ctx* c, tb_plan* p, T* arena, const int8_t* d_sv,
 // ---------------------------------------------------------------------------
 // batched upload: items, groups (dependency order), counters
 // ---------------------------------------------------------------------------
+// One (item, step) of a batch with its launch-order key.
+struct GroupKey {
+  int level, kinds, tiny, item, step;
+};
+
+// The batch's steps in launch order: by tree level, then kind (stream-like
+// before GEMM), tiny steps first, then item and step.
+static std::vector<GroupKey> sorted_groups(int n, tb_plan* const* plans, bool skip_leaves) {
+  std::vector<GroupKey> gk;
+  for (int i = 0; i < n; i++) {
+    const PlanHost& h = plans[i]->h;
+    for (int s = 0; s < (int)h.steps.size(); s++) {
+      const Step& st = h.steps[s];
+      if (skip_leaves && st.kind == STEP_LEAVES) continue;
+      gk.push_back({st.level, st.kind == STEP_GEMM ? 2 : 1, st.kind == STEP_TILE && tiny_step(h.tiles[st.desc]),
+                    i, s});
+    }
+  }
+  std::stable_sort(gk.begin(), gk.end(), [](const GroupKey& a, const GroupKey& b) {
+    if (a.level != b.level) return a.level < b.level;
+    if (a.kinds != b.kinds) return a.kinds < b.kinds;
+    if (a.tiny != b.tiny) return a.tiny > b.tiny;
+    if (a.item != b.item) return a.item < b.item;
+    return a.step < b.step;
+  });
+  return gk;
+}
+
+// Groups (host copy, gk.size() entries) and one launch range per (level,
+// kind); returns the number of tickets.
+static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plans, Group* hg,
+                           std::vector<tb_ctx::LevelRange>& ranges) {
+  int64_t tk = 0;
+  ranges.clear();
+  int cur_level = -1, cur_kinds = -1;
+  for (size_t g = 0; g < gk.size(); g++) {
+    const tb_plan* p = plans[gk[g].item];
+    hg[g].item = gk[g].item;
+    hg[g].step = gk[g].step;
+    hg[g].first = tk;
+    hg[g].tiny = gk[g].tiny;
+    hg[g].pad_ = 0;
+    hg[g].tile =
+        gk[g].tiny ? reinterpret_cast<const TileDesc*>(p->d_tiles.p) + p->h.steps[gk[g].step].desc : nullptr;
+    if (gk[g].level != cur_level || gk[g].kinds != cur_kinds) {
+      ranges.push_back({tk, 0, gk[g].kinds, (int)g, (int)g});
+      cur_level = gk[g].level;
+      cur_kinds = gk[g].kinds;
+    }
+    const int64_t nt = p->h.steps[gk[g].step].n_tiles;
+    tk += nt;
+    ranges.back().count += nt;
+    ranges.back().g1 = (int)g + 1;
+  }
+  return tk;
+}
 template <typename T>
 static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std::vector<int64_t>& arena_off,
                               const std::vector<int64_t>& sv_off, bool skip_leaves,
@@ -347,49 +403,10 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     done_base += it.n_steps;
     hi[i] = it;
   }
-  // groups sorted by (level, kind, tiny first, item, step)
-  struct GK { int level, kinds, tiny, item, step; };
-  std::vector<GK> gk;
-  for (int i = 0; i < n; i++) {
-    const PlanHost& h = plans[i]->h;
-    for (int s = 0; s < (int)h.steps.size(); s++) {
-      const Step& st = h.steps[s];
-      if (skip_leaves && st.kind == STEP_LEAVES) continue;
-      gk.push_back({st.level, st.kind == STEP_GEMM ? 2 : 1, st.kind == STEP_TILE && tiny_step(h.tiles[st.desc]),
-                    i, s});
-    }
-  }
-  std::stable_sort(gk.begin(), gk.end(), [](const GK& a, const GK& b) {
-    if (a.level != b.level) return a.level < b.level;
-    if (a.kinds != b.kinds) return a.kinds < b.kinds;
-    if (a.tiny != b.tiny) return a.tiny > b.tiny;
-    if (a.item != b.item) return a.item < b.item;
-    return a.step < b.step;
-  });
+  std::vector<GroupKey> gk = sorted_groups(n, plans, skip_leaves);
   CU(c->h_groups.ensure(sizeof(Group) * std::max<size_t>(gk.size(), 1)));
   Group* hg = reinterpret_cast<Group*>(c->h_groups.p);
-  int64_t tk = 0;
-  c->level_ranges.clear();
-  int cur_level = -1, cur_kinds = -1;
-  for (size_t g = 0; g < gk.size(); g++) {
-    hg[g].item = gk[g].item;
-    hg[g].step = gk[g].step;
-    hg[g].first = tk;
-    hg[g].tiny = gk[g].tiny;
-    hg[g].pad_ = 0;
-    hg[g].tile = gk[g].tiny ? reinterpret_cast<const TileDesc*>(plans[gk[g].item]->d_tiles.p) +
-                                  plans[gk[g].item]->h.steps[gk[g].step].desc
-                            : nullptr;
-    if (gk[g].level != cur_level || gk[g].kinds != cur_kinds) {
-      c->level_ranges.push_back({tk, 0, gk[g].kinds, (int)g, (int)g});
-      cur_level = gk[g].level;
-      cur_kinds = gk[g].kinds;
-    }
-    int64_t nt = plans[gk[g].item]->h.steps[gk[g].step].n_tiles;
-    tk += nt;
-    c->level_ranges.back().count += nt;
-    c->level_ranges.back().g1 = (int)g + 1;
-  }
+  const int64_t tk = fill_groups(gk, plans, hg, c->level_ranges);
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
   // chunks for the persistent executor: runs of stream tiles (tables are
@@ -399,7 +416,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   // stream tiles of its whole level, so many small steps of many items do
   // not turn into as many tiny runs.
   std::vector<int64_t> level_tiles;
-  for (const GK& x : gk) {
+  for (const GroupKey& x : gk) {
     const Step& st = plans[x.item]->h.steps[x.step];
     if (st.kind != STEP_TILE) continue;
     if ((int)level_tiles.size() <= x.level) level_tiles.resize(x.level + 1, 0);
@@ -1806,15 +1823,17 @@ extern "C" int32_t tbi_measure_maxplus_peak(int32_t device, double* ops_per_s) {
 }
 
 // ---------------------------------------------------------------------------
-// Serving: continuous batching at tree-level granularity.
+// Serving: continuous batching in cohorts over several streams.
 //
-// A device-owner thread admits submitted requests while their arenas fit in
-// a device pool and the active-item limit allows, then repeats steps: one
-// step runs, for every active item, the steps of its current tree level --
-// stream-like tiles in one launch, GEMM tiles in another -- so an item that
-// arrived a moment ago runs its leaves while older items run deeper levels.
-// Finished items release their arena at once and their request completes
-// when its last item does.
+// A device-owner thread admits queued requests while pool memory, item slots
+// and a free stream slot allow; the requests admitted together form a
+// cohort, which runs as one batch (its items' level launches, as
+// TB_MODE_LAYERED, with the result copy and an event) on the slot's stream,
+// without the owner thread waiting for it.  Requests that arrive while
+// cohorts run are admitted into the next free slot, so their work overlaps on
+// the device with the running cohorts.  The owner thread polls the cohorts'
+// events; a finished cohort frees its pool memory and slot at once and
+// completes its requests.
 // ---------------------------------------------------------------------------
 #include <atomic>
 #include <chrono>
@@ -1884,60 +1903,81 @@ struct PoolAlloc {
 
 }  // namespace
 
+constexpr int kServeSlots = 4;  // cohorts in flight at once (one stream each)
+
 struct Server {
+  struct Active {
+    tb_request* req;
+    int idx;
+    tb_plan* plan;
+    int64_t off, elems;
+  };
+  // one stream and the batch state of the cohort running on it
+  struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    DevBuf items, groups, sv, rv, out;
+    HostBuf h_items, h_groups, h_sv, h_rv, h_out;
+    std::vector<tb_ctx::LevelRange> ranges;
+    std::vector<Active> act;
+    bool busy = false;
+  };
   tb_ctx* ctx = nullptr;
   std::thread th;
   std::atomic<bool> stop{false};
   std::mutex qm;
   std::condition_variable qcv;
   std::deque<tb_request*> pending;
-  cudaStream_t stream = nullptr;
-  DevBuf pool, items, groups, sv, rv, out, err;
-  HostBuf h_items, h_groups, h_sv, h_rv, h_out;
+  DevBuf pool;
   PoolAlloc palloc;
   int64_t pool_elems = 0;
   int max_items = 0;
-  struct Active {
-    tb_request* req;
-    int idx;
-    tb_plan* plan;
-    int64_t off, elems;
-    int level;
-  };
-  std::vector<Active> active;
-  std::atomic<int64_t> steps{0}, launches{0}, completed{0};
-  std::string fatal;
+  int n_active = 0;  // items of the cohorts in flight
+  Slot slots[kServeSlots];
+  std::atomic<int64_t> steps{0}, launches{0}, completed{0}, active_items{0};
 };
 
-template <typename T>
-static void serve_finish(Server* S, tb_request* q) {
-  std::lock_guard<std::mutex> lk(q->m);
+static void serve_complete(tb_request* q, tb_status st, const std::string& msg) {
+  std::lock_guard<std::mutex> lq(q->m);
+  if (q->state == 2) return;
+  q->status = st;
+  q->err = msg;
   q->t_done = now_s();
   q->state = 2;
   q->cv.notify_all();
 }
 
+// Upload a cohort's batch state and enqueue its level launches, the result
+// copy and the completion event on the slot's stream; returns at once.
 template <typename T>
-static tb_status serve_step(Server* S) {
+static tb_status serve_launch(Server* S, Server::Slot& sl) {
   tb_ctx* c = S->ctx;
-  const int n = (int)S->active.size();
-  // item table
-  CU(S->h_items.ensure(sizeof(ItemDev<T>) * n));
-  CU(S->items.ensure(sizeof(ItemDev<T>) * n));
+  const int n = (int)sl.act.size();
+  cudaStream_t s = sl.stream;
+  std::vector<tb_plan*> plans(n);
   size_t svn = 0;
-  for (auto& a : S->active) svn += a.req->items[a.idx].sv.size();
-  CU(S->h_sv.ensure(std::max<size_t>(svn, 16)));
-  CU(S->sv.ensure(std::max<size_t>(svn, 16)));
-  CU(S->h_rv.ensure(sizeof(float) * n));
-  CU(S->rv.ensure(sizeof(float) * n));
-  CU(S->h_out.ensure(sizeof(float) * n));
-  CU(S->out.ensure(sizeof(float) * n));
-  ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(S->h_items.p);
-  int8_t* hsv = reinterpret_cast<int8_t*>(S->h_sv.p);
-  float* hr = reinterpret_cast<float*>(S->h_rv.p);
+  for (int i = 0; i < n; i++) {
+    plans[i] = sl.act[i].plan;
+    svn += sl.act[i].req->items[sl.act[i].idx].sv.size();
+  }
+  const std::vector<GroupKey> gk = sorted_groups(n, plans.data(), false);
+  const size_t ng = std::max<size_t>(gk.size(), 1);
+  CU(sl.h_items.ensure(sizeof(ItemDev<T>) * n));
+  CU(sl.items.ensure(sizeof(ItemDev<T>) * n));
+  CU(sl.h_groups.ensure(sizeof(Group) * ng));
+  CU(sl.groups.ensure(sizeof(Group) * ng));
+  CU(sl.h_sv.ensure(std::max<size_t>(svn, 16)));
+  CU(sl.sv.ensure(std::max<size_t>(svn, 16)));
+  CU(sl.h_rv.ensure(sizeof(float) * n));
+  CU(sl.rv.ensure(sizeof(float) * n));
+  CU(sl.h_out.ensure(sizeof(float) * n + 64));
+  CU(sl.out.ensure(sizeof(float) * n + 64));
+  ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(sl.h_items.p);
+  int8_t* hsv = reinterpret_cast<int8_t*>(sl.h_sv.p);
+  float* hr = reinterpret_cast<float*>(sl.h_rv.p);
   size_t so = 0;
   for (int i = 0; i < n; i++) {
-    const auto& a = S->active[i];
+    const auto& a = sl.act[i];
     const auto& qi = a.req->items[a.idx];
     tb_plan* p = a.plan;
     ItemDev<T> it{};
@@ -1946,7 +1986,9 @@ static tb_status serve_step(Server* S) {
     it.tiles = reinterpret_cast<const TileDesc*>(p->d_tiles.p);
     it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
-    it.slice_vals = reinterpret_cast<const int8_t*>(S->sv.p) + so;
+    it.slice_vals = reinterpret_cast<const int8_t*>(sl.sv.p) + so;
+    it.w = nullptr;  // the leaves take their weights from LeafDesc::w (refreshed at submit)
+    it.flags = (c->opt.gemm_i16 && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = 0;
@@ -1957,151 +1999,155 @@ static tb_status serve_step(Server* S) {
     so += qi.sv.size();
     hr[i] = qi.r;
   }
-  // groups of this step: kind 1 first, then kind 2
-  std::vector<Group> g1, g2;
-  int64_t t1 = 0, t2 = 0;
-  for (int i = 0; i < n; i++) {
-    const auto& a = S->active[i];
-    const PlanHost& h = a.plan->h;
-    for (int32_t si : h.levels[a.level]) {
-      const Step& st = h.steps[si];
-      if (st.kind == STEP_GEMM) {
-        g2.push_back({i, si, t2});
-        t2 += st.n_tiles;
-      } else {
-        g1.push_back({i, si, t1});
-        t1 += st.n_tiles;
-      }
+  Group* hg = reinterpret_cast<Group*>(sl.h_groups.p);
+  fill_groups(gk, plans.data(), hg, sl.ranges);
+  CU(cudaMemcpyAsync(sl.items.p, hi, sizeof(ItemDev<T>) * n, cudaMemcpyHostToDevice, s));
+  if (svn) CU(cudaMemcpyAsync(sl.sv.p, hsv, svn, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(sl.rv.p, hr, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(sl.groups.p, hg, sizeof(Group) * gk.size(), cudaMemcpyHostToDevice, s));
+  float* dout = reinterpret_cast<float*>(sl.out.p);
+  int* derr = reinterpret_cast<int*>(dout + n);  // error word after the results
+  CU(cudaMemsetAsync(derr, 0, sizeof(int), s));
+  const ItemDev<T>* di = reinterpret_cast<const ItemDev<T>*>(sl.items.p);
+  const Group* dg = reinterpret_cast<const Group*>(sl.groups.p);
+  const float* drv = reinterpret_cast<const float*>(sl.rv.p);
+  for (const auto& lr : sl.ranges) {
+    if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
+    const Group* lg = dg + lr.g0;
+    const int lng = lr.g1 - lr.g0;
+    if (lr.kinds == 2) {
+      const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
+      CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), s, di, lg, lng, lr.first, lr.first + lr.count,
+                             (lr.count + grid - 1) / grid, dout, drv, derr)));
+    } else if (c->stream_wide) {
+      const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas_wide);
+      CU((launch_level<T, 5>((unsigned)grid, smem_bytes(1), s, di, lg, lng, lr.first, lr.first + lr.count,
+                             (lr.count + grid - 1) / grid, dout, drv, derr)));
+    } else {
+      const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
+      CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, di, lg, lng, lr.first, lr.first + lr.count,
+                             (lr.count + grid - 1) / grid, dout, drv, derr)));
     }
-  }
-  const size_t ng = g1.size() + g2.size();
-  CU(S->h_groups.ensure(sizeof(Group) * std::max<size_t>(ng, 1)));
-  CU(S->groups.ensure(sizeof(Group) * std::max<size_t>(ng, 1)));
-  Group* hg = reinterpret_cast<Group*>(S->h_groups.p);
-  std::copy(g1.begin(), g1.end(), hg);
-  std::copy(g2.begin(), g2.end(), hg + g1.size());
-  cudaStream_t s = S->stream;
-  CU(cudaMemcpyAsync(S->items.p, hi, sizeof(ItemDev<T>) * n, cudaMemcpyHostToDevice, s));
-  if (svn) CU(cudaMemcpyAsync(S->sv.p, hsv, svn, cudaMemcpyHostToDevice, s));
-  CU(cudaMemcpyAsync(S->rv.p, hr, sizeof(float) * n, cudaMemcpyHostToDevice, s));
-  CU(cudaMemcpyAsync(S->groups.p, hg, sizeof(Group) * ng, cudaMemcpyHostToDevice, s));
-  CU(cudaMemsetAsync(S->err.p, 0, 16, s));
-  const ItemDev<T>* di = reinterpret_cast<const ItemDev<T>*>(S->items.p);
-  const Group* dg = reinterpret_cast<const Group*>(S->groups.p);
-  float* dout = reinterpret_cast<float*>(S->out.p);
-  const float* drv = reinterpret_cast<const float*>(S->rv.p);
-  int* derr = reinterpret_cast<int*>(S->err.p);
-  if (t1 > 0) {
-    const int64_t grid = std::min<int64_t>(t1, c->stream_ctas);
-    CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, di, dg, (int)g1.size(), 0, t1, (t1 + grid - 1) / grid,
-                                                                   dout, drv, derr)));
-    CU(cudaGetLastError());
     S->launches++;
   }
-  if (t2 > 0) {
-    if (t2 > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "step too large for one launch");
-    const int64_t grid2 = std::min<int64_t>(t2, c->gemm_ctas);
-    CU((launch_level<T, 2>((unsigned)grid2, smem_bytes(2), s, di, dg + g1.size(), (int)g2.size(), 0, t2,
-                                                                   (t2 + grid2 - 1) / grid2, dout, drv, derr)));
-    CU(cudaGetLastError());
-    S->launches++;
-  }
-  CU(cudaMemcpyAsync(S->h_out.p, dout, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
-  int herr = 0;
-  CU(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CU(cudaStreamSynchronize(s));
+  // results and the error word back to the host, then the completion event
+  CU(cudaMemcpyAsync(sl.h_out.p, dout, sizeof(float) * n + sizeof(int), cudaMemcpyDeviceToHost, s));
+  CU(cudaEventRecord(sl.done, s));
   S->steps++;
-  if (herr) return fail(TB_ERR_TIMEOUT, "a bounded device-side wait timed out");
-  // advance every item; collect finished ones
-  const float* ho = reinterpret_cast<const float*>(S->h_out.p);
-  std::vector<Server::Active> keep;
+  return TB_OK;
+}
+
+// A cohort's event has completed (or its launch failed): take its results,
+// free its memory and slot, complete requests whose last item it held.
+static void serve_finish(Server* S, Server::Slot& sl, tb_status st, const std::string& msg) {
+  const int n = (int)sl.act.size();
+  const float* ho = reinterpret_cast<const float*>(sl.h_out.p);
+  if (st == TB_OK && *reinterpret_cast<const int*>(ho + n) != 0) {
+    st = TB_ERR_TIMEOUT;
+  }
   for (int i = 0; i < n; i++) {
-    Server::Active a = S->active[i];
-    a.level++;
-    if (a.level >= (int)a.plan->h.levels.size()) {
-      tb_request* q = a.req;
+    Server::Active& a = sl.act[i];
+    tb_request* q = a.req;
+    S->palloc.release(a.off, a.elems);
+    if (st != TB_OK) {
+      serve_complete(q, st, st == TB_ERR_TIMEOUT && msg.empty() ? "a bounded device-side wait timed out" : msg);
+    } else {
+      std::unique_lock<std::mutex> lq(q->m);
       q->result = std::max(q->result, ho[i]);
-      S->palloc.release(a.off, a.elems);
-      if (--q->items_left == 0) {
-        serve_finish<T>(S, q);
+      const bool last = --q->items_left == 0;
+      lq.unlock();
+      if (last) {
+        serve_complete(q, TB_OK, "");
         S->completed++;
       }
-    } else {
-      keep.push_back(a);
     }
   }
-  S->active.swap(keep);
-  return TB_OK;
+  S->n_active -= n;
+  S->active_items = S->n_active;
+  sl.act.clear();
+  sl.busy = false;
+}
+
+// Admit queued requests (whole requests, first come first served) into a
+// free slot while pool memory and item slots allow; returns whether a cohort
+// was formed.
+static bool serve_admit(Server* S, Server::Slot& sl) {
+  while (!S->pending.empty()) {
+    tb_request* q = S->pending.front();
+    if (S->n_active + (int)sl.act.size() + (int)q->items.size() > S->max_items &&
+        !(S->n_active == 0 && sl.act.empty()))
+      break;
+    std::vector<Server::Active> adm;
+    bool ok = true;
+    for (int k = 0; k < (int)q->items.size(); k++) {
+      tb_plan* p = q->items[k].plan;
+      const int64_t off = S->palloc.alloc(p->h.arena_elems);
+      if (off < 0) {
+        ok = false;
+        break;
+      }
+      adm.push_back({q, k, p, off, p->h.arena_elems});
+    }
+    if (!ok) {
+      for (auto& a : adm) S->palloc.release(a.off, a.elems);
+      if (S->n_active == 0 && sl.act.empty()) {
+        // cannot fit even alone: fail the request
+        S->pending.pop_front();
+        serve_complete(q, TB_ERR_OOM, "request needs more device memory than the serving pool");
+        continue;
+      }
+      break;
+    }
+    S->pending.pop_front();
+    {
+      std::lock_guard<std::mutex> lq(q->m);
+      q->state = 1;
+      q->t_start = now_s();
+    }
+    for (auto& a : adm) sl.act.push_back(a);
+  }
+  return !sl.act.empty();
 }
 
 template <typename T>
 static void serve_loop(Server* S) {
   cudaSetDevice(S->ctx->device);
   while (true) {
+    bool busy = false;
     {
       std::unique_lock<std::mutex> lk(S->qm);
-      // admit while slots and memory allow
-      while (!S->pending.empty()) {
-        tb_request* q = S->pending.front();
-        if ((int)(S->active.size() + q->items.size()) > S->max_items && !S->active.empty()) break;
-        std::vector<Server::Active> adm;
-        bool ok = true;
-        for (int k = 0; k < (int)q->items.size(); k++) {
-          tb_plan* p = q->items[k].plan;
-          int64_t off = S->palloc.alloc(p->h.arena_elems);
-          if (off < 0) {
-            ok = false;
-            break;
-          }
-          adm.push_back({q, k, p, off, p->h.arena_elems, 0});
-        }
-        if (!ok) {
-          for (auto& a : adm) S->palloc.release(a.off, a.elems);
-          if (S->active.empty()) {
-            // cannot fit even alone: fail the request
-            S->pending.pop_front();
-            std::lock_guard<std::mutex> lq(q->m);
-            q->status = TB_ERR_OOM;
-            q->err = "request needs more device memory than the serving pool";
-            q->state = 2;
-            q->t_done = now_s();
-            q->cv.notify_all();
-            continue;
-          }
-          break;
-        }
-        S->pending.pop_front();
-        {
-          std::lock_guard<std::mutex> lq(q->m);
-          q->state = 1;
-          q->t_start = now_s();
-        }
-        for (auto& a : adm) S->active.push_back(a);
+      // completions
+      for (auto& sl : S->slots) {
+        if (!sl.busy) continue;
+        const cudaError_t e = cudaEventQuery(sl.done);
+        if (e == cudaErrorNotReady) continue;
+        serve_finish(S, sl, e == cudaSuccess ? TB_OK : TB_ERR_CUDA,
+                     e == cudaSuccess ? "" : std::string("serving: ") + cudaGetErrorString(e));
       }
-      if (S->active.empty()) {
-        if (S->stop) break;
+      // admissions into free slots
+      for (auto& sl : S->slots) {
+        if (sl.busy || S->pending.empty()) continue;
+        if (!serve_admit(S, sl)) break;
+        const int n = (int)sl.act.size();
+        S->n_active += n;
+        S->active_items = S->n_active;
+        sl.busy = true;
+        const tb_status st = serve_launch<T>(S, sl);
+        if (st != TB_OK) {
+          cudaStreamSynchronize(sl.stream);  // nothing of it may still run
+          serve_finish(S, sl, st, g_err);
+        }
+      }
+      for (auto& sl : S->slots) busy = busy || sl.busy;
+      if (!busy) {
+        if (S->stop && S->pending.empty()) break;
         S->qcv.wait_for(lk, std::chrono::milliseconds(2));
         continue;
       }
     }
-    tb_status st = serve_step<T>(S);
-    if (st != TB_OK) {
-      // fail every active request; the server keeps running
-      std::string msg = g_err;
-      for (auto& a : S->active) {
-        S->palloc.release(a.off, a.elems);
-        tb_request* q = a.req;
-        std::lock_guard<std::mutex> lq(q->m);
-        if (q->state != 2) {
-          q->status = st;
-          q->err = msg;
-          q->state = 2;
-          q->t_done = now_s();
-          q->cv.notify_all();
-        }
-      }
-      S->active.clear();
-    }
+    // cohorts in flight: poll again shortly (a submission also wakes the loop)
+    std::unique_lock<std::mutex> lk(S->qm);
+    S->qcv.wait_for(lk, std::chrono::microseconds(50));
   }
 }
 
@@ -2123,9 +2169,11 @@ tb_status tb_serve_start(tb_ctx* c, int64_t pool_bytes, int32_t max_items) {
   S->pool_elems = pool_bytes / 4;
   S->max_items = max_items > 0 ? max_items : 4096;
   CU(S->pool.ensure((size_t)S->pool_elems * 4));
-  CU(S->err.ensure(64));
   S->palloc.reset(S->pool_elems);
-  CU(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  for (auto& sl : S->slots) {
+    CU(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+  }
   Server* raw = S.release();
   raw->th = c->opt.dtype == TB_DTYPE_F32 ? std::thread(serve_loop<float>, raw) : std::thread(serve_loop<int32_t>, raw);
   g_servers[c] = raw;
@@ -2146,15 +2194,13 @@ tb_status tb_serve_stop(tb_ctx* c) {
     S->stop = true;
   }
   S->qcv.notify_all();
-  S->th.join();  // drains admitted work; requests still queued are failed below
-  for (tb_request* q : S->pending) {
-    std::lock_guard<std::mutex> lq(q->m);
-    q->status = TB_ERR_INVALID;
-    q->err = "server stopped";
-    q->state = 2;
-    q->cv.notify_all();
+  S->th.join();  // runs every queued and admitted request to completion
+  for (tb_request* q : S->pending) serve_complete(q, TB_ERR_INVALID, "server stopped");
+  for (auto& sl : S->slots) {
+    cudaStreamSynchronize(sl.stream);
+    cudaEventDestroy(sl.done);
+    cudaStreamDestroy(sl.stream);
   }
-  cudaStreamDestroy(S->stream);
   delete S;
   return TB_OK;
 }
@@ -2234,7 +2280,7 @@ tb_status tb_serve_stats(tb_ctx* c, int64_t* steps, int64_t* launches, int64_t* 
   if (steps) *steps = S->steps;
   if (launches) *launches = S->launches;
   if (completed) *completed = S->completed;
-  if (active) *active = (int64_t)S->active.size();
+  if (active) *active = S->active_items;
   return TB_OK;
 }
 

@@ -3,13 +3,18 @@
 A request is one graph: the host side prepares it (kernelization, contraction
 order, index slicing when its space complexity exceeds a cap) into one or more
 items (plan, slice values, r); the engine's owner thread admits requests as
-device memory and item slots free up and runs every admitted item's current
-tree level in each step, so new requests overlap with running ones.
+device memory, item slots and stream slots free up, and runs the requests
+admitted together as one cohort on its own stream without waiting for it, so
+new requests overlap with running ones.
 
 The workload generator restates the serving mix: 3-regular graphs and
 King's subgraphs at filling 0.8, unit or U{1..10} weights, arriving as a
-Poisson process (sizes capped where this host's order search keeps every
-request tractable).
+Poisson process.  King's subgraphs span L in [10, 36] (the reductions leave
+kernels of sc <= ~18 even at L = 36).  3-regular graphs stop at n = 200: the
+work of a contraction order of a random 3-regular graph grows about as
+2^(0.16 n) (this host's annealer: ~2^31 at n = 180, ~2^42 at n = 220 after two
+seconds of annealing), so n = 400 (~2^64) is out of reach of any order and of
+any serving latency.
 """
 from __future__ import annotations
 
@@ -56,8 +61,13 @@ def prepare(engine: Engine, g: Graph, w, sc_cap: float = 24.0, name: str = "", s
         p.constant = float(kr.r)
         return p
     code = _order.initialize_code(kr.g, _order.GreedyMethod(seed))
-    code = _order.treesa(code, _order.TreeSA(sc_target=sc_cap, betas=np.arange(1.0, 15.0, 1.0), ntrials=2,
-                                             niters=20, seed=seed, nthreads=1))
+    # larger kernels get a longer anneal: their work grows as 2^tc
+    big = kr.g.n > 150
+    code = _order.treesa(code, _order.TreeSA(sc_target=sc_cap if not big else 20.0,
+                                             betas=np.arange(0.5 if big else 1.0, 20.0 if big else 15.0,
+                                                             0.1 if big else 1.0),
+                                             ntrials=8 if big else 2, niters=100 if big else 20, seed=seed,
+                                             nthreads=0 if big else 1))
     sliced, cc = _order.greedy_slice(code, sc_cap, 24)
     if cc[1] > sc_cap:
         raise ValueError(f"{name}: space complexity {cc[1]:.0f} after slicing 24 labels exceeds {sc_cap}")
@@ -71,11 +81,10 @@ def prepare(engine: Engine, g: Graph, w, sc_cap: float = 24.0, name: str = "", s
     return p
 
 
-def serving_mix(n_requests: int, seed: int, n_max: int = 200, l_max: int = 24):
+def serving_mix(n_requests: int, seed: int, n_max: int = 200, l_max: int = 36):
     """(name, graph, weights) of the serving mix: 3-regular graphs with even n
-    in [60, n_max] and King's subgraphs with L in [10, l_max].  (Requests up
-    to n=400 / L=36 need order quality beyond this host's annealer: their
-    slices would number in the millions.)"""
+    in [60, n_max] and King's subgraphs with L in [10, l_max] (see the module
+    note on the 3-regular range)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n_requests):
