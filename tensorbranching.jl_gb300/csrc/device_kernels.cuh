@@ -42,6 +42,8 @@ __device__ __forceinline__ void run_small_step(const ItemDev<T>& it, const Step&
                                                const float* r, int item) {
   if (st.kind == STEP_LEAVES) leaves_tile<T>(it.leaves, it.n_leaves, it.slice_vals, it.arena, (int)tile, it.w);
   else if (st.kind == STEP_FINAL) final_tile<T>(it.fin, it.arena, r ? r[item] : 0.0f, out_item + item);
+  else if (st.kind == STEP_FILL && (it.flags & 2)) fill_tile<T>(it.gemms[st.desc], it.arena, tile);
+  // STEP_FILL without bit 1 and STEP_KRED with it have nothing to do
 }
 
 __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int64_t tk) {
@@ -95,13 +97,13 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
         const ItemDev<T>& it = items[g.item];
         const Step& st = it.steps[g.step];
         const int64_t g_first = g.first;
-        if ((KINDS & 1) && st.kind == STEP_TILE) {
+        if ((KINDS & 1) && (st.kind == STEP_TILE || (st.kind == STEP_KRED && !(it.flags & 2)))) {
           stream_tiles<T>(it.tiles[st.desc], tk - g_first, g_end - g_first, it.arena, tb_smem, err);
         } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
           // a timed-out copy wait (err set) may leave copies in flight into
           // this CTA's shared memory: use it no further
           if (!gemm_tiles_any<T>(it.gemms[st.desc], tk - g_first, g_end - g_first, it.arena, tb_smem, err,
-                                 (it.flags & 1) != 0))
+                                 (it.flags & 1) != 0, (it.flags & 2) != 0))
             return;
         } else {
           for (int64_t x = tk; x < g_end; x++) run_small_step<T>(it, st, x - g_first, out_item, r, g.item);
@@ -160,10 +162,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
     const Group g = groups[ch.group];
     const ItemDev<T>& it = items[g.item];
     const Step& st = it.steps[g.step];
-    if (st.kind == STEP_TILE) {
+    if (st.kind == STEP_TILE || (st.kind == STEP_KRED && !(it.flags & 2))) {
       stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
     } else if (st.kind == STEP_GEMM) {
-      if (!gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0))
+      if (!gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0,
+                             (it.flags & 2) != 0))
         return;  // err is set; copies may still be landing in this CTA's shared memory
     } else {
       for (int64_t x = ch.t0; x < ch.t1; x++) run_small_step<T>(it, st, x, out_item, r, g.item);

@@ -94,6 +94,7 @@ struct tb_plan {
   bool structure_uploaded = false;
   bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
   bool i16_ok = false;         // bound weights are integers >= 0 summing below 8192
+  bool nonneg_ok = false;      // bound weights are >= 0: every tensor value is >= 0 or -inf
   bool mis_checked = false;    // leaves checked to be vertex / edge tensors
   std::vector<int> vertex_leaves;
   uint64_t version = 0;        // bumps when device buffers move
@@ -387,6 +388,9 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     // exact packed-int16 GEMM tiles only when the context allows them and
     // the per-call weights are the plan's bound ones (the batched solves)
     it.flags = (c->opt.gemm_i16 && w_off && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
+    // split-K parts by atomic max where every value is >= 0 or -inf (int32:
+    // always), with the plan's bound weights
+    if (w_off && (!std::is_same<T, float>::value || p->nonneg_ok)) it.flags |= 2;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = done_base;
@@ -418,7 +422,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   std::vector<int64_t> level_tiles;
   for (const GroupKey& x : gk) {
     const Step& st = plans[x.item]->h.steps[x.step];
-    if (st.kind != STEP_TILE) continue;
+    if (st.kind != STEP_TILE && st.kind != STEP_KRED && st.kind != STEP_FILL) continue;
     if ((int)level_tiles.size() <= x.level) level_tiles.resize(x.level + 1, 0);
     level_tiles[x.level] += st.n_tiles;
   }
@@ -428,7 +432,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     const Step& st = plans[gk[g].item]->h.steps[gk[g].step];
     const int64_t nt = st.n_tiles;
     int64_t cs = 1;
-    if (st.kind == STEP_TILE) {
+    if (st.kind == STEP_TILE || st.kind == STEP_KRED || st.kind == STEP_FILL) {
       const int64_t lt = level_tiles[gk[g].level];
       const int64_t div = std::max(1, c->chunk_div) * ctas;
       cs = std::max((nt + ctas - 1) / ctas, (lt + div - 1) / div);
@@ -1133,9 +1137,10 @@ tb_status tb_plan_bind_mis(tb_plan* p, const float* w) {
   p->weights.assign(w, w + p->h.n_labels);
   p->h.has_weights = true;
   p->leaves_dirty = true;
-  if (ok16 != p->i16_ok) {
+  if (ok16 != p->i16_ok || nonneg != p->nonneg_ok) {
     p->i16_ok = ok16;
-    p->version = ++p->ctx->plan_counter;  // captured batches hold the flag
+    p->nonneg_ok = nonneg;
+    p->version = ++p->ctx->plan_counter;  // captured batches hold the flags
   }
   return TB_OK;
 }
@@ -1989,6 +1994,7 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
     it.slice_vals = reinterpret_cast<const int8_t*>(sl.sv.p) + so;
     it.w = nullptr;  // the leaves take their weights from LeafDesc::w (refreshed at submit)
     it.flags = (c->opt.gemm_i16 && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
+    if (!std::is_same<T, float>::value || p->nonneg_ok) it.flags |= 2;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = 0;

@@ -941,6 +941,27 @@ __global__ void __launch_bounds__(256) gemm_k1(const T* __restrict__ A, const T*
 // ---------------------------------------------------------------------------
 // fused GEMM tile: k-pair interleaved operands staged by bulk async copies
 // ---------------------------------------------------------------------------
+// Atomic max into the output of a split-K node.  int32: the integer max.
+// f32: the int max of the bits, exact for values >= 0 and -inf (the only
+// negative one, whose bits are a negative int): what MIS networks with
+// weights >= 0 hold.  The output starts at kFillBits (STEP_FILL).
+template <typename T>
+__device__ __forceinline__ void red_max(T* p, T v) {
+  if constexpr (std::is_same<T, float>::value) atomicMax(reinterpret_cast<int*>(p), __float_as_int(v));
+  else atomicMax(reinterpret_cast<int*>(p), (int)v);
+}
+
+// STEP_FILL tile: kFillPerTile elements of a split-K node's output set to
+// kFillBits (16-byte stores; the output is 32-element aligned).
+template <typename T>
+__device__ __forceinline__ void fill_tile(const GemmDesc& d, T* __restrict__ arena, int64_t tile) {
+  const int64_t size = int64_t(1) << (d.m_log2 + d.n_log2 + d.bt_log2);
+  int4* c = reinterpret_cast<int4*>(arena + d.c_fin);
+  const int4 v = make_int4(kFillBits, kFillBits, kFillBits, kFillBits);
+  for (int64_t q = tile * (kFillPerTile / 4) + threadIdx.x; q < (tile + 1) * (kFillPerTile / 4) && 4 * q < size;
+       q += kThreads)
+    c[q] = v;
+}
 constexpr int kGemmStages = 3;
 constexpr int kGemmBK = 32;
 
@@ -1038,7 +1059,7 @@ __device__ __forceinline__ void gemm_issue(const GemmDesc& d, int64_t u0, int q,
 // wait (err is set; copies in flight are drained with a bounded wait).
 template <typename T, int BM, int BN, int S = kGemmStages, int BK = kGemmBK, bool I16 = false>
 __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restrict__ arena, int* __restrict__ smem,
-                           int* err) {
+                           int* err, bool kpart_atomic = false) {
   using SM = GemmSmem<BM, BN, S, BK, I16>;
   constexpr int KP = SM::KP;
   constexpr int TM = BM / 16, TN = BN / 16;
@@ -1148,14 +1169,15 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
       }
     }
     // epilogue: scatter the tile into C's layout (part p of a split K at
-    // c_off + p 2^(m+n+bt))
+    // c_off + p 2^(m+n+bt), or by atomic max into the output c_fin)
     {
       const int tm_log2 = d.m_log2 - d.bm_log2, tmn_log2 = tm_log2 + d.n_log2 - d.bn_log2;
       const int64_t u = u0 + ui;
       const int64_t mn = u & ((int64_t(1) << tmn_log2) - 1), rest = u >> tmn_log2;
       const int64_t b = rest & ((int64_t(1) << d.bt_log2) - 1), part = rest >> d.bt_log2;
       const int mt = (int)(mn & ((int64_t(1) << tm_log2) - 1)), nt = (int)(mn >> tm_log2);
-      int64_t cb = d.c_off + (part << (d.m_log2 + d.n_log2 + d.bt_log2));
+      const bool atomic = kpart_atomic && d.ks_log2 > 0;
+      int64_t cb = atomic ? d.c_fin : d.c_off + (part << (d.m_log2 + d.n_log2 + d.bt_log2));
       for (int x = 0; x < d.bt_log2; x++)
         if ((b >> x) & 1) cb += int64_t(1) << d.b_pc[x];
       for (int x = d.bm_log2; x < d.m_log2; x++)
@@ -1169,7 +1191,14 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
         if constexpr (I16) return unpack_max_i16(acc[i][j]);
         else return acc[i][j];
       };
-      if (TM >= 4 && d.m_pc[0] == 0) {
+      if (atomic) {
+#pragma unroll
+        for (int i = 0; i < TM; i++) {
+          T* ro = Cb + scM[gm_row<TM, BM>(wm, lm, i)];
+#pragma unroll
+          for (int j = 0; j < TN; j++) red_max<T>(ro + scN[gm_col<TN, BN>(wn, ln, j)], out(i, j));
+        }
+      } else if (TM >= 4 && d.m_pc[0] == 0) {
 #pragma unroll
         for (int i = 0; i < TM; i += 2) {
           T* ro = Cb + scM[gm_row<TM, BM>(wm, lm, i)];
@@ -1217,23 +1246,23 @@ __device__ __forceinline__ bool gemm_tile(const GemmDesc& d, int64_t tile, T* ar
 // Dispatch on the CTA tile shape chosen by the plan compiler.
 template <typename T>
 __device__ __forceinline__ bool gemm_tiles_any(const GemmDesc& d, int64_t u0, int64_t u1, T* arena, int* smem,
-                                               int* err, bool i16 = false) {
+                                               int* err, bool i16 = false, bool kpart_atomic = false) {
   // copy stages: as many as fit the shared memory of the 128 x 128 form
   const int bm = d.bm_log2, bn = d.bn_log2;
   if constexpr (std::is_same<T, float>::value) {
     // exact packed-int16 arithmetic for the large tiles (see pack_i16)
     if (i16) {
-      if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 2, kGemmBK, true>(d, u0, u1, arena, smem, err);
-      if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 3, kGemmBK, true>(d, u0, u1, arena, smem, err);
-      if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 3, kGemmBK, true>(d, u0, u1, arena, smem, err);
+      if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 2, kGemmBK, true>(d, u0, u1, arena, smem, err, kpart_atomic);
+      if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 3, kGemmBK, true>(d, u0, u1, arena, smem, err, kpart_atomic);
+      if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 3, kGemmBK, true>(d, u0, u1, arena, smem, err, kpart_atomic);
     }
   }
-  if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 3>(d, u0, u1, arena, smem, err);
-  if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 4>(d, u0, u1, arena, smem, err);
-  if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 4>(d, u0, u1, arena, smem, err);
-  if (bm == 6 && bn == 6) return gemm_tiles<T, 64, 64, 6>(d, u0, u1, arena, smem, err);
-  if (bm >= 5 && bn >= 5) return gemm_tiles<T, 32, 32, 8>(d, u0, u1, arena, smem, err);
-  return gemm_tiles<T, 16, 16, 8>(d, u0, u1, arena, smem, err);
+  if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 3>(d, u0, u1, arena, smem, err, kpart_atomic);
+  if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 4>(d, u0, u1, arena, smem, err, kpart_atomic);
+  if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 4>(d, u0, u1, arena, smem, err, kpart_atomic);
+  if (bm == 6 && bn == 6) return gemm_tiles<T, 64, 64, 6>(d, u0, u1, arena, smem, err, kpart_atomic);
+  if (bm >= 5 && bn >= 5) return gemm_tiles<T, 32, 32, 8>(d, u0, u1, arena, smem, err, kpart_atomic);
+  return gemm_tiles<T, 16, 16, 8>(d, u0, u1, arena, smem, err, kpart_atomic);
 }
 template <typename T>
 __device__ __forceinline__ bool gemm_tile_any(const GemmDesc& d, int64_t tile, T* arena, int* smem, int* err) {

@@ -187,7 +187,7 @@ bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
   if (M.size() < 4 || N.size() < 4 || K.size() < 5) return false;  // K >= 32: one pipeline stage
   if (M.size() > 30 || N.size() > 30 || K.size() > 30 || Bt.size() > 30) return false;
   std::memset(&g, 0xff, sizeof(g));
-  g.a_off = a_off; g.b_off = b_off; g.c_off = c_off;
+  g.a_off = a_off; g.b_off = b_off; g.c_off = c_off; g.c_fin = c_off;
   g.m_log2 = (int)M.size(); g.n_log2 = (int)N.size(); g.k_log2 = (int)K.size(); g.bt_log2 = (int)Bt.size();
   // CTA tiles the device dispatches: 128x128, 128x64, 64x128, 64x64, 32x32, 16x16
   int bm = std::min(g.m_log2, 7), bn = std::min(g.n_log2, 7);
@@ -563,10 +563,21 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
         const int64_t csize = int64_t(1) << (g.m_log2 + g.n_log2 + g.bt_log2);
         const int64_t part_off = extra;
         extra = align_up(extra + (csize << ks), 32);
+        g.c_fin = p.off[me];
         g.c_off = part_off;
         g.ks_log2 = ks;
         g.n_tiles <<= ks;
-        Step gs{STEP_GEMM, (int32_t)p.gemms.size(), step_of[a], step_of[b], g.n_tiles, 0};
+        // the K parts combine either by atomic max straight into the output,
+        // which a fill step first sets to the identity (items whose values are
+        // all >= 0 or -inf), or through partials and a max step.  The fill
+        // comes after the A operand's step, and the GEMM waits for the fill.
+        const int32_t gi = (int32_t)p.gemms.size();
+        Step fs{STEP_FILL, gi, step_of[a], -1, (int32_t)((csize + kFillPerTile - 1) / kFillPerTile), 0};
+        fs.level = 1 + p.steps[fs.dep0].level;
+        p.steps.push_back(fs);
+        p.step_node.push_back(-1);
+        p.total_tiles += fs.n_tiles;
+        Step gs{STEP_GEMM, gi, (int32_t)p.steps.size() - 1, step_of[b], g.n_tiles, 0};
         gs.level = 1 + std::max(p.steps[gs.dep0].level, p.steps[gs.dep1].level);
         p.gemms.push_back(g);
         p.steps.push_back(gs);
@@ -579,7 +590,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
         TileDesc d;
         if (!(e = plan_tile(pl, nullptr, p.flabels[me], part_off, -1, p.off[me], d, p.tile_bits)).empty())
           return "node " + std::to_string(j) + " (K parts): " + e;
-        st.kind = STEP_TILE;
+        st.kind = STEP_KRED;
         st.desc = (int32_t)p.tiles.size();
         st.n_tiles = d.n_tiles;
         p.tiles.push_back(d);
@@ -592,6 +603,7 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
         p.total_tiles += st.n_tiles;
         continue;
       }
+      g.c_fin = g.c_off;
       st.kind = STEP_GEMM;
       st.desc = (int32_t)p.gemms.size();
       st.n_tiles = g.n_tiles;
@@ -769,7 +781,7 @@ std::string retile_plan(PlanHost& p, int bits) {
   for (size_t si = 0; si < steps.size(); si++) {
     Step& st = steps[si];
     const int sn = p.step_node[si];
-    if (st.kind == STEP_TILE && sn != -1) {
+    if ((st.kind == STEP_TILE || st.kind == STEP_KRED) && sn != -1) {
       TileDesc d;
       std::string e;
       if (sn >= 0) {

@@ -17,7 +17,16 @@ enum StepKind : int32_t {
   STEP_TILE = 2,    // stream tile contraction (fused permute/reduce/contract)
   STEP_GEMM = 3,    // register-blocked gather GEMM contraction
   STEP_FINAL = 4,   // max over the root tensor + r -> item result
+  STEP_FILL = 5,    // a split-K GEMM node's output set to the atomic identity (items
+                    // whose K parts combine by atomic max; a no-op for the others)
+  STEP_KRED = 6,    // max over a split-K GEMM node's part outputs: a stream tile step
+                    // (items whose K parts go through partials; a no-op for the others)
 };
+
+// The atomic identity STEP_FILL writes: INT_MIN, below every int32 and, read
+// as the bits of a float, below every float >= 0 and -inf.
+constexpr int32_t kFillBits = (int32_t)0x80000000u;
+constexpr int kFillPerTile = 4096;  // elements one STEP_FILL tile writes
 
 // Stream tile contraction:  C[c] = max over reduced labels of A[.] (+ B[.]).
 // The node's labels are split into
@@ -57,6 +66,9 @@ static_assert(sizeof(TileDesc) <= kDescWords * 4 && kDescWords % 4 == 0, "descri
 // output C[m, n, b] is scattered to C's own layout through m_pc / n_pc / b_pc.
 struct GemmDesc {
   int64_t a_off, b_off, c_off;
+  int64_t c_fin;             // the node's output; with a split K, items whose values are
+                             // all >= 0 or -inf (f32) or any int32 max their parts into it
+                             // atomically instead of writing partials at c_off
   int32_t m_log2, n_log2, k_log2, bt_log2;
   int32_t bm_log2, bn_log2;  // CTA tile BM x BN
   int32_t n_tiles;           // (M / BM) (N / BN) 2^bt 2^ks work units
@@ -124,7 +136,8 @@ struct ItemDev {
   const LeafDesc* leaves;
   const int8_t* slice_vals;
   const float* w;      // vertex weights by label (per call), or null: LeafDesc::w
-  int32_t flags;       // bit 0: GEMM tiles may use exact packed-int16 arithmetic
+  int32_t flags;       // bit 0: GEMM tiles may use exact packed-int16 arithmetic;
+                       // bit 1: split-K parts combine by atomic max into the output
   float r;
   int32_t n_leaves;
   int32_t done_base;   // offset of this item's step counters

@@ -51,7 +51,7 @@ class FinalDesc(ctypes.Structure):
 
 
 class GemmDesc(ctypes.Structure):
-    _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64),
+    _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64), ("c_fin", c_int64),
                 ("m_log2", c_int32), ("n_log2", c_int32), ("k_log2", c_int32), ("bt_log2", c_int32),
                 ("bm_log2", c_int32), ("bn_log2", c_int32), ("n_tiles", c_int32), ("ks_log2", c_int32),
                 ("m_pc", c_int8 * 32), ("n_pc", c_int8 * 32), ("b_pc", c_int8 * 32)]
@@ -62,7 +62,7 @@ class PlainRec(ctypes.Structure):
                 ("c", c_int64), ("M", c_int64), ("N", c_int64), ("K", c_int64), ("batch", c_int64)]
 
 
-STEP_LEAVES, STEP_TILE, STEP_GEMM, STEP_FINAL = 1, 2, 3, 4
+STEP_LEAVES, STEP_TILE, STEP_GEMM, STEP_FINAL, STEP_FILL, STEP_KRED = 1, 2, 3, 4, 5, 6
 PLAIN_TILE, PLAIN_GEMM = 1, 2
 
 
@@ -350,9 +350,10 @@ def emu_gemm(rec, arena):
 GEMM_TILES = {(7, 7), (7, 6), (6, 7), (6, 6), (5, 5), (4, 4)}
 
 
-def emu_gemm_step(g, arena, written):
+def emu_gemm_step(g, arena, written, kpart_atomic=False):
     """Fused GEMM tile: k-pair interleaved operands, scatter store to C (or,
-    with a split K, part p of the partials at c_off + p |C|)."""
+    with a split K, part p of the partials at c_off + p |C|, or every part
+    by atomic max of the value bits into the output c_fin)."""
     assert (g.bm_log2, g.bn_log2) in GEMM_TILES
     assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 5
     ks = g.ks_log2
@@ -381,6 +382,15 @@ def emu_gemm_step(g, arena, written):
     sm = scat(g.m_log2, g.m_pc)
     sn = scat(g.n_log2, g.n_pc)
     sb = scat(g.bt_log2, g.b_pc)
+    if kpart_atomic and ks > 0:
+        addr = g.c_fin + sb[None, :, None, None] + sn[None, None, :, None] + sm[None, None, None, :]
+        addr = np.broadcast_to(addr, C.shape).ravel()
+        vals = np.ascontiguousarray(C, np.float32).ravel()
+        assert np.all((vals >= 0) | (vals == -np.inf)), "atomic parts need values >= 0 or -inf"
+        assert np.all(written[addr] == 1), "the output was not filled first"
+        bits = arena.view(np.int32)
+        np.maximum.at(bits, addr, vals.view(np.int32))
+        return
     part = (np.arange(1 << ks, dtype=np.int64) << rc)
     addr = g.c_off + part[:, None, None, None] + sb[None, :, None, None] + sn[None, None, :, None] + \
         sm[None, None, None, :]
@@ -399,8 +409,11 @@ def to_reported(v, flab, lab):
     return v[x]
 
 
-def run_fused(desc, weights, slice_vals=()):
-    """Replay the fused program; returns (root tensor, arena, node views)."""
+def run_fused(desc, weights, slice_vals=(), kpart_atomic=False):
+    """Replay the fused program; returns (root tensor, arena, node views).
+    kpart_atomic: split-K parts combine by atomic max of the value bits into
+    the output after STEP_FILL (the form for values >= 0 or -inf), instead of
+    partials and STEP_KRED."""
     arena = np.full(desc["arena"], np.nan, np.float32)
     written = np.zeros(desc["arena"], np.int32)
     leaves = desc["leaves"]
@@ -416,7 +429,18 @@ def run_fused(desc, weights, slice_vals=()):
     node_of_step = {}
     j = 0
     for si, st in enumerate(desc["steps"]):
-        if st.kind == STEP_TILE:
+        if st.kind == STEP_FILL:
+            if kpart_atomic:
+                g = desc["gemms"][st.desc]
+                size = 1 << (g.m_log2 + g.n_log2 + g.bt_log2)
+                assert g.c_fin % 32 == 0 and g.c_fin + size <= arena.size
+                assert st.n_tiles == -(-size // 4096)
+                arena[g.c_fin:g.c_fin + size].view(np.int32)[:] = np.int32(-2 ** 31)
+                written[g.c_fin:g.c_fin + size] += 1
+            continue
+        if st.kind == STEP_KRED and kpart_atomic:
+            continue
+        if st.kind in (STEP_TILE, STEP_KRED):
             d = desc["tiles"][st.desc]
             expect = None
             if desc["n_nodes"]:
@@ -425,7 +449,7 @@ def run_fused(desc, weights, slice_vals=()):
                 j += 1
             emu_stream_tile(d, arena, written)
         elif st.kind == STEP_GEMM:
-            emu_gemm_step(desc["gemms"][st.desc], arena, written)
+            emu_gemm_step(desc["gemms"][st.desc], arena, written, kpart_atomic)
     fin = desc["fin"]
     root = arena[fin.root_off:fin.root_off + (1 << fin.root_log2)].copy()
     assert np.all(written[fin.root_off:fin.root_off + (1 << fin.root_log2)] == 1), "root not written exactly once"

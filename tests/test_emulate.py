@@ -102,11 +102,18 @@ def test_gemm_steps(tb, orc, lib, shape):
     assert len(gem) == 1
     ks = d["gemms"][gem[0].desc].ks_log2
     assert (ks > 0) == (shape[2] >= 7)
-    root, nodes = emulate.run_fused(d, w)
+    if ks > 0:
+        fills = [s for s in d["steps"] if s.kind == emulate.STEP_FILL]
+        assert len(fills) == 1 and gem[0].dep0 == d["steps"].index(fills[0])
+        assert fills[0].level < gem[0].level
     ref, dumps = orc.execute(code, w, dump=True)
-    assert np.array_equal(root, ref)
-    for a, b in zip(nodes, dumps):
-        assert np.array_equal(a, b)
+    # the K parts through partials and a max step, and by atomic max of the
+    # value bits into the filled output (the weights are >= 0)
+    for atomic in (False, True):
+        root, nodes = emulate.run_fused(d, w, kpart_atomic=atomic)
+        assert np.array_equal(root, ref)
+        for a, b in zip(nodes, dumps):
+            assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("bits", [8, 10, 11])

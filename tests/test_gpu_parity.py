@@ -155,12 +155,13 @@ def test_rebinding_weights_between_solves(tb, orc, engine):
 
 
 @pytest.mark.parametrize("arith", ["f32", "i16x2"])
-@pytest.mark.parametrize("kind", ["small_int", "large_int", "fractional"])
+@pytest.mark.parametrize("kind", ["small_int", "large_int", "fractional", "negative"])
 def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
     """By default GEMM tiles compute in f32; a context opened with
     gemm_arith="i16x2" runs exact packed-int16 GEMM tiles when the weights
-    are integers >= 0 summing below 8192, f32 otherwise; all equal the
-    oracle."""
+    are integers >= 0 summing below 8192, f32 otherwise; split-K parts
+    combine by atomic max when the weights are >= 0, through partials
+    otherwise; all equal the oracle."""
     from cases import gemm_case
 
     eng = engine if arith == "f32" else engine_i16
@@ -170,6 +171,9 @@ def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
             w = (w * 300).astype(np.float32)           # sum > 8192
         elif kind == "fractional":
             w = (w + 0.5).astype(np.float32)
+        elif kind == "negative":
+            # negative values: split-K parts go through partials, not atomics
+            w = (w - 5.0).astype(np.float32)
         plan = eng.plan(code, w)
         ref, dumps = orc.execute(code, w, node_iy=plan.all_node_labels(), dump=True)
         for mode in ("batched", "layered"):
