@@ -466,6 +466,41 @@ def measure(tb, eng, wl, name, args, steps, warmup, plain_steps, flush, dev, ws,
     return res, plans
 
 
+def gemm_square(tb, eng, simt, n=2048, batch=8, reps=5):
+    """The plain path's batched max-plus GEMM (K1, tb_gemm_device) at a dense
+    square shape, M = N = K = n, on device buffers: 2 n^3 batch tropical ops
+    per launch over the mean of `reps` launches (CUDA events on the launching
+    stream, after two warm-up launches)."""
+    import torch
+
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A = torch.randint(0, 64, (batch * n * n,), device="cuda", generator=g).float()
+    B = torch.randint(0, 64, (batch * n * n,), device="cuda", generator=g).float()
+    C = torch.empty(batch * n * n, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(2):
+        eng.gemm(n, n, n, batch, A.data_ptr(), B.data_ptr(), C.data_ptr(), s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        eng.gemm(n, n, n, batch, A.data_ptr(), B.data_ptr(), C.data_ptr(), s.cuda_stream)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    # spot check one output column of one batch against a host max-plus product
+    b, j = batch - 1, n // 3
+    Ah = A[b * n * n:(b + 1) * n * n].view(n, n).T.cpu().numpy()       # [m, k] (column-major storage)
+    Bh = B[b * n * n + j * n:b * n * n + (j + 1) * n].cpu().numpy()     # column j: [k]
+    ref = (Ah + Bh[None, :]).max(axis=1)
+    got = C[b * n * n + j * n:b * n * n + (j + 1) * n].cpu().numpy()
+    ok = bool(np.array_equal(ref, got))
+    ops = 2.0 * n ** 3 * batch
+    return {"kernel": "gemm_k1 (tb_gemm_device)", "M": n, "N": n, "K": n, "batch": batch, "ms": ms,
+            "achieved": ops / (ms / 1000.0) / 1e12, "peak": simt / 1e12, "unit": "TFLOP/s",
+            "frac": ops / (ms / 1000.0) / simt, "dtype": "f32", "column_checked": ok}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -614,6 +649,8 @@ def main():
         "roofline": roof, "kernels": gk, "step_roofline": head["step_roofline"],
         "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
     }
+    if rank == 0:
+        res["gemm_square"] = gemm_square(tb, eng, simt)
     if "plain" in head:
         res["plain"] = head["plain"]
         res["speedup_vs_plain"] = head["plain"]["speedup_vs_plain"]

@@ -124,7 +124,10 @@ typedef struct tb_tune_result {
   int32_t n_tried;     /* configurations timed */
   int32_t stream_ctas_per_sm; /* resident CTAs per SM of the per-level stream kernel:
                                  3 (80 registers a thread) or 2 (128) */
-  int32_t reserved[6];
+  int32_t kpart_atomic; /* 1: split-K GEMM parts combine by atomic max into the
+                           output (items whose values are all >= 0 or -inf);
+                           0: through partials and a max step */
+  int32_t reserved[5];
 } tb_tune_result;
 
 /* Fill *opt with defaults (f32, graphs on, autotune on for TB_MODE_AUTO). */
@@ -217,8 +220,9 @@ tb_status tb_score_trees(tb_ctx* ctx, int32_t n_labels, int32_t n_tensors, const
 /*
  * Choose the stream tile size (tile_bits 8..11) and the executor schedule
  * (persistent launch with 1..2 CTAs per SM and three run lengths, or
- * per-level launches with the stream kernel at 3 or 2 CTAs per SM) for this
- * batch by running it with each setting and
+ * per-level launches with the stream kernel at 3 or 2 CTAs per SM, split-K
+ * parts through partials or by atomic max) for this batch by running it with
+ * each setting and
  * keeping the fastest; the chosen tiles stay in the plans and the schedule in
  * the context for TB_MODE_AUTO.  Arguments as tb_solve_batch.  Runs the batch
  * about 40 times.  No counterpart in the reference (its contraction has no

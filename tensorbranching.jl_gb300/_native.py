@@ -71,7 +71,8 @@ class TbTuneResult(ctypes.Structure):
         ("ms_default", c_double),
         ("n_tried", c_int32),
         ("stream_ctas_per_sm", c_int32),
-        ("reserved", c_int32 * 6),
+        ("kpart_atomic", c_int32),
+        ("reserved", c_int32 * 5),
     ]
 
 

@@ -114,7 +114,8 @@ struct GraphKey {
   std::vector<const tb_plan*> plans;
   std::vector<uint64_t> versions;
   int mode = 0;
-  int sched = 0;  // persistent CTAs and chunk divisor the chunk list was built for
+  int sched = 0;  // persistent CTAs and chunk divisor the chunk list was built for,
+                  // and the stream kernel form and split-K combine the graph holds
   bool operator==(const GraphKey& o) const {
     return plans == o.plans && versions == o.versions && mode == o.mode && sched == o.sched;
   }
@@ -130,6 +131,7 @@ struct tb_ctx {
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   int stream_ctas_wide = 0;  // the same for the 128-register form of the stream level kernel
   bool stream_wide = false;  // per-level stream launches use that form (tb_autotune)
+  bool kpart_atomic = false; // split-K parts combine by atomic max where values allow (tb_autotune)
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   std::vector<int32_t> small_order;   // fused small form: items by shared need, largest first
   std::vector<SmallGroup> small_groups;  // launches over small_order
@@ -390,7 +392,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     it.flags = (c->opt.gemm_i16 && w_off && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
     // split-K parts by atomic max where every value is >= 0 or -inf (int32:
     // always), with the plan's bound weights
-    if (w_off && (!std::is_same<T, float>::value || p->nonneg_ok)) it.flags |= 2;
+    if (c->kpart_atomic && w_off && (!std::is_same<T, float>::value || p->nonneg_ok)) it.flags |= 2;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = done_base;
@@ -683,7 +685,7 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     CU(c->arena.ensure(bytes));
     GraphKey key;
     key.mode = mode;
-    key.sched = c->persistent_ctas * 64 + c->chunk_div;
+    key.sched = (c->persistent_ctas * 64 + c->chunk_div) * 4 + (c->stream_wide ? 1 : 0) + (c->kpart_atomic ? 2 : 0);
     key.plans.reserve(n);
     key.versions.reserve(n);
     for (int i = 0; i < n; i++) {
@@ -879,7 +881,23 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
     }
     c->stream_wide = best_wide;
   }
-  // 4. the fused small form, when every plan has one
+  // 4. split-K GEMM nodes: parts through partials and a max step, or by
+  // atomic max into the output (where every value is >= 0 or -inf)
+  bool has_split = false;
+  for (tb_plan* p : uniq)
+    for (const GemmDesc& g : p->h.gemms) has_split = has_split || g.ks_log2 > 0;
+  bool best_atomic = c->kpart_atomic;
+  if (has_split && best_mode != TB_MODE_FUSED) {
+    c->kpart_atomic = !best_atomic;
+    if ((st = time_batch(c, n, plans, sv, r, best_mode, ms))) return st;
+    res.n_tried++;
+    if (ms < best) {
+      best = ms;
+      best_atomic = c->kpart_atomic;
+    }
+    c->kpart_atomic = best_atomic;
+  }
+  // 5. the fused small form, when every plan has one
   bool all_small = true;
   for (tb_plan* p : uniq) all_small = all_small && p->h.small_ok;
   if (all_small) {
@@ -895,6 +913,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   res.ctas_per_sm = c->persistent_ctas / std::max(1, c->sms);
   res.chunk_div = best_div;
   res.stream_ctas_per_sm = (c->stream_wide ? c->stream_ctas_wide : c->stream_ctas) / std::max(1, c->sms);
+  res.kpart_atomic = c->kpart_atomic ? 1 : 0;
   res.ms = best;
   c->tune = res;
   c->tuned = true;
@@ -1603,6 +1622,16 @@ extern "C" int32_t tbi_ctx_set_stream_wide(tb_ctx* c, int32_t wide) {
   return TB_OK;
 }
 
+// Split-K parts by atomic max into the output where every value is >= 0 or
+// -inf (1), or through partials and a max step (0), as the autotuner may
+// choose; for tests that pin one.
+extern "C" int32_t tbi_ctx_set_kpart_atomic(tb_ctx* c, int32_t atomic) {
+  if (!c) return TB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->kpart_atomic = atomic != 0;
+  return TB_OK;
+}
+
 extern "C" int32_t tbi_ctx_info(const tb_ctx* c, int32_t* out4) {
   if (!c || !out4) return TB_ERR_INVALID;
   out4[0] = c->stream_ctas;
@@ -1994,7 +2023,7 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
     it.slice_vals = reinterpret_cast<const int8_t*>(sl.sv.p) + so;
     it.w = nullptr;  // the leaves take their weights from LeafDesc::w (refreshed at submit)
     it.flags = (c->opt.gemm_i16 && std::is_same<T, float>::value && p->i16_ok) ? 1 : 0;
-    if (!std::is_same<T, float>::value || p->nonneg_ok) it.flags |= 2;
+    if (c->kpart_atomic && (!std::is_same<T, float>::value || p->nonneg_ok)) it.flags |= 2;
     it.r = 0.0f;
     it.n_leaves = p->h.n_tensors;
     it.done_base = 0;

@@ -184,6 +184,16 @@ class Engine:
         f.argtypes = [c_void_p, c_int32]
         _native.check(f(self.ctx, 1 if wide else 0), self.ctx)
 
+    def set_kpart_atomic(self, atomic: bool) -> None:
+        """Split-K GEMM parts by atomic max into the output where every value
+        is >= 0 or -inf (True) or through partials and a max step (False), as
+        the autotuner may choose (tbi_ctx_set_kpart_atomic, an internal engine
+        symbol)."""
+        f = self.lib.tbi_ctx_set_kpart_atomic
+        f.restype = c_int32
+        f.argtypes = [c_void_p, c_int32]
+        _native.check(f(self.ctx, 1 if atomic else 0), self.ctx)
+
     def retile(self, plan: "Plan", bits: int) -> None:
         """Re-plan a plan's stream tiles for up to 2^bits outputs (8..11), as
         the autotuner does (tbi_plan_retile, an internal engine symbol)."""
@@ -220,7 +230,8 @@ class Engine:
         _native.check(st, self.ctx)
         names = {v: k for k, v in _native.MODES.items()}
         return {"mode": names[res.mode], "tile_bits": res.tile_bits, "ctas_per_sm": res.ctas_per_sm,
-                "chunk_div": res.chunk_div, "stream_ctas_per_sm": res.stream_ctas_per_sm, "ms": res.ms,
+                "chunk_div": res.chunk_div, "stream_ctas_per_sm": res.stream_ctas_per_sm,
+                "kpart_atomic": bool(res.kpart_atomic), "ms": res.ms,
                 "ms_default": res.ms_default, "n_tried": res.n_tried}
 
     def solve_batch(self, plans, slice_vals=None, r=None, mode: str = "batched"):

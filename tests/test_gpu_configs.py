@@ -52,13 +52,16 @@ def _solve(eng, workloads, name, modes, max_items=0):
     return wl, items, res
 
 
-@pytest.mark.parametrize("arith", ["f32", "i16x2"])
-def test_rr220_full_contraction(tb, orc, workloads, answers, engine, engine_i16, arith):
+@pytest.mark.parametrize("arith,atomic", [("f32", False), ("f32", True), ("i16x2", False)])
+def test_rr220_full_contraction(tb, orc, workloads, answers, engine, engine_i16, arith, atomic):
     """3-regular n=220: one contraction with tensors up to 2^28 entries, GEMM
-    tiles in f32 and in the exact packed-int16 form; MIS 99 by the oracle
-    (run now) and by the integer program (stored)."""
+    tiles in f32 and in the exact packed-int16 form, the split-K node's parts
+    through partials and by atomic max; MIS 99 by the oracle (run now) and by
+    the integer program (stored)."""
     eng = engine if arith == "f32" else engine_i16
+    eng.set_kpart_atomic(atomic)
     wl, items, res = _solve(eng, workloads, "rr220", ("layered", "batched"))
+    eng.set_kpart_atomic(False)
     ref = orc.solve(items[0]["code"], items[0]["weights"])
     ans = answers["rr220"]
     assert ans["graph_mis"] == [ref] == ans["items"]

@@ -165,7 +165,9 @@ def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
     from cases import gemm_case
 
     eng = engine if arith == "f32" else engine_i16
-    for shape in ((7, 7, 6, 1), (8, 7, 5, 1), (7, 6, 8, 0)):
+    for shape, atomic in (((7, 7, 6, 1), False), ((8, 7, 5, 1), False), ((7, 6, 8, 0), False),
+                          ((7, 6, 8, 0), True)):
+        eng.set_kpart_atomic(atomic)
         g, w, code = gemm_case(tb, *shape)
         if kind == "large_int":
             w = (w * 300).astype(np.float32)           # sum > 8192
@@ -178,7 +180,8 @@ def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
         ref, dumps = orc.execute(code, w, node_iy=plan.all_node_labels(), dump=True)
         for mode in ("batched", "layered"):
             out, mx = eng.solve_batch([plan, plan], r=[0.0, 2.0], mode=mode)
-            assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode, arith)
+            assert mx == np.max(ref) + 2 and out[0] == np.max(ref), (kind, shape, mode, arith, atomic)
+    eng.set_kpart_atomic(False)
 
 
 @pytest.mark.parametrize("wide", [False, True])
