@@ -974,9 +974,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
 __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
   asm volatile("mbarrier.inval.shared.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
@@ -1006,7 +1003,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 template <int BM, int BN, int S = kGemmStages, int BK = kGemmBK, bool I16 = false>
 struct GemmSmem {
   static constexpr int KP = BK / 2;
-  static constexpr int BAR_BYTES = 128;  // full[S] and empty[S] mbarriers
+  static constexpr int BAR_BYTES = 128;  // full[S] mbarriers (room for 16)
   static constexpr int A_STAGE = KP * BM * 2;  // elements
   static constexpr int B_STAGE = KP * BN * 2;
   static constexpr int SCAT_OFF = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;  // epilogue tables
@@ -1069,7 +1066,6 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   static_assert(BK == 32 || BK == 16, "BK");
   const int t = threadIdx.x;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* empty = full + S;
   const T* As = reinterpret_cast<const T*>(reinterpret_cast<char*>(smem) + SM::BAR_BYTES);
   const T* Bs = As + S * SM::A_STAGE;
   int* scM = reinterpret_cast<int*>(reinterpret_cast<char*>(smem) + SM::SCAT_OFF);
@@ -1081,10 +1077,7 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   __syncthreads();  // the previous user of this shared memory is done
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (t == 0)
-    for (int i = 0; i < S; i++) {
-      mbar_init(&full[i], 1);
-      mbar_init(&empty[i], kThreads / 32);
-    }
+    for (int i = 0; i < S; i++) mbar_init(&full[i], 1);
   // C offsets of the tile's rows / columns from their low bits: the scatter
   // is linear over disjoint bits, so a unit adds only its (m0, n0, b) base
   for (int i = t; i < BM; i += kThreads) {
@@ -1104,9 +1097,9 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   if (t == 0)
     for (; issued < S && issued < total_q; issued++) gemm_issue<T, BM, BN, S, BK>(d, u0, issued, issued, arena, smem);
 
-  // A warp that has used a chunk arrives on its empty barrier; thread 0
-  // refills the slot once all warps have.  A timed-out wait clears ok and the
-  // loops run on (results are discarded); the failure is collected at the end.
+  // After a block barrier that ends a chunk, thread 0 refills its slot.  A
+  // timed-out wait clears ok and the loops run on (results are discarded);
+  // the failure is collected at the end.
   bool ok = true;
   int slot = 0;
   uint32_t par = 0;
@@ -1151,16 +1144,18 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
 #pragma unroll 1
         for (int kp = 0; kp < KP; kp++) mp_step_i16<TM, TN, BM, BN>(pk, pk + NA, kp, wm, wn, lm, ln, acc);
       } else {
-#pragma unroll 1
+        // two k-pairs per iteration, so the next one's shared loads are issued
+        // while this one's adds and maxes run
+#pragma unroll 2
         for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[slot]);
+        // every warp is done with this stage: thread 0 refills it at once (a
+        // block barrier per chunk measured faster than per-warp arrivals on
+        // an empty barrier that thread 0 waits on)
+        __syncthreads();
         if (t == 0 && q + S < total_q && ok) {
-          ok = mbar_wait(&empty[slot], par);
-          if (ok) {
-            gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
-            issued = q + S + 1;
-          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // reads above, then async writes
+          gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
+          issued = q + S + 1;
         }
       }
       if (++slot == S) {
@@ -1231,10 +1226,7 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
     return false;
   }
   if (t == 0)
-    for (int i = 0; i < S; i++) {
-      mbar_inval(&full[i]);
-      mbar_inval(&empty[i]);
-    }
+    for (int i = 0; i < S; i++) mbar_inval(&full[i]);
   return true;
 }
 
