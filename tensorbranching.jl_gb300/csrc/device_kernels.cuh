@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_tile(const TileDesc d, T* arena
   extern __shared__ int tb_smem[];
   const int64_t t0 = (int64_t)blockIdx.x * chunk;
   const int64_t t1 = t0 + chunk < d.n_tiles ? t0 + chunk : d.n_tiles;
-  stream_tiles<T>(d, t0, t1, arena, tb_smem);
+  stream_tiles<T, true>(d, t0, t1, arena, tb_smem);
 }
 
 template <typename T>
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
         const Step& st = it.steps[g.step];
         const int64_t g_first = g.first;
         if ((KINDS & 1) && (st.kind == STEP_TILE || (st.kind == STEP_KRED && !(it.flags & 2)))) {
-          stream_tiles<T>(it.tiles[st.desc], tk - g_first, g_end - g_first, it.arena, tb_smem, err);
+          stream_tiles<T, KINDS == 5>(it.tiles[st.desc], tk - g_first, g_end - g_first, it.arena, tb_smem, err);
         } else if ((KINDS & 2) && st.kind == STEP_GEMM) {
           // a timed-out copy wait (err set) may leave copies in flight into
           // this CTA's shared memory: use it no further
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(const ItemDev<T>* it
     const ItemDev<T>& it = items[g.item];
     const Step& st = it.steps[g.step];
     if (st.kind == STEP_TILE || (st.kind == STEP_KRED && !(it.flags & 2))) {
-      stream_tiles<T>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
+      stream_tiles<T, false>(it.tiles[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err);
     } else if (st.kind == STEP_GEMM) {
       if (!gemm_tiles_any<T>(it.gemms[st.desc], ch.t0, ch.t1, it.arena, tb_smem, err, (it.flags & 1) != 0,
                              (it.flags & 2) != 0))

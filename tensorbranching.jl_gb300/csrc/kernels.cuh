@@ -232,7 +232,9 @@ __device__ __forceinline__ void issue_sub(T* __restrict__ dst, const T* __restri
 
 // Per-CTA state of a run of stream tiles: shared-memory tables, the
 // thread's fixed indices and the copy / compute / store cursors.
-template <typename T>
+constexpr int kPreChunks = 2;  // 16-byte copies per thread and operand with precomputed offsets
+
+template <typename T, bool PRE>
 struct StreamRun {
   T* buf0;
   const int* ldA;
@@ -262,11 +264,33 @@ struct StreamRun {
   // compute / store cursor
   int64_t ct;
   int oc, cb, rl;
+  // 16-byte copies whose per-thread source and destination offsets are fixed
+  // for the run (all but the item's base): computed once, when both operands
+  // go by 16-byte chunks and each thread has at most kPreChunks of each.
+  // Only the 128-register forms (PRE) keep the offsets: at 80 registers
+  // they spill and cost more than they save.
+  bool pre;
+  int nca, ncb;
+  int a_src[kPreChunks], a_dst[kPreChunks], b_src[kPreChunks], b_dst[kPreChunks];
 
   __device__ __forceinline__ void issue() {
     T* dst = buf0 + ib * BUF;
-    issue_sub<T>(dst, A0 + (pa_g + pa_l), na, pa, ldA);
-    if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), nb, pb, ldB);
+    if (PRE && pre) {
+      const T* sa = A0 + (pa_g + pa_l);
+#pragma unroll
+      for (int k = 0; k < kPreChunks; k++)
+        if (k < nca) cp_async16(dst + a_dst[k], sa + a_src[k]);
+      if (hasB) {
+        const T* sb = B0 + (pb_g + pb_l);
+        T* db = dst + NA;
+#pragma unroll
+        for (int k = 0; k < kPreChunks; k++)
+          if (k < ncb) cp_async16(db + b_dst[k], sb + b_src[k]);
+      }
+    } else {
+      issue_sub<T>(dst, A0 + (pa_g + pa_l), na, pa, ldA);
+      if (hasB) issue_sub<T>(dst + NA, B0 + (pb_g + pb_l), nb, pb, ldB);
+    }
     ib = ib + 1 == S ? 0 : ib + 1;
     if (pr + 1 < nloop) {
       const int k = __ffs(~pr) - 1;
@@ -319,8 +343,8 @@ struct StreamRun {
 // in-tile reduction terms on; fewer go one add and one max each.
 constexpr int kPairMin = 8;
 
-template <typename T, int OPT, int NTR>
-__device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
+template <typename T, int OPT, int NTR, bool PRE>
+__device__ __forceinline__ void stream_loop_fixed(StreamRun<T, PRE>& R) {
   constexpr int LTR = NTR >= 16 ? 4 : NTR >= 8 ? 3 : NTR >= 4 ? 2 : NTR >= 2 ? 1 : 0;
   static_assert((1 << LTR) == NTR, "NTR is a power of two");
   int ba[LTR > 0 ? LTR : 1], bb[LTR > 0 ? LTR : 1];
@@ -383,8 +407,8 @@ __device__ __forceinline__ void stream_loop_fixed(StreamRun<T>& R) {
 
 // Any shape: unary nodes, reduction splits, longer in-tile reductions.
 // MAXOPT bounds the outputs per thread (1 for tiles of <= 256 outputs).
-template <typename T, int MAXOPT>
-__device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
+template <typename T, int MAXOPT, bool PRE>
+__device__ __forceinline__ void stream_loop_any(StreamRun<T, PRE>& R) {
   const int t = threadIdx.x;
   T acc[MAXOPT];
 #pragma unroll
@@ -440,7 +464,7 @@ __device__ __forceinline__ void stream_loop_any(StreamRun<T>& R) {
 // once, and the operand sub-tiles of the next stream_stages(d) - 1 (tile,
 // loop step) items are copied asynchronously while the current one is
 // reduced.
-template <typename T>
+template <typename T, bool PRE = false>
 __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __restrict__ arena,
                              int* __restrict__ smem, int* err = nullptr) {
   (void)err;  // the per-thread copy pipeline has no waits to bound
@@ -452,7 +476,7 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   }
   __syncthreads();
   const TileDesc& d = *reinterpret_cast<const TileDesc*>(smem);
-  StreamRun<T> R;
+  StreamRun<T, PRE> R;
   R.hasB = d.b_off >= 0;
   R.NA = stream_a_words(d);  // A region (padded), B region follows
   R.BUF = stream_buf_words(d);
@@ -590,38 +614,59 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   const bool fixed = R.hasB && R.split == 0 && ntr <= 16;
   const int shape = R.opt * 32 + ntr;
   __syncthreads();  // tables ready
+  {
+    const int ca = (1 << d.na) >> 2, cbn = R.hasB ? (1 << d.nb) >> 2 : 0;
+    R.pre = PRE && d.pa >= 2 && ca <= kPreChunks * kThreads &&
+            (!R.hasB || (d.pb >= 2 && cbn <= kPreChunks * kThreads));
+    R.nca = R.ncb = 0;
+#pragma unroll
+    for (int k = 0; k < kPreChunks; k++) {
+      R.a_src[k] = R.a_dst[k] = R.b_src[k] = R.b_dst[k] = 0;
+      const int q = t + k * kThreads, j = q << 2;
+      if (R.pre && q < ca) {
+        R.a_dst[k] = swz16(j);
+        R.a_src[k] = (j & ((1 << d.pa) - 1)) + ldA[j >> d.pa];
+        R.nca = k + 1;
+      }
+      if (R.pre && q < cbn) {
+        R.b_dst[k] = swz16(j);
+        R.b_src[k] = (j & ((1 << d.pb) - 1)) + ldB[j >> d.pb];
+        R.ncb = k + 1;
+      }
+    }
+  }
   // prologue: items 0 .. S-2, one commit group each (empty past the end)
   for (int k = 0; k < R.S - 1; k++) R.refill();
   if (fixed) {
     switch (shape) {
-      case 1 * 32 + 1: stream_loop_fixed<T, 1, 1>(R); break;
-      case 1 * 32 + 2: stream_loop_fixed<T, 1, 2>(R); break;
-      case 1 * 32 + 4: stream_loop_fixed<T, 1, 4>(R); break;
-      case 1 * 32 + 8: stream_loop_fixed<T, 1, 8>(R); break;
-      case 1 * 32 + 16: stream_loop_fixed<T, 1, 16>(R); break;
-      case 2 * 32 + 1: stream_loop_fixed<T, 2, 1>(R); break;
-      case 2 * 32 + 2: stream_loop_fixed<T, 2, 2>(R); break;
-      case 2 * 32 + 4: stream_loop_fixed<T, 2, 4>(R); break;
-      case 2 * 32 + 8: stream_loop_fixed<T, 2, 8>(R); break;
-      case 2 * 32 + 16: stream_loop_fixed<T, 2, 16>(R); break;
-      case 4 * 32 + 1: stream_loop_fixed<T, 4, 1>(R); break;
-      case 4 * 32 + 2: stream_loop_fixed<T, 4, 2>(R); break;
-      case 4 * 32 + 4: stream_loop_fixed<T, 4, 4>(R); break;
-      case 4 * 32 + 8: stream_loop_fixed<T, 4, 8>(R); break;
-      case 4 * 32 + 16: stream_loop_fixed<T, 4, 16>(R); break;
-      case 8 * 32 + 1: stream_loop_fixed<T, 8, 1>(R); break;
-      case 8 * 32 + 2: stream_loop_fixed<T, 8, 2>(R); break;
-      case 8 * 32 + 4: stream_loop_fixed<T, 8, 4>(R); break;
-      case 8 * 32 + 8: stream_loop_fixed<T, 8, 8>(R); break;
+      case 1 * 32 + 1: stream_loop_fixed<T, 1, 1, PRE>(R); break;
+      case 1 * 32 + 2: stream_loop_fixed<T, 1, 2, PRE>(R); break;
+      case 1 * 32 + 4: stream_loop_fixed<T, 1, 4, PRE>(R); break;
+      case 1 * 32 + 8: stream_loop_fixed<T, 1, 8, PRE>(R); break;
+      case 1 * 32 + 16: stream_loop_fixed<T, 1, 16, PRE>(R); break;
+      case 2 * 32 + 1: stream_loop_fixed<T, 2, 1, PRE>(R); break;
+      case 2 * 32 + 2: stream_loop_fixed<T, 2, 2, PRE>(R); break;
+      case 2 * 32 + 4: stream_loop_fixed<T, 2, 4, PRE>(R); break;
+      case 2 * 32 + 8: stream_loop_fixed<T, 2, 8, PRE>(R); break;
+      case 2 * 32 + 16: stream_loop_fixed<T, 2, 16, PRE>(R); break;
+      case 4 * 32 + 1: stream_loop_fixed<T, 4, 1, PRE>(R); break;
+      case 4 * 32 + 2: stream_loop_fixed<T, 4, 2, PRE>(R); break;
+      case 4 * 32 + 4: stream_loop_fixed<T, 4, 4, PRE>(R); break;
+      case 4 * 32 + 8: stream_loop_fixed<T, 4, 8, PRE>(R); break;
+      case 4 * 32 + 16: stream_loop_fixed<T, 4, 16, PRE>(R); break;
+      case 8 * 32 + 1: stream_loop_fixed<T, 8, 1, PRE>(R); break;
+      case 8 * 32 + 2: stream_loop_fixed<T, 8, 2, PRE>(R); break;
+      case 8 * 32 + 4: stream_loop_fixed<T, 8, 4, PRE>(R); break;
+      case 8 * 32 + 8: stream_loop_fixed<T, 8, 8, PRE>(R); break;
       default:
-        if (R.opt == 1) stream_loop_any<T, 1>(R);
-        else stream_loop_any<T, kMaxOpt>(R);
+        if (R.opt == 1) stream_loop_any<T, 1, PRE>(R);
+        else stream_loop_any<T, kMaxOpt, PRE>(R);
         break;
     }
   } else if (R.opt == 1) {
-    stream_loop_any<T, 1>(R);
+    stream_loop_any<T, 1, PRE>(R);
   } else {
-    stream_loop_any<T, kMaxOpt>(R);
+    stream_loop_any<T, kMaxOpt, PRE>(R);
   }
   cp_async_wait<0>();
 }
