@@ -130,7 +130,8 @@ struct tb_ctx {
   int persistent_ctas = 0;
   int stream_ctas = 0;  // resident CTAs of the stream-tile kernels
   int stream_ctas_wide = 0;  // the same for the 128-register form of the stream level kernel
-  bool stream_wide = false;  // per-level stream launches use that form (tb_autotune)
+  bool stream_wide = true;   // per-level stream launches use that form (measured faster on
+                             // every benchmark workload; tb_autotune may choose the other)
   bool kpart_atomic = false; // split-K parts combine by atomic max where values allow (tb_autotune)
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   std::vector<int32_t> small_order;   // fused small form: items by shared need, largest first
@@ -820,19 +821,24 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   res.n_tried++;
   // 1. stream tile size under both schedules (per-level launches and the
   // persistent executor prefer different tile sizes)
+  // (per-level launches in both register budgets of the stream kernel)
   int best_bits = base_bits, best_mode = TB_MODE_BATCHED, batched_bits = base_bits;
+  bool best_wide = false;
   double best = ms, best_batched = ms;
   for (int bits = 8; bits <= 11; bits++) {
     retile_all(c, uniq, bits, err);
     if (!err.empty()) return fail(TB_ERR_INVALID, "autotune: " + err);
-    for (int mode : {TB_MODE_BATCHED, TB_MODE_LAYERED}) {
+    for (int form = 0; form < 3; form++) {
+      const int mode = form == 0 ? TB_MODE_BATCHED : TB_MODE_LAYERED;
       if (bits == base_bits && mode == TB_MODE_BATCHED) continue;  // timed above
+      c->stream_wide = form == 2;
       if ((st = time_batch(c, n, plans, sv, r, mode, ms))) return st;
       res.n_tried++;
       if (ms < best) {
         best = ms;
         best_bits = bits;
         best_mode = mode;
+        best_wide = c->stream_wide;
       }
       if (mode == TB_MODE_BATCHED && ms < best_batched) {
         best_batched = ms;
@@ -840,6 +846,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
       }
     }
   }
+  c->stream_wide = best_wide;
   // 2. the persistent executor with 1..max CTAs per SM and coarser or finer
   // runs of stream tiles, at its own best tile size
   int best_cps = c->ctas_per_sm_max, best_div = 4;
@@ -868,20 +875,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
   c->persistent_ctas = c->opt.persistent_ctas > 0 ? c->opt.persistent_ctas : best_cps * c->sms;
   c->chunk_div = best_div;
   c->tune_fallback = best_mode;
-  // 3. per-level launches: the stream level kernel at 80 registers and three
-  // CTAs per SM, or 128 registers and two
-  bool best_wide = c->stream_wide;
-  if (best_mode == TB_MODE_LAYERED) {
-    c->stream_wide = !best_wide;
-    if ((st = time_batch(c, n, plans, sv, r, TB_MODE_LAYERED, ms))) return st;
-    res.n_tried++;
-    if (ms < best) {
-      best = ms;
-      best_wide = c->stream_wide;
-    }
-    c->stream_wide = best_wide;
-  }
-  // 4. split-K GEMM nodes: parts through partials and a max step, or by
+  // 3. split-K GEMM nodes: parts through partials and a max step, or by
   // atomic max into the output (where every value is >= 0 or -inf)
   bool has_split = false;
   for (tb_plan* p : uniq)
@@ -897,7 +891,7 @@ static tb_status autotune_locked(tb_ctx* c, int n, tb_plan* const* plans, const 
     }
     c->kpart_atomic = best_atomic;
   }
-  // 5. the fused small form, when every plan has one
+  // 4. the fused small form, when every plan has one
   bool all_small = true;
   for (tb_plan* p : uniq) all_small = all_small && p->h.small_ok;
   if (all_small) {

@@ -319,11 +319,17 @@ struct StreamRun {
 #pragma unroll
     for (int i = 0; i < N; i++) {
       if (i < opt) {
-        const int c = cl + (i << lo_bits);
-        Ct[(c & cmask) + stC[c >> pc]] = acc[i];
+        if constexpr (PRE) {
+          Ct[st_off[i]] = acc[i];
+        } else {
+          const int c = cl + (i << lo_bits);
+          Ct[(c & cmask) + stC[c >> pc]] = acc[i];
+        }
       }
     }
   }
+  // the thread's output offsets within a tile (fixed for the run)
+  int st_off[PRE ? kMaxOpt : 1];
   __device__ __forceinline__ void next_tile() {
     const int k = __ffsll(~ct) - 1;
     oc += incCg[k];
@@ -614,6 +620,14 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   const bool fixed = R.hasB && R.split == 0 && ntr <= 16;
   const int shape = R.opt * 32 + ntr;
   __syncthreads();  // tables ready
+  if constexpr (PRE) {
+    const int cmask = (1 << d.pc) - 1;
+#pragma unroll
+    for (int i = 0; i < kMaxOpt; i++) {
+      const int c = R.cl + (i << R.lo_bits);
+      R.st_off[i] = i < R.opt ? (c & cmask) + stC[c >> d.pc] : 0;
+    }
+  }
   {
     const int ca = (1 << d.na) >> 2, cbn = R.hasB ? (1 << d.nb) >> 2 : 0;
     R.pre = PRE && d.pa >= 2 && ca <= kPreChunks * kThreads &&

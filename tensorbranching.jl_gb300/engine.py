@@ -177,8 +177,8 @@ class Engine:
 
     def set_stream_wide(self, wide: bool) -> None:
         """Per-level stream launches with 128 registers a thread and two CTAs
-        per SM (True) or 80 and three (False), as the autotuner may choose
-        (tbi_ctx_set_stream_wide, an internal engine symbol)."""
+        per SM (True, the default) or 80 and three (False), as the autotuner
+        may choose (tbi_ctx_set_stream_wide, an internal engine symbol)."""
         f = self.lib.tbi_ctx_set_stream_wide
         f.restype = c_int32
         f.argtypes = [c_void_p, c_int32]

@@ -206,4 +206,4 @@ def test_stream_tile_configurations(tb, orc, engine, bits, wide):
         got = engine.dump(plan, mode="layered")
         for a, b in zip(got, dumps):
             assert np.array_equal(a, b)
-    engine.set_stream_wide(False)
+    engine.set_stream_wide(True)  # the default
