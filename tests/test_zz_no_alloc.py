@@ -23,14 +23,14 @@ def _solve_static(native, code, w):
     return st, out.value, lib.tb_last_error(None).decode()
 
 
-def test_static_matches_solve_batch_twice(tb, native, engine):
+def test_static_matches_solve_batch_twice(tb, orc, native, engine):
     # rr100 seed 3 has stream tiles that need more than 48 KiB of shared memory
     cases = [rr_case(tb, 60, 1), rr_case(tb, 44, 2, weighted=False), rr_case(tb, 100, 3)]
     for g, w, code in cases:  # two calls in a row, different networks
         st, v, msg = _solve_static(native, code, w)
         assert st == 0, msg
         _, ref = engine.solve_batch([engine.plan(code, w)], mode="plain")
-        assert v == ref
+        assert v == ref == orc.solve(code, w)
     # and the first network again, after the second one left its data behind
     g, w, code = cases[0]
     st, v, msg = _solve_static(native, code, w)
