@@ -259,10 +259,11 @@ struct StreamRun {
   int iah[kMaxOpt], ibh[kMaxOpt];
   int64_t n_items;
   // prefetch cursor (tile pt, loop step pr) and its operand offsets
-  int64_t pt, issued;
+  int64_t issued;
+  uint32_t pt;  // tile indices fit 32 bits (TileDesc::n_tiles is an int32)
   int pr, pa_g, pb_g, pa_l, pb_l, ib;
   // compute / store cursor
-  int64_t ct;
+  uint32_t ct;
   int oc, cb, rl;
   // 16-byte copies whose per-thread source and destination offsets are fixed
   // for the run (all but the item's base): computed once, when both operands
@@ -300,7 +301,7 @@ struct StreamRun {
     } else {
       pr = 0;
       pa_l = pb_l = 0;
-      const int k = __ffsll(~pt) - 1;
+      const int k = __ffs(~pt) - 1;
       pa_g += incAg[k];
       pb_g += incBg[k];
       pt++;
@@ -331,7 +332,7 @@ struct StreamRun {
   // the thread's output offsets within a tile (fixed for the run)
   int st_off[PRE ? kMaxOpt : 1];
   __device__ __forceinline__ void next_tile() {
-    const int k = __ffsll(~ct) - 1;
+    const int k = __ffs(~ct) - 1;
     oc += incCg[k];
     ct++;
   }
@@ -606,14 +607,14 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
   R.A0 = arena + d.a_off;
   R.B0 = arena + (R.hasB ? d.b_off : 0);
   R.C0 = arena + d.c_off;
-  R.pt = t0;
+  R.pt = (uint32_t)t0;
   R.issued = 0;
   R.pr = 0;
   R.pa_g = ga;
   R.pb_g = gb;
   R.pa_l = R.pb_l = 0;
   R.ib = 0;
-  R.ct = t0;
+  R.ct = (uint32_t)t0;
   R.oc = gc;
   R.cb = 0;
   R.rl = 0;
