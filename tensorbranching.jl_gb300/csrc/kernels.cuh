@@ -1301,6 +1301,15 @@ __device__ __forceinline__ bool gemm_tiles_any(const GemmDesc& d, int64_t u0, in
                                                int* err, bool i16 = false, bool kpart_atomic = false) {
   // copy stages: as many as fit the shared memory of the 128 x 128 form
   const int bm = d.bm_log2, bn = d.bn_log2;
+  if (d.k_log2 < 5) {
+    // K = 16: one 16-wide chunk a unit; the ring holds the next units' chunks
+    if (bm == 7 && bn == 7) return gemm_tiles<T, 128, 128, 6, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 8, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 8, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    if (bm == 6 && bn == 6) return gemm_tiles<T, 64, 64, 12, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    if (bm >= 5 && bn >= 5) return gemm_tiles<T, 32, 32, 16, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    return gemm_tiles<T, 16, 16, 16, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+  }
   if constexpr (std::is_same<T, float>::value) {
     // exact packed-int16 arithmetic for the large tiles (see pack_i16)
     if (i16) {
@@ -1332,6 +1341,13 @@ static_assert(GemmSmem<128, 64, 4>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<32, 32, 8>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<16, 16, 8>::BYTES <= gemm_smem_bytes_max(),
               "GEMM stages exceed the shared memory of the 128 x 128 form");
-static_assert(2 * 8 * 8 <= 128, "mbarriers of 8 stages");
+static_assert(GemmSmem<128, 128, 6, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<128, 64, 8, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<64, 128, 8, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<64, 64, 12, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<32, 32, 16, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<16, 16, 16, 16>::BYTES <= gemm_smem_bytes_max(),
+              "K=16 GEMM stages exceed the shared memory of the 128 x 128 form");
+static_assert(16 * 8 <= 128, "full mbarriers of 16 stages");
 
 }  // namespace tb

@@ -184,7 +184,7 @@ bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
     if (j >= B.size() || B[j] != Bt[q]) return false;
   if (j != B.size()) return false;
   if (C.size() != M.size() + N.size() + Bt.size()) return false;
-  if (M.size() < 4 || N.size() < 4 || K.size() < 5) return false;  // K >= 32: one pipeline stage
+  if (M.size() < 4 || N.size() < 4 || K.size() < 4) return false;  // K >= 16: one BK = 16 chunk
   if (M.size() > 30 || N.size() > 30 || K.size() > 30 || Bt.size() > 30) return false;
   std::memset(&g, 0xff, sizeof(g));
   g.a_off = a_off; g.b_off = b_off; g.c_off = c_off; g.c_fin = c_off;
@@ -472,8 +472,11 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       if (!ina && inc) N.push_back(l);
       else if (!ina) priv = true;
     }
-    bool gemm = gmin > 0 && !priv && a >= T && b >= T && (int)M.size() >= gmin && (int)N.size() >= gmin &&
-                (int)K.size() >= gmin + 1;
+    // K = 16 (one BK = 16 chunk a tile) pays only with 64 x 64 tiles or
+    // larger: below that the stream tile is faster
+    const int mn_min = (int)K.size() > gmin ? gmin : gmin + 2;
+    bool gemm = gmin > 0 && !priv && a >= T && b >= T && (int)M.size() >= mn_min && (int)N.size() >= mn_min &&
+                (int)K.size() >= gmin;
     auto by_c = [&](std::vector<int32_t>& v, const std::vector<int32_t>& pref) {
       std::stable_sort(v.begin(), v.end(), [&](int32_t x, int32_t y) {
         bool px = index_of(pref, x) >= 0, py = index_of(pref, y) >= 0;

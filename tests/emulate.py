@@ -355,7 +355,7 @@ def emu_gemm_step(g, arena, written, kpart_atomic=False):
     with a split K, part p of the partials at c_off + p |C|, or every part
     by atomic max of the value bits into the output c_fin)."""
     assert (g.bm_log2, g.bn_log2) in GEMM_TILES
-    assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 5
+    assert g.m_log2 >= g.bm_log2 and g.n_log2 >= g.bn_log2 and g.k_log2 >= 4  # K = 16: BK = 16 tiles
     ks = g.ks_log2
     assert 0 <= ks <= 4 and (ks == 0 or g.k_log2 - ks >= 6)
     M, N, K, Bt = 1 << g.m_log2, 1 << g.n_log2, 1 << g.k_log2, 1 << g.bt_log2

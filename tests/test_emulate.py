@@ -90,7 +90,7 @@ def test_invalid_plans_rejected(tb, lib):
 
 
 @pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (4, 4, 8, 0),
-                                   (6, 6, 9, 1), (5, 5, 7, 2)])
+                                   (6, 6, 9, 1), (5, 5, 7, 2), (6, 6, 4, 1), (7, 7, 4, 2), (7, 6, 4, 0)])
 def test_gemm_steps(tb, orc, lib, shape):
     """GEMM steps, including K split into parts plus a max over the parts
     when the output tiles are too few for the GPU."""
@@ -99,7 +99,7 @@ def test_gemm_steps(tb, orc, lib, shape):
     g, w, code = gemm_case(tb, *shape)
     d = emulate.describe(lib, code)
     gem = [s for s in d["steps"] if s.kind == emulate.STEP_GEMM]
-    assert len(gem) == 1
+    assert len(gem) == 1  # K = 16 (k = 4 labels) included: BK = 16 tiles
     ks = d["gemms"][gem[0].desc].ks_log2
     assert (ks > 0) == (shape[2] >= 7)
     if ks > 0:
@@ -114,6 +114,18 @@ def test_gemm_steps(tb, orc, lib, shape):
         assert np.array_equal(root, ref)
         for a, b in zip(nodes, dumps):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("shape,gemm", [((4, 4, 4, 1), False), ((5, 7, 4, 0), False), ((6, 6, 4, 1), True),
+                                         ((4, 4, 5, 1), True)])
+def test_gemm_threshold(tb, lib, shape, gemm):
+    """A node with K = 16 becomes a GEMM only when M and N are >= 64 (64 x 64
+    tiles or larger); with K >= 32, M and N >= 16 suffice."""
+    from cases import gemm_case
+
+    g, w, code = gemm_case(tb, *shape)
+    d = emulate.describe(lib, code)
+    assert any(s.kind == emulate.STEP_GEMM for s in d["steps"]) == gemm
 
 
 @pytest.mark.parametrize("bits", [8, 10, 11])

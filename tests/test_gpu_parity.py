@@ -112,7 +112,8 @@ def test_contract_generic_tensors(tb, orc, engine):
 
 
 @pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (7, 7, 6, 2),
-                                   (8, 7, 5, 1), (4, 4, 8, 0), (6, 6, 9, 1), (5, 5, 7, 2), (7, 7, 8, 1)])
+                                   (8, 7, 5, 1), (4, 4, 8, 0), (6, 6, 9, 1), (5, 5, 7, 2), (7, 7, 8, 1),
+                                   (6, 6, 4, 1), (7, 7, 4, 2), (7, 6, 4, 0)])
 def test_fused_gemm_nodes(tb, orc, engine, shape):
     from cases import gemm_case
 
@@ -166,7 +167,7 @@ def test_gemm_arithmetic_forms(tb, orc, engine, engine_i16, kind, arith):
 
     eng = engine if arith == "f32" else engine_i16
     for shape, atomic in (((7, 7, 6, 1), False), ((8, 7, 5, 1), False), ((7, 6, 8, 0), False),
-                          ((7, 6, 8, 0), True)):
+                          ((7, 6, 8, 0), True), ((7, 7, 4, 1), False)):
         eng.set_kpart_atomic(atomic)
         g, w, code = gemm_case(tb, *shape)
         if kind == "large_int":
