@@ -1307,6 +1307,8 @@ __device__ __forceinline__ bool gemm_tiles_any(const GemmDesc& d, int64_t u0, in
     if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 8, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
     if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 8, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
     if (bm == 6 && bn == 6) return gemm_tiles<T, 64, 64, 12, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    if (bm == 8) return gemm_tiles<T, 256, 16, 5, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
+    if (bn == 8) return gemm_tiles<T, 16, 256, 5, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
     if (bm >= 5 && bn >= 5) return gemm_tiles<T, 32, 32, 16, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
     return gemm_tiles<T, 16, 16, 16, 16>(d, u0, u1, arena, smem, err, kpart_atomic);
   }
@@ -1322,6 +1324,8 @@ __device__ __forceinline__ bool gemm_tiles_any(const GemmDesc& d, int64_t u0, in
   if (bm == 7 && bn == 6) return gemm_tiles<T, 128, 64, 4>(d, u0, u1, arena, smem, err, kpart_atomic);
   if (bm == 6 && bn == 7) return gemm_tiles<T, 64, 128, 4>(d, u0, u1, arena, smem, err, kpart_atomic);
   if (bm == 6 && bn == 6) return gemm_tiles<T, 64, 64, 6>(d, u0, u1, arena, smem, err, kpart_atomic);
+  if (bm == 8) return gemm_tiles<T, 256, 16, 2>(d, u0, u1, arena, smem, err, kpart_atomic);
+  if (bn == 8) return gemm_tiles<T, 16, 256, 2>(d, u0, u1, arena, smem, err, kpart_atomic);
   if (bm >= 5 && bn >= 5) return gemm_tiles<T, 32, 32, 8>(d, u0, u1, arena, smem, err, kpart_atomic);
   return gemm_tiles<T, 16, 16, 8>(d, u0, u1, arena, smem, err, kpart_atomic);
 }
@@ -1339,14 +1343,18 @@ static_assert(GemmSmem<128, 64, 4>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<64, 128, 4>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<64, 64, 6>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<32, 32, 8>::BYTES <= gemm_smem_bytes_max() &&
-                  GemmSmem<16, 16, 8>::BYTES <= gemm_smem_bytes_max(),
+                  GemmSmem<16, 16, 8>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<256, 16, 2>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<16, 256, 2>::BYTES <= gemm_smem_bytes_max(),
               "GEMM stages exceed the shared memory of the 128 x 128 form");
 static_assert(GemmSmem<128, 128, 6, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<128, 64, 8, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<64, 128, 8, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<64, 64, 12, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<32, 32, 16, 16>::BYTES <= gemm_smem_bytes_max() &&
-                  GemmSmem<16, 16, 16, 16>::BYTES <= gemm_smem_bytes_max(),
+                  GemmSmem<16, 16, 16, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<256, 16, 5, 16>::BYTES <= gemm_smem_bytes_max() &&
+                  GemmSmem<16, 256, 5, 16>::BYTES <= gemm_smem_bytes_max(),
               "K=16 GEMM stages exceed the shared memory of the 128 x 128 form");
 static_assert(16 * 8 <= 128, "full mbarriers of 16 stages");
 

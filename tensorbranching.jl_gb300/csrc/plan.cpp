@@ -189,9 +189,15 @@ bool plan_gemm(const std::vector<int32_t>& A, const std::vector<int32_t>& B,
   std::memset(&g, 0xff, sizeof(g));
   g.a_off = a_off; g.b_off = b_off; g.c_off = c_off; g.c_fin = c_off;
   g.m_log2 = (int)M.size(); g.n_log2 = (int)N.size(); g.k_log2 = (int)K.size(); g.bt_log2 = (int)Bt.size();
-  // CTA tiles the device dispatches: 128x128, 128x64, 64x128, 64x64, 32x32, 16x16
+  // CTA tiles the device dispatches: 128x128, 128x64, 64x128, 64x64, 32x32,
+  // 16x16, and 256x16 / 16x256 when one side is 16 or 32 and the other >= 256
   int bm = std::min(g.m_log2, 7), bn = std::min(g.n_log2, 7);
-  if (bm < 6 || bn < 6) bm = bn = std::min(std::min(bm, bn), 5);
+  if (std::min(g.m_log2, g.n_log2) <= 5 && std::max(g.m_log2, g.n_log2) >= 8) {
+    bm = g.m_log2 >= 8 ? 8 : 4;
+    bn = g.n_log2 >= 8 ? 8 : 4;
+  } else if (bm < 6 || bn < 6) {
+    bm = bn = std::min(std::min(bm, bn), 5);
+  }
   g.bm_log2 = bm;
   g.bn_log2 = bn;
   int64_t nt = (int64_t(1) << (g.m_log2 - g.bm_log2)) * (int64_t(1) << (g.n_log2 - g.bn_log2)) *
@@ -473,10 +479,11 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
       else if (!ina) priv = true;
     }
     // K = 16 (one BK = 16 chunk a tile) pays only with 64 x 64 tiles or
-    // larger: below that the stream tile is faster
-    const int mn_min = (int)K.size() > gmin ? gmin : gmin + 2;
-    bool gemm = gmin > 0 && !priv && a >= T && b >= T && (int)M.size() >= mn_min && (int)N.size() >= mn_min &&
-                (int)K.size() >= gmin;
+    // larger, or the 256 x 16 skinny tiles: below that the stream tile is
+    // faster
+    const int lo = (int)std::min(M.size(), N.size()), hi = (int)std::max(M.size(), N.size());
+    const bool mn_ok = (int)K.size() > gmin ? lo >= gmin : (lo >= gmin + 2 || (lo >= gmin && hi >= 8));
+    bool gemm = gmin > 0 && !priv && a >= T && b >= T && mn_ok && (int)K.size() >= gmin;
     auto by_c = [&](std::vector<int32_t>& v, const std::vector<int32_t>& pref) {
       std::stable_sort(v.begin(), v.end(), [&](int32_t x, int32_t y) {
         bool px = index_of(pref, x) >= 0, py = index_of(pref, y) >= 0;

@@ -347,7 +347,7 @@ def emu_gemm(rec, arena):
     arena[rec.c:rec.c + M * N * B] = C.reshape(-1)
 
 
-GEMM_TILES = {(7, 7), (7, 6), (6, 7), (6, 6), (5, 5), (4, 4)}
+GEMM_TILES = {(7, 7), (7, 6), (6, 7), (6, 6), (5, 5), (4, 4), (8, 4), (4, 8)}
 
 
 def emu_gemm_step(g, arena, written, kpart_atomic=False):

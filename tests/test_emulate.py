@@ -90,7 +90,8 @@ def test_invalid_plans_rejected(tb, lib):
 
 
 @pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (4, 4, 8, 0),
-                                   (6, 6, 9, 1), (5, 5, 7, 2), (6, 6, 4, 1), (7, 7, 4, 2), (7, 6, 4, 0)])
+                                   (6, 6, 9, 1), (5, 5, 7, 2), (6, 6, 4, 1), (7, 7, 4, 2), (7, 6, 4, 0),
+                                   (8, 4, 4, 1), (4, 9, 4, 0), (9, 5, 5, 1), (5, 8, 6, 1)])
 def test_gemm_steps(tb, orc, lib, shape):
     """GEMM steps, including K split into parts plus a max over the parts
     when the output tiles are too few for the GPU."""
@@ -116,16 +117,22 @@ def test_gemm_steps(tb, orc, lib, shape):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("shape,gemm", [((4, 4, 4, 1), False), ((5, 7, 4, 0), False), ((6, 6, 4, 1), True),
-                                         ((4, 4, 5, 1), True)])
-def test_gemm_threshold(tb, lib, shape, gemm):
-    """A node with K = 16 becomes a GEMM only when M and N are >= 64 (64 x 64
-    tiles or larger); with K >= 32, M and N >= 16 suffice."""
+@pytest.mark.parametrize("shape,tile", [((4, 4, 4, 1), None), ((5, 7, 4, 0), None), ((6, 6, 4, 1), (6, 6)),
+                                         ((4, 4, 5, 1), (4, 4)), ((4, 8, 4, 0), (4, 8)), ((9, 5, 4, 1), (8, 4)),
+                                         ((5, 7, 5, 0), (5, 5)), ((7, 6, 5, 0), (7, 6))])
+def test_gemm_threshold(tb, lib, shape, tile):
+    """A node with K = 16 becomes a GEMM only when M and N are >= 64, or one
+    is >= 16 and the other >= 256 (256 x 16 tiles); with K >= 32, M and N >=
+    16 suffice.  The CTA tile (log2 of its rows and columns) follows M and N."""
     from cases import gemm_case
 
     g, w, code = gemm_case(tb, *shape)
     d = emulate.describe(lib, code)
-    assert any(s.kind == emulate.STEP_GEMM for s in d["steps"]) == gemm
+    gem = [s for s in d["steps"] if s.kind == emulate.STEP_GEMM]
+    assert bool(gem) == (tile is not None)
+    if gem:
+        gd = d["gemms"][gem[0].desc]
+        assert (gd.bm_log2, gd.bn_log2) == tile
 
 
 @pytest.mark.parametrize("bits", [8, 10, 11])

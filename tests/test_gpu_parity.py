@@ -113,7 +113,8 @@ def test_contract_generic_tensors(tb, orc, engine):
 
 @pytest.mark.parametrize("shape", [(4, 4, 5, 1), (5, 4, 6, 2), (6, 6, 5, 0), (7, 5, 5, 1), (7, 7, 6, 2),
                                    (8, 7, 5, 1), (4, 4, 8, 0), (6, 6, 9, 1), (5, 5, 7, 2), (7, 7, 8, 1),
-                                   (6, 6, 4, 1), (7, 7, 4, 2), (7, 6, 4, 0)])
+                                   (6, 6, 4, 1), (7, 7, 4, 2), (7, 6, 4, 0),
+                                   (8, 4, 4, 1), (4, 9, 4, 0), (9, 5, 5, 1), (5, 8, 6, 1)])
 def test_fused_gemm_nodes(tb, orc, engine, shape):
     from cases import gemm_case
 
