@@ -93,6 +93,7 @@ struct tb_plan {
   PlanHost h;
   std::vector<float> weights;  // bound vertex weights by label
   DevBuf d_steps, d_tiles, d_gemms, d_leaves, d_small, d_small_leaf;
+  DevBuf d_steps_merged, d_gemms_merged;  // the split-K GEMMs merged (PlanHost::steps_merged)
   bool structure_uploaded = false;
   bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
   bool i16_ok = false;         // bound weights are integers >= 0 summing below 8192
@@ -138,6 +139,7 @@ struct tb_ctx {
   bool stream_wide = true;   // per-level stream launches use that form (measured faster on
                              // every benchmark workload; tb_autotune may choose the other)
   bool kpart_atomic = false; // split-K parts combine by atomic max where values allow (tb_autotune)
+  bool kpart_merge = true;   // batches whose items fill the GPU run split-K GEMMs merged (merge_choice)
   int gemm_ctas = 0;    // resident CTAs of the GEMM-tile kernels
   std::vector<int32_t> small_order;   // fused small form: items by shared need, largest first
   std::vector<SmallGroup> small_groups;  // launches over small_order
@@ -263,16 +265,22 @@ static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
   if (!p->structure_uploaded || (leaf_weights && p->leaves_dirty))
     for (int i : p->vertex_leaves) h.leaves[i].w = p->weights[h.leaves[i].label];
   if (!p->structure_uploaded) {
-    void* before[6] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p};
+    void* before[8] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p,
+                       p->d_steps_merged.p, p->d_gemms_merged.p};
     CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
     CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
     CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
+    if (h.has_split) {
+      CU(up(p->d_steps_merged, h.steps_merged.data(), h.steps_merged.size() * sizeof(Step)));
+      CU(up(p->d_gemms_merged, h.gemms_merged.data(), h.gemms_merged.size() * sizeof(GemmDesc)));
+    }
     CU(up(p->d_leaves, h.leaves.data(), h.leaves.size() * sizeof(LeafDesc)));
     if (h.small_ok) {
       CU(up(p->d_small, h.small.empty() ? nullptr : h.small.data(), h.small.size() * sizeof(SmallNode)));
       CU(up(p->d_small_leaf, h.small_leaf.data(), h.small_leaf.size() * sizeof(int32_t)));
     }
-    void* after[6] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p};
+    void* after[8] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p,
+                      p->d_steps_merged.p, p->d_gemms_merged.p};
     // captured graphs hold these device pointers: a move invalidates them
     if (std::memcmp(before, after, sizeof(before)) != 0) p->version = ++p->ctx->plan_counter;
     p->structure_uploaded = true;
@@ -330,15 +338,53 @@ struct GroupKey {
   int level, kinds, tiny, item, step;
 };
 
+// Steps of item i of a batch: the merged split-K form where merged[i].
+static const std::vector<Step>& batch_steps(tb_plan* const* plans, const char* merged, int i) {
+  const PlanHost& h = plans[i]->h;
+  return merged && merged[i] ? h.steps_merged : h.steps;
+}
+
+// Which items run their split-K GEMMs merged (one pass over the whole K, no
+// partials and no max step): those whose plan, over all the batch's items
+// that share it, keeps >= 90% of the GEMM CTA slots of the last wave busy
+// without the split at every split GEMM.  The plan compiler split K for one
+// item alone; a batch of many items fills the GPU by itself.
+static std::vector<char> merge_choice(const tb_ctx* c, int n, tb_plan* const* plans) {
+  std::vector<char> m(n, 0);
+  if (!c->kpart_merge) return m;
+  std::unordered_map<const tb_plan*, int> count;
+  for (int i = 0; i < n; i++)
+    if (plans[i]->h.has_split) count[plans[i]]++;
+  std::unordered_map<const tb_plan*, char> ok;
+  const int64_t ctas = std::max(1, c->gemm_ctas);
+  for (const auto& kv : count) {
+    bool good = true;
+    for (const GemmDesc& g : kv.first->h.gemms) {
+      if (g.ks_log2 == 0) continue;
+      const int64_t units = (int64_t)kv.second * (g.n_tiles >> g.ks_log2);
+      good = good && (double)units >= 0.9 * (double)(((units + ctas - 1) / ctas) * ctas);
+    }
+    ok[kv.first] = good;
+  }
+  for (int i = 0; i < n; i++) {
+    auto f = ok.find(plans[i]);
+    m[i] = f != ok.end() && f->second;
+  }
+  return m;
+}
+
 // The batch's steps in launch order: by tree level, then kind (stream-like
-// before GEMM), tiny steps first, then item and step.
-static std::vector<GroupKey> sorted_groups(int n, tb_plan* const* plans, bool skip_leaves) {
+// before GEMM), tiny steps first, then item and step.  Steps without tiles
+// (the fill and max steps of a merged split-K GEMM) are left out.
+static std::vector<GroupKey> sorted_groups(int n, tb_plan* const* plans, bool skip_leaves, const char* merged) {
   std::vector<GroupKey> gk;
   for (int i = 0; i < n; i++) {
     const PlanHost& h = plans[i]->h;
-    for (int s = 0; s < (int)h.steps.size(); s++) {
-      const Step& st = h.steps[s];
+    const std::vector<Step>& steps = batch_steps(plans, merged, i);
+    for (int s = 0; s < (int)steps.size(); s++) {
+      const Step& st = steps[s];
       if (skip_leaves && st.kind == STEP_LEAVES) continue;
+      if (st.n_tiles == 0) continue;
       gk.push_back({st.level, st.kind == STEP_GEMM ? 2 : 1, st.kind == STEP_TILE && tiny_step(h.tiles[st.desc]),
                     i, s});
     }
@@ -355,7 +401,7 @@ static std::vector<GroupKey> sorted_groups(int n, tb_plan* const* plans, bool sk
 
 // Groups (host copy, gk.size() entries) and one launch range per (level,
 // kind); returns the number of tickets.
-static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plans, Group* hg,
+static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plans, const char* merged, Group* hg,
                            std::vector<tb_ctx::LevelRange>& ranges) {
   int64_t tk = 0;
   ranges.clear();
@@ -374,7 +420,7 @@ static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plan
       cur_level = gk[g].level;
       cur_kinds = gk[g].kinds;
     }
-    const int64_t nt = p->h.steps[gk[g].step].n_tiles;
+    const int64_t nt = batch_steps(plans, merged, gk[g].item)[gk[g].step].n_tiles;
     tk += nt;
     ranges.back().count += nt;
     ranges.back().g1 = (int)g + 1;
@@ -388,14 +434,15 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   // items
   CU(c->h_items.ensure(sizeof(ItemDev<T>) * n));
   ItemDev<T>* hi = reinterpret_cast<ItemDev<T>*>(c->h_items.p);
+  const std::vector<char> merged = merge_choice(c, n, plans);
   int done_base = 0;
   for (int i = 0; i < n; i++) {
     tb_plan* p = plans[i];
     ItemDev<T> it{};
     it.arena = reinterpret_cast<T*>(c->arena.p) + arena_off[i];
-    it.steps = reinterpret_cast<const Step*>(p->d_steps.p);
+    it.steps = reinterpret_cast<const Step*>(merged[i] ? p->d_steps_merged.p : p->d_steps.p);
     it.tiles = reinterpret_cast<const TileDesc*>(p->d_tiles.p);
-    it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
+    it.gemms = reinterpret_cast<const GemmDesc*>(merged[i] ? p->d_gemms_merged.p : p->d_gemms.p);
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
     it.slice_vals = reinterpret_cast<const int8_t*>(c->slice_vals.p) + sv_off[i];
     it.w = w_off ? reinterpret_cast<const float*>(c->wvals.p) + (*w_off)[i] : nullptr;
@@ -421,10 +468,10 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
     done_base += it.n_steps;
     hi[i] = it;
   }
-  std::vector<GroupKey> gk = sorted_groups(n, plans, skip_leaves);
+  std::vector<GroupKey> gk = sorted_groups(n, plans, skip_leaves, merged.data());
   CU(c->h_groups.ensure(sizeof(Group) * std::max<size_t>(gk.size(), 1)));
   Group* hg = reinterpret_cast<Group*>(c->h_groups.p);
-  const int64_t tk = fill_groups(gk, plans, hg, c->level_ranges);
+  const int64_t tk = fill_groups(gk, plans, merged.data(), hg, c->level_ranges);
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
   // chunks for the persistent executor: runs of stream tiles (tables are
@@ -435,7 +482,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   // not turn into as many tiny runs.
   std::vector<int64_t> level_tiles;
   for (const GroupKey& x : gk) {
-    const Step& st = plans[x.item]->h.steps[x.step];
+    const Step& st = batch_steps(plans, merged.data(), x.item)[x.step];
     if (st.kind != STEP_TILE && st.kind != STEP_KRED && st.kind != STEP_FILL) continue;
     if ((int)level_tiles.size() <= x.level) level_tiles.resize(x.level + 1, 0);
     level_tiles[x.level] += st.n_tiles;
@@ -443,7 +490,7 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   const int64_t ctas = std::max(1, c->persistent_ctas);
   std::vector<Chunk> chs;
   for (size_t g = 0; g < gk.size(); g++) {
-    const Step& st = plans[gk[g].item]->h.steps[gk[g].step];
+    const Step& st = batch_steps(plans, merged.data(), gk[g].item)[gk[g].step];
     const int64_t nt = st.n_tiles;
     int64_t cs = 1;
     if (st.kind == STEP_TILE || st.kind == STEP_KRED || st.kind == STEP_FILL) {
@@ -713,7 +760,8 @@ static tb_status solve_batch_t(tb_ctx* c, int n, tb_plan* const* plans, const in
     CU(c->arena.ensure(bytes));
     GraphKey key;
     key.mode = mode;
-    key.sched = (c->persistent_ctas * 64 + c->chunk_div) * 4 + (c->stream_wide ? 1 : 0) + (c->kpart_atomic ? 2 : 0);
+    key.sched = ((c->persistent_ctas * 64 + c->chunk_div) * 4 + (c->stream_wide ? 1 : 0) + (c->kpart_atomic ? 2 : 0)) *
+                    2 + (c->kpart_merge ? 1 : 0);
     key.plans.reserve(n);
     key.versions.reserve(n);
     for (int i = 0; i < n; i++) {
@@ -1511,7 +1559,8 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
   struct PlainRec { int32_t node, kind; TileDesc tile; int64_t a, b, c, M, N, K, batch; };
   size_t bytes = 8 * 9 + total * 8 + total * 4 + nlab * 8 + h.steps.size() * sizeof(Step) +
                  h.tiles.size() * sizeof(TileDesc) + h.leaves.size() * sizeof(LeafDesc) + sizeof(FinalDesc) +
-                 h.gemms.size() * sizeof(GemmDesc) + nplain * sizeof(PlainRec);
+                 h.gemms.size() * sizeof(GemmDesc) + nplain * sizeof(PlainRec) + h.steps.size() * sizeof(Step) +
+                 h.gemms.size() * sizeof(GemmDesc);
   char* b = (char*)std::malloc(bytes);
   if (!b) return TB_ERR_OOM;
   char* p = b;
@@ -1539,6 +1588,10 @@ extern "C" int32_t tbi_plan_describe(int32_t n_labels, int32_t n_tensors, const 
       rec.a = op.a_off; rec.b = op.b_off; rec.c = op.c_off; rec.M = op.M; rec.N = op.N; rec.K = op.K; rec.batch = op.batch;
       std::memcpy(p, &rec, sizeof(rec)); p += sizeof(rec);
     }
+  // the merged split-K form, same counts as steps and gemms
+  std::memcpy(p, h.steps_merged.data(), h.steps.size() * sizeof(Step)); p += h.steps.size() * sizeof(Step);
+  if (!h.gemms.empty()) std::memcpy(p, h.gemms_merged.data(), h.gemms.size() * sizeof(GemmDesc));
+  p += h.gemms.size() * sizeof(GemmDesc);
   *blob = b;
   *blob_bytes = (int64_t)bytes;
   return TB_OK;
@@ -1655,6 +1708,15 @@ extern "C" int32_t tbi_ctx_set_kpart_atomic(tb_ctx* c, int32_t atomic) {
   if (!c) return TB_ERR_INVALID;
   std::lock_guard<std::mutex> lk(c->mu);
   c->kpart_atomic = atomic != 0;
+  return TB_OK;
+}
+
+// Split-K GEMMs of batches whose items fill the GPU run merged (1, the
+// default) or always as the plan split them (0); for tests that pin one.
+extern "C" int32_t tbi_ctx_set_kpart_merge(tb_ctx* c, int32_t merge) {
+  if (!c) return TB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->kpart_merge = merge != 0;
   return TB_OK;
 }
 
@@ -2020,7 +2082,8 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
     plans[i] = sl.act[i].plan;
     svn += sl.act[i].req->items[sl.act[i].idx].sv.size();
   }
-  const std::vector<GroupKey> gk = sorted_groups(n, plans.data(), false);
+  const std::vector<char> merged = merge_choice(c, n, plans.data());
+  const std::vector<GroupKey> gk = sorted_groups(n, plans.data(), false, merged.data());
   const size_t ng = std::max<size_t>(gk.size(), 1);
   CU(sl.h_items.ensure(sizeof(ItemDev<T>) * n));
   CU(sl.items.ensure(sizeof(ItemDev<T>) * n));
@@ -2042,9 +2105,9 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
     tb_plan* p = a.plan;
     ItemDev<T> it{};
     it.arena = reinterpret_cast<T*>(S->pool.p) + a.off;
-    it.steps = reinterpret_cast<const Step*>(p->d_steps.p);
+    it.steps = reinterpret_cast<const Step*>(merged[i] ? p->d_steps_merged.p : p->d_steps.p);
     it.tiles = reinterpret_cast<const TileDesc*>(p->d_tiles.p);
-    it.gemms = reinterpret_cast<const GemmDesc*>(p->d_gemms.p);
+    it.gemms = reinterpret_cast<const GemmDesc*>(merged[i] ? p->d_gemms_merged.p : p->d_gemms.p);
     it.leaves = reinterpret_cast<const LeafDesc*>(p->d_leaves.p);
     it.slice_vals = reinterpret_cast<const int8_t*>(sl.sv.p) + so;
     it.w = nullptr;  // the leaves take their weights from LeafDesc::w (refreshed at submit)
@@ -2061,7 +2124,7 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
     hr[i] = qi.r;
   }
   Group* hg = reinterpret_cast<Group*>(sl.h_groups.p);
-  fill_groups(gk, plans.data(), hg, sl.ranges);
+  fill_groups(gk, plans.data(), merged.data(), hg, sl.ranges);
   CU(cudaMemcpyAsync(sl.items.p, hi, sizeof(ItemDev<T>) * n, cudaMemcpyHostToDevice, s));
   if (svn) CU(cudaMemcpyAsync(sl.sv.p, hsv, svn, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(sl.rv.p, hr, sizeof(float) * n, cudaMemcpyHostToDevice, s));

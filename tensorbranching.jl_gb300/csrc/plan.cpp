@@ -674,8 +674,39 @@ std::string compile_plan(const PlanInput& in, PlanHost& p, int gemm_min_log2) {
   }
   p.plain_elems = fused_end + scratch;
   p.arena_elems = extra;  // the plain path never touches the K-part partials
+  merge_split_k(p);
   compile_small(p);
   return "";
+}
+
+void merge_split_k(PlanHost& p) {
+  p.steps_merged = p.steps;
+  p.gemms_merged = p.gemms;
+  p.has_split = false;
+  std::vector<int32_t> to(p.steps.size());
+  for (size_t si = 0; si < p.steps.size(); si++) to[si] = (int32_t)si;
+  for (size_t si = 0; si < p.steps.size(); si++) {
+    const Step& st = p.steps[si];
+    if (st.kind == STEP_GEMM && p.gemms[st.desc].ks_log2 > 0) {
+      GemmDesc& g = p.gemms_merged[st.desc];
+      g.n_tiles >>= g.ks_log2;
+      g.ks_log2 = 0;
+      g.c_off = g.c_fin;
+      Step& m = p.steps_merged[si];
+      m.n_tiles = g.n_tiles;
+      const Step& fill = p.steps[st.dep0];  // the fill waits on the A operand's step
+      m.dep0 = fill.dep0;
+      p.steps_merged[st.dep0].n_tiles = 0;
+      p.has_split = true;
+    } else if (st.kind == STEP_KRED) {
+      p.steps_merged[si].n_tiles = 0;
+      to[si] = st.dep0;  // its GEMM step
+    }
+  }
+  for (Step& m : p.steps_merged) {
+    if (m.dep0 >= 0) m.dep0 = to[m.dep0];
+    if (m.dep1 >= 0) m.dep1 = to[m.dep1];
+  }
 }
 
 void compile_small(PlanHost& p) {
@@ -814,6 +845,7 @@ std::string retile_plan(PlanHost& p, int bits) {
   p.steps.swap(steps);
   p.total_tiles = total;
   p.tile_bits = bits;
+  merge_split_k(p);
   return "";
 }
 

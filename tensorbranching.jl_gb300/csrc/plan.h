@@ -70,6 +70,14 @@ struct PlanHost {
   std::vector<int32_t> step_node;              // node a step contracts (-1: leaves, final); a split-K
                                                // reduce step holds -2 - node
   std::vector<int64_t> split_off;              // per node: arena offset of its K-part partials (-1)
+  // The same program with every split-K GEMM merged back into one pass over
+  // the whole K (for batches whose items fill the GPU without the split):
+  // the GEMM step writes the output directly and waits on the A operand's
+  // step, the fill and max-over-parts steps have no tiles, and steps that
+  // waited on the max wait on the GEMM.  Same step indices and levels.
+  bool has_split = false;
+  std::vector<Step> steps_merged;
+  std::vector<GemmDesc> gemms_merged;
 
   // fused small form (compile_small): every tensor in the reported label
   // order, leaves packed first, intermediates placed by first fit, every
@@ -91,6 +99,8 @@ std::string compile_plan(const PlanInput& in, PlanHost& out, int gemm_min_log2);
 // Re-plan every stream-tile step of the fused form with tiles of up to
 // 2^bits outputs (8..11); GEMM steps and the arena layout are unchanged.
 std::string retile_plan(PlanHost& p, int bits);
+// Fill has_split, steps_merged and gemms_merged from steps and gemms.
+void merge_split_k(PlanHost& p);
 
 // Plan one stream tile for C = max_{R} A (+ B).  A, C (and B if non-null)
 // are label lists in their memory order.  Returns "" or an error.

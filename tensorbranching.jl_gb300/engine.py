@@ -194,6 +194,16 @@ class Engine:
         f.argtypes = [c_void_p, c_int32]
         _native.check(f(self.ctx, 1 if atomic else 0), self.ctx)
 
+    def set_kpart_merge(self, merge: bool) -> None:
+        """Split-K GEMMs of batches whose items fill the GPU without the
+        split run as one pass over the whole K (True, the default) or always
+        as the plan split them (False) (tbi_ctx_set_kpart_merge, an internal
+        engine symbol)."""
+        f = self.lib.tbi_ctx_set_kpart_merge
+        f.restype = c_int32
+        f.argtypes = [c_void_p, c_int32]
+        _native.check(f(self.ctx, 1 if merge else 0), self.ctx)
+
     def retile(self, plan: "Plan", bits: int) -> None:
         """Re-plan a plan's stream tiles for up to 2^bits outputs (8..11), as
         the autotuner does (tbi_plan_retile, an internal engine symbol)."""

@@ -125,10 +125,48 @@ def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4, tile_bits=9):
     fin = take(FinalDesc, 1)[0]
     gemms = take(GemmDesc, ngemm)
     plain = take(PlainRec, nplain)
+    # the merged split-K form (PlanHost::steps_merged, gemms_merged)
+    steps_merged = take(Step, n_steps)
+    gemms_merged = take(GemmDesc, ngemm)
     assert p == len(raw)
     return dict(n_tensors=n_tensors, n_nodes=n_nodes, steps=steps, tiles=tiles, leaves=leaves, fin=fin,
                 plain=plain, off=offs, rank=ranks, arena=arena, plain_elems=plain_elems, gemms=gemms,
-                labels=labels, flabels=flabels)
+                labels=labels, flabels=flabels, steps_merged=steps_merged, gemms_merged=gemms_merged)
+
+
+def merged(desc):
+    """The descriptor with its merged split-K form as the program."""
+    d = dict(desc)
+    d["steps"], d["gemms"] = desc["steps_merged"], desc["gemms_merged"]
+    return d
+
+
+def dep_order(steps):
+    """An order of the steps that follows only their dependencies (not the
+    list or level order), taking the latest ready step first, with the
+    steps that have no tiles left out.  A step without tiles counts as done
+    from the start, as in the persistent executor (its done count 0 meets
+    its tile count 0).  A dependency missing from the program shows up as a
+    read of an unwritten operand."""
+    n = len(steps)
+    deps = [[d for d in (s.dep0, s.dep1) if d >= 0] if s.n_tiles > 0 else [] for s in steps]
+    users = [[] for _ in range(n)]
+    for i, ds in enumerate(deps):
+        for d in ds:
+            users[d].append(i)
+    left = [len(ds) for ds in deps]
+    ready = [i for i in range(n) if left[i] == 0]
+    out = []
+    while ready:
+        ready.sort()
+        i = ready.pop()
+        out.append(i)
+        for u in users[i]:
+            left[u] -= 1
+            if left[u] == 0:
+                ready.append(u)
+    assert len(out) == n, "dependency cycle"
+    return [i for i in out if steps[i].n_tiles > 0]
 
 
 def swz(j):
@@ -364,6 +402,8 @@ def emu_gemm_step(g, arena, written, kpart_atomic=False):
                      [g.b_pc[i] for i in range(g.bt_log2)], [], [])
     for x, n in ((g.a_off, M * K * Bt), (g.b_off, N * K * Bt), (g.c_off, (1 << rc) << ks)):
         assert 0 <= x and x + n <= arena.size and x % 32 == 0
+    for x, n in ((g.a_off, M * K * Bt), (g.b_off, N * K * Bt)):
+        assert np.all(written[x:x + n] == 1), "GEMM operand not written before the GEMM step"
     # bulk copies: rows of 2*BM (2*BN) elements at 2*m0 within a k-pair row
     BM, BN = 1 << g.bm_log2, 1 << g.bn_log2
     assert (2 * BM * 4) % 16 == 0 and (2 * BN * 4) % 16 == 0
@@ -409,11 +449,11 @@ def to_reported(v, flab, lab):
     return v[x]
 
 
-def run_fused(desc, weights, slice_vals=(), kpart_atomic=False):
+def run_fused(desc, weights, slice_vals=(), kpart_atomic=False, by_deps=False):
     """Replay the fused program; returns (root tensor, arena, node views).
     kpart_atomic: split-K parts combine by atomic max of the value bits into
     the output after STEP_FILL (the form for values >= 0 or -inf), instead of
-    partials and STEP_KRED."""
+    partials and STEP_KRED.  by_deps: run the steps in dep_order."""
     arena = np.full(desc["arena"], np.nan, np.float32)
     written = np.zeros(desc["arena"], np.int32)
     leaves = desc["leaves"]
@@ -428,7 +468,9 @@ def run_fused(desc, weights, slice_vals=(), kpart_atomic=False):
     off, rank = desc["off"], desc["rank"]
     node_of_step = {}
     j = 0
-    for si, st in enumerate(desc["steps"]):
+    order = dep_order(desc["steps"]) if by_deps else range(len(desc["steps"]))
+    for si in order:
+        st = desc["steps"][si]
         if st.kind == STEP_FILL:
             if kpart_atomic:
                 g = desc["gemms"][st.desc]

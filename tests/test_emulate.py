@@ -109,9 +109,26 @@ def test_gemm_steps(tb, orc, lib, shape):
         assert fills[0].level < gem[0].level
     ref, dumps = orc.execute(code, w, dump=True)
     # the K parts through partials and a max step, and by atomic max of the
-    # value bits into the filled output (the weights are >= 0)
+    # value bits into the filled output (the weights are >= 0), in list order
+    # and in an order that follows only the dependencies
     for atomic in (False, True):
-        root, nodes = emulate.run_fused(d, w, kpart_atomic=atomic)
+        for by_deps in (False, True):
+            root, nodes = emulate.run_fused(d, w, kpart_atomic=atomic, by_deps=by_deps)
+            assert np.array_equal(root, ref)
+            for a, b in zip(nodes, dumps):
+                assert np.array_equal(a, b)
+    # the merged form (batches that fill the GPU): one pass over the whole K
+    # into the output, the fill and max steps without tiles
+    m = emulate.merged(d)
+    g0, g1 = d["gemms"][gem[0].desc], m["gemms"][gem[0].desc]
+    si = d["steps"].index(gem[0])
+    assert g1.ks_log2 == 0 and g1.c_off == g0.c_fin and g1.n_tiles == g0.n_tiles >> ks
+    assert m["steps"][si].n_tiles == g1.n_tiles
+    for k, st in enumerate(d["steps"]):
+        if st.kind in (emulate.STEP_FILL, emulate.STEP_KRED):
+            assert m["steps"][k].n_tiles == 0
+    for atomic in (False, True):
+        root, nodes = emulate.run_fused(m, w, kpart_atomic=atomic, by_deps=True)
         assert np.array_equal(root, ref)
         for a, b in zip(nodes, dumps):
             assert np.array_equal(a, b)

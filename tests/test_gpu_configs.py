@@ -140,3 +140,23 @@ def test_sliced_batches(tb, orc, workloads, answers, engine, name):
         it = items[k]
         assert ans["items"][k] == orc.solve(it["code"], it["weights"], sliced=it["fixed"],
                                             slice_vals=it["values"])
+
+
+@pytest.mark.parametrize("merge,atomic", [(False, False), (False, True), (True, True)])
+def test_split_k_forms_in_a_batch(tb, workloads, answers, engine, merge, atomic):
+    """The 64 slices of 3-regular n=220 share one plan whose GEMM splits K
+    for one item alone: the batch fills the GPU, so by default the GEMM runs
+    as one pass over the whole K.  The split form (partials and a max step,
+    or atomic max into the filled output) and the merged one give the same
+    values."""
+    engine.set_kpart_merge(merge)
+    engine.set_kpart_atomic(atomic)
+    try:
+        wl, items, res = _solve(engine, workloads, "rr220w_s22", ("layered", "batched"))
+    finally:
+        engine.set_kpart_merge(True)
+        engine.set_kpart_atomic(False)
+    ans = answers["rr220w_s22"]
+    for mode, (out, mx) in res.items():
+        assert list(out) == ans["items"], (mode, merge, atomic)
+        assert mx == ans["graph_mis"][0]
