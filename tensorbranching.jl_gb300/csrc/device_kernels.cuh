@@ -62,16 +62,22 @@ __device__ __forceinline__ int find_group(const Group* groups, int n_groups, int
 // which the autotuner may choose.
 template <typename T, int KINDS>
 __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const ItemDev<T>* items, const Group* groups, int n_groups,
-                                                   int64_t first_ticket, int64_t last_ticket, int64_t chunk,
-                                                   float* out_item, const float* r, int* err) {
+                                                   const LevelSpan span, float* out_item, const float* r, int* err) {
   extern __shared__ int tb_smem[];
   __shared__ int s_g;
   {
-    // CTA b runs tickets [b * chunk, (b + 1) * chunk) of this level, a run of
+    // CTA b runs one run of tickets of this level (LevelSpan), a run of
     // tiles per group: each stream tile builds its tables once, each GEMM run
     // keeps one copy pipeline across its tiles
-    int64_t tk = first_ticket + (int64_t)blockIdx.x * chunk;
-    const int64_t end = tk + chunk < last_ticket ? tk + chunk : last_ticket;
+    const int b = (int)blockIdx.x;
+    int64_t tk, end;
+    if (b < span.split_cta) {
+      tk = span.first + (int64_t)b * span.chunk;
+      end = tk + span.chunk < span.mid ? tk + span.chunk : span.mid;
+    } else {
+      tk = span.mid + (int64_t)(b - span.split_cta) * span.chunk2;
+      end = tk + span.chunk2 < span.last ? tk + span.chunk2 : span.last;
+    }
     if (tk >= end) return;
     // the first group by binary search, then the following ones in order
     // (the index lives in shared memory, not across the tile code's registers)
@@ -82,13 +88,13 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
       const Group& g = groups[gi];
       int next = gi + 1;
       if ((KINDS & 1) && g.tiny) {
-        // a run of tiny steps (one tile each, listed first in their level):
-        // warp w takes the run's tiles w, w + 8, ...
-        int n = 1;
-        while (gi + n < n_groups && groups[gi + n].first < end && groups[gi + n].tiny) n++;
+        // a run of tiny steps (one tile, so one ticket, each; listed first
+        // in their level) up to the CTA's last ticket or the level's last
+        // tiny step: warp w takes the run's steps w, w + 8, ...
+        const int n = (int)(g.run < end - tk ? g.run : end - tk);
         for (int q = threadIdx.x >> 5; q < n; q += kThreads / 32) {
           const Group& gq = groups[gi + q];
-          tiny_node<T>(gq.tile, items[gq.item].arena);
+          tiny_node<T>(gq.tile, reinterpret_cast<T*>(gq.arena));
         }
         next = gi + n;
         tk = next < n_groups && groups[next].first < end ? groups[next].first : end;
@@ -344,11 +350,10 @@ static cudaError_t level_attr(int smem) {
 
 template <typename T, int KINDS>
 cudaError_t launch_level(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const Group* groups,
-                         int n_groups, int64_t first, int64_t last, int64_t chunk, float* out_item, const float* r,
-                         int* err) {
+                         int n_groups, const LevelSpan& span, float* out_item, const float* r, int* err) {
   cudaError_t e = level_attr<T, KINDS>(smem);
   if (e != cudaSuccess) return e;
-  k_level<T, KINDS><<<grid, kThreads, smem, s>>>(items, groups, n_groups, first, last, chunk, out_item, r, err);
+  k_level<T, KINDS><<<grid, kThreads, smem, s>>>(items, groups, n_groups, span, out_item, r, err);
   return cudaGetLastError();
 }
 

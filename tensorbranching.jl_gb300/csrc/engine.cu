@@ -94,6 +94,7 @@ struct tb_plan {
   std::vector<float> weights;  // bound vertex weights by label
   DevBuf d_steps, d_tiles, d_gemms, d_leaves, d_small, d_small_leaf;
   DevBuf d_steps_merged, d_gemms_merged;  // the split-K GEMMs merged (PlanHost::steps_merged)
+  DevBuf d_tiny;                          // TinyDesc of each TileDesc (used for the tiny steps)
   bool structure_uploaded = false;
   bool leaves_dirty = false;   // LeafDesc::w on the device is older than the bound weights
   bool i16_ok = false;         // bound weights are integers >= 0 summing below 8192
@@ -165,8 +166,10 @@ struct tb_ctx {
   int64_t n_chunks = 0;
   struct LevelRange {
     int64_t first, count;
-    int kinds;   // 1 stream-like, 2 GEMM
-    int g0, g1;  // its groups [g0, g1) (contiguous: groups are sorted by level and kind)
+    int kinds;     // 1 stream-like, 2 GEMM
+    int g0, g1;    // its groups [g0, g1) (contiguous: groups are sorted by level and kind)
+    int64_t tiny;  // tickets of its tiny steps (listed first)
+    double tiny_cost, rest_cost;  // estimated CTA time of its tiny steps and of the rest (us; level_span)
   };
   std::vector<LevelRange> level_ranges;
   size_t sv_bytes = 0;
@@ -225,6 +228,32 @@ static bool tiny_step(const TileDesc& d) {
   return d.n_tiles == 1 && d.n_loop == 0 && d.n_tc <= kTinyOut && d.n_tr <= kTinyRed && d.n_tc + d.n_tr <= 10;
 }
 
+// tiny_node's form of a tiny step: tensor positions straight from the tile
+// bits (one tile, no grid or loop bits: tile bits cover whole tensors)
+static TinyDesc make_tiny(const TileDesc& d) {
+  TinyDesc t;
+  std::memset(&t, 0xff, sizeof(t));
+  t.a_off = d.a_off;
+  t.b_off = d.b_off;
+  t.c_off = d.c_off;
+  t.n_tc = (int8_t)d.n_tc;
+  t.n_tr = (int8_t)d.n_tr;
+  if (!tiny_step(d)) {
+    t.n_tc = t.n_tr = 0;
+    return t;
+  }
+  for (int b = 0; b < d.n_tc; b++) {
+    t.oa[b] = d.tc_a[b] >= 0 ? d.ta_pos[d.tc_a[b]] : (int8_t)-1;
+    t.ob[b] = d.b_off >= 0 && d.tc_b[b] >= 0 ? d.tb_pos[d.tc_b[b]] : (int8_t)-1;
+    t.oc[b] = d.tc_pos[b];
+  }
+  for (int b = 0; b < d.n_tr; b++) {
+    t.ra[b] = d.tr_a[b] >= 0 ? d.ta_pos[d.tr_a[b]] : (int8_t)-1;
+    t.rb[b] = d.b_off >= 0 && d.tr_b[b] >= 0 ? d.tb_pos[d.tr_b[b]] : (int8_t)-1;
+  }
+  return t;
+}
+
 template <typename T>
 static size_t elem() { return sizeof(T); }
 
@@ -265,11 +294,16 @@ static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
   if (!p->structure_uploaded || (leaf_weights && p->leaves_dirty))
     for (int i : p->vertex_leaves) h.leaves[i].w = p->weights[h.leaves[i].label];
   if (!p->structure_uploaded) {
-    void* before[8] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p,
-                       p->d_steps_merged.p, p->d_gemms_merged.p};
+    void* before[9] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p,
+                       p->d_steps_merged.p, p->d_gemms_merged.p, p->d_tiny.p};
     CU(up(p->d_steps, h.steps.data(), h.steps.size() * sizeof(Step)));
     CU(up(p->d_tiles, h.tiles.empty() ? nullptr : h.tiles.data(), h.tiles.size() * sizeof(TileDesc)));
     CU(up(p->d_gemms, h.gemms.empty() ? nullptr : h.gemms.data(), h.gemms.size() * sizeof(GemmDesc)));
+    {
+      std::vector<TinyDesc> tiny(h.tiles.size());
+      for (size_t k = 0; k < h.tiles.size(); k++) tiny[k] = make_tiny(h.tiles[k]);
+      CU(up(p->d_tiny, tiny.empty() ? nullptr : tiny.data(), tiny.size() * sizeof(TinyDesc)));
+    }
     if (h.has_split) {
       CU(up(p->d_steps_merged, h.steps_merged.data(), h.steps_merged.size() * sizeof(Step)));
       CU(up(p->d_gemms_merged, h.gemms_merged.data(), h.gemms_merged.size() * sizeof(GemmDesc)));
@@ -279,8 +313,8 @@ static tb_status upload_plan(tb_plan* p, bool leaf_weights) {
       CU(up(p->d_small, h.small.empty() ? nullptr : h.small.data(), h.small.size() * sizeof(SmallNode)));
       CU(up(p->d_small_leaf, h.small_leaf.data(), h.small_leaf.size() * sizeof(int32_t)));
     }
-    void* after[8] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p,
-                      p->d_steps_merged.p, p->d_gemms_merged.p};
+    void* after[9] = {p->d_steps.p, p->d_tiles.p, p->d_gemms.p, p->d_leaves.p, p->d_small.p, p->d_small_leaf.p,
+                      p->d_steps_merged.p, p->d_gemms_merged.p, p->d_tiny.p};
     // captured graphs hold these device pointers: a move invalidates them
     if (std::memcmp(before, after, sizeof(before)) != 0) p->version = ++p->ctx->plan_counter;
     p->structure_uploaded = true;
@@ -373,6 +407,18 @@ static std::vector<char> merge_choice(const tb_ctx* c, int n, tb_plan* const* pl
   return m;
 }
 
+// Estimated CTA time (us) of per-level launch work, for level_span's split
+// of a grid between tiny steps and the rest (measured on KSG levels: a warp
+// runs a one-pass tiny step in ~2 us, eight warps at a time, and each further
+// four passes add about as much; a stream step builds its tables in ~3 us
+// and runs each tile of a run in < 1 us).
+constexpr double kGroupCostUs = 3.0;
+constexpr double kTileCostUs = 0.8;
+static double tiny_cost_us(int n_tc, int n_tr) {
+  const int passes = std::max(1, 1 << std::max(0, n_tc + n_tr - 5));
+  return (2.0 + 1.5 * (double)((passes - 1) / 4)) / 8.0;
+}
+
 // The batch's steps in launch order: by tree level, then kind (stream-like
 // before GEMM), tiny steps first, then item and step.  Steps without tiles
 // (the fill and max steps of a merged split-K GEMM) are left out.
@@ -401,8 +447,8 @@ static std::vector<GroupKey> sorted_groups(int n, tb_plan* const* plans, bool sk
 
 // Groups (host copy, gk.size() entries) and one launch range per (level,
 // kind); returns the number of tickets.
-static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plans, const char* merged, Group* hg,
-                           std::vector<tb_ctx::LevelRange>& ranges) {
+static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plans, const char* merged,
+                           const std::vector<void*>& arenas, Group* hg, std::vector<tb_ctx::LevelRange>& ranges) {
   int64_t tk = 0;
   ranges.clear();
   int cur_level = -1, cur_kinds = -1;
@@ -412,11 +458,11 @@ static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plan
     hg[g].step = gk[g].step;
     hg[g].first = tk;
     hg[g].tiny = gk[g].tiny;
-    hg[g].pad_ = 0;
-    hg[g].tile =
-        gk[g].tiny ? reinterpret_cast<const TileDesc*>(p->d_tiles.p) + p->h.steps[gk[g].step].desc : nullptr;
+    hg[g].run = 0;
+    hg[g].tile = gk[g].tiny ? reinterpret_cast<const TinyDesc*>(p->d_tiny.p) + p->h.steps[gk[g].step].desc : nullptr;
+    hg[g].arena = gk[g].tiny ? arenas[gk[g].item] : nullptr;
     if (gk[g].level != cur_level || gk[g].kinds != cur_kinds) {
-      ranges.push_back({tk, 0, gk[g].kinds, (int)g, (int)g});
+      ranges.push_back({tk, 0, gk[g].kinds, (int)g, (int)g, 0, 0.0, 0.0});
       cur_level = gk[g].level;
       cur_kinds = gk[g].kinds;
     }
@@ -424,7 +470,21 @@ static int64_t fill_groups(const std::vector<GroupKey>& gk, tb_plan* const* plan
     tk += nt;
     ranges.back().count += nt;
     ranges.back().g1 = (int)g + 1;
+    if (gk[g].tiny) {
+      const TileDesc& d = p->h.tiles[p->h.steps[gk[g].step].desc];
+      ranges.back().tiny += nt;
+      ranges.back().tiny_cost += tiny_cost_us(d.n_tc, d.n_tr);
+    } else {
+      ranges.back().rest_cost += kGroupCostUs + kTileCostUs * (double)nt;
+    }
   }
+  // run lengths of the tiny groups (listed first in their launch range)
+  for (size_t g = gk.size(); g-- > 0;)
+    if (gk[g].tiny)
+      hg[g].run = 1 + (g + 1 < gk.size() && gk[g + 1].tiny && gk[g + 1].level == gk[g].level &&
+                               gk[g + 1].kinds == gk[g].kinds
+                           ? hg[g + 1].run
+                           : 0);
   return tk;
 }
 template <typename T>
@@ -471,7 +531,9 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   std::vector<GroupKey> gk = sorted_groups(n, plans, skip_leaves, merged.data());
   CU(c->h_groups.ensure(sizeof(Group) * std::max<size_t>(gk.size(), 1)));
   Group* hg = reinterpret_cast<Group*>(c->h_groups.p);
-  const int64_t tk = fill_groups(gk, plans, merged.data(), hg, c->level_ranges);
+  std::vector<void*> arenas(n);
+  for (int i = 0; i < n; i++) arenas[i] = hi[i].arena;
+  const int64_t tk = fill_groups(gk, plans, merged.data(), arenas, hg, c->level_ranges);
   c->n_tickets = tk;
   c->n_groups = (int)gk.size();
   // chunks for the persistent executor: runs of stream tiles (tables are
@@ -533,6 +595,57 @@ static tb_status upload_batch(tb_ctx* c, int n, tb_plan* const* plans, const std
   return TB_OK;
 }
 
+// Grid and ticket span of one per-level launch on at most max_ctas CTAs.
+// A launch whose tiny steps come first gives them and its other tiles CTAs
+// in proportion to their estimated cost, so neither part waits on a few
+// overloaded CTAs (costs in us of one CTA's time, from fill_groups:
+// tiny_cost_us a tiny step, kGroupCostUs + kTileCostUs a tile of the rest).
+static LevelSpan level_span(const tb_ctx::LevelRange& lr, int64_t max_ctas, int64_t& grid) {
+  LevelSpan sp{};
+  sp.first = lr.first;
+  sp.last = lr.first + lr.count;
+  max_ctas = std::max<int64_t>(1, max_ctas);
+  const int64_t tiny = lr.tiny, rest = lr.count - lr.tiny;
+  if (tiny == 0 || rest == 0 || max_ctas < 2) {
+    grid = std::min<int64_t>(lr.count, max_ctas);
+    sp.mid = sp.last;
+    sp.chunk = (lr.count + grid - 1) / grid;
+    sp.chunk2 = 1;
+    sp.split_cta = (int32_t)grid;
+    return sp;
+  }
+  const double wt = std::max(lr.tiny_cost, 1e-3), wr = std::max(lr.rest_cost, 1e-3);
+  int64_t gt = (int64_t)std::llround((double)max_ctas * wt / (wt + wr));
+  gt = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(gt, max_ctas - 1), tiny));
+  const int64_t gr = std::min<int64_t>(max_ctas - gt, rest);
+  sp.mid = lr.first + tiny;
+  sp.chunk = (tiny + gt - 1) / gt;
+  sp.chunk2 = (rest + gr - 1) / gr;
+  sp.split_cta = (int32_t)gt;
+  grid = gt + gr;
+  return sp;
+}
+
+// One per-level launch of the ranges' kernel form on stream s.
+template <typename T>
+static cudaError_t launch_range(const tb_ctx* c, const tb_ctx::LevelRange& lr, cudaStream_t s,
+                                const ItemDev<T>* items, const Group* groups, float* out_item, const float* r,
+                                int* err) {
+  const Group* lg = groups + lr.g0;
+  const int ng = lr.g1 - lr.g0;
+  int64_t grid = 0;
+  if (lr.kinds == 2) {
+    const LevelSpan sp = level_span(lr, c->gemm_ctas, grid);
+    return launch_level<T, 2>((unsigned)grid, smem_bytes(2), s, items, lg, ng, sp, out_item, r, err);
+  }
+  if (c->stream_wide) {
+    const LevelSpan sp = level_span(lr, c->stream_ctas_wide, grid);
+    return launch_level<T, 5>((unsigned)grid, smem_bytes(1), s, items, lg, ng, sp, out_item, r, err);
+  }
+  const LevelSpan sp = level_span(lr, c->stream_ctas, grid);
+  return launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, items, lg, ng, sp, out_item, r, err);
+}
+
 // One launch of the per-level schedule: every tile of one (tree level,
 // kind) of the uploaded batch.
 template <typename T>
@@ -544,22 +657,7 @@ static tb_status enqueue_level(tb_ctx* c, const tb_ctx::LevelRange& lr) {
   int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(c->misc.p) + 16);
   if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
   // the kernel searches only this level's groups (their tickets are absolute)
-  const Group* lg = groups + lr.g0;
-  const int ng = lr.g1 - lr.g0;
-  if (lr.kinds == 2) {
-    const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-    CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
-                           (lr.count + grid - 1) / grid, out_item, rv, err)));
-  } else if (c->stream_wide) {
-    const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas_wide);
-    CU((launch_level<T, 5>((unsigned)grid, smem_bytes(1), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
-                           (lr.count + grid - 1) / grid, out_item, rv, err)));
-  } else {
-    const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-    CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, lg, ng, lr.first, lr.first + lr.count,
-                           (lr.count + grid - 1) / grid, out_item, rv, err)));
-  }
-  CU(cudaGetLastError());
+  CU(launch_range<T>(c, lr, c->stream, items, groups, out_item, rv, err));
   return TB_OK;
 }
 
@@ -1403,19 +1501,7 @@ static tb_status run_single(tb_ctx* c, tb_plan* p, const float* const* leaf_data
     const Group* groups = reinterpret_cast<const Group*>(c->groups.p);
     float* oi = reinterpret_cast<float*>(c->out_item.p);
     for (auto& lr : c->level_ranges) {
-      if (lr.kinds == 2) {
-        const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-        CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
-                               lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
-      } else if (c->stream_wide) {
-        const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas_wide);
-        CU((launch_level<T, 5>((unsigned)grid, smem_bytes(1), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
-                               lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
-      } else {
-        const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-        CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), c->stream, items, groups + lr.g0, lr.g1 - lr.g0,
-                               lr.first, lr.first + lr.count, (lr.count + grid - 1) / grid, oi, nullptr, err)));
-      }
+      CU(launch_range<T>(c, lr, c->stream, items, groups, oi, nullptr, err));
       CU(cudaGetLastError());
     }
   }
@@ -1636,9 +1722,32 @@ extern "C" void tbi_free(void* p) { std::free(p); }
 
 extern "C" int32_t tbi_sizes(int32_t* out, int32_t n) {
   int32_t v[6] = {(int32_t)sizeof(TileDesc), (int32_t)sizeof(Step), (int32_t)sizeof(LeafDesc),
-                  (int32_t)sizeof(FinalDesc), (int32_t)sizeof(GemmDesc), 0};
+                  (int32_t)sizeof(FinalDesc), (int32_t)sizeof(GemmDesc), (int32_t)sizeof(TinyDesc)};
   for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
   return 0;
+}
+
+// Internal: the launch span level_span gives a range of `count` tickets
+// from `first`, the first `tiny` of them tiny steps and the rest one-tile
+// steps, on at most max_ctas CTAs: out7 = {grid, first, mid, last, chunk,
+// chunk2, split_cta}.
+extern "C" int32_t tbi_level_span(int64_t first, int64_t count, int64_t tiny, int64_t max_ctas, int64_t* out7) {
+  if (!out7 || count < 1 || tiny < 0 || tiny > count) return TB_ERR_INVALID;
+  tb_ctx::LevelRange lr{first, count, 1, 0, 0, tiny, (double)tiny * tiny_cost_us(0, 0),
+                        (double)(count - tiny) * (kGroupCostUs + kTileCostUs)};
+  int64_t grid = 0;
+  const LevelSpan sp = level_span(lr, max_ctas, grid);
+  const int64_t v[7] = {grid, sp.first, sp.mid, sp.last, sp.chunk, sp.chunk2, sp.split_cta};
+  for (int i = 0; i < 7; i++) out7[i] = v[i];
+  return TB_OK;
+}
+
+// Internal: the TinyDesc the engine uploads for a stream-tile descriptor;
+// returns 1 when the step runs as a tiny step (tiny_node), else 0.
+extern "C" int32_t tbi_tiny_desc(const TileDesc* d, TinyDesc* out) {
+  if (!d || !out) return TB_ERR_INVALID;
+  *out = make_tiny(*d);
+  return tiny_step(*d) ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -2124,7 +2233,9 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
     hr[i] = qi.r;
   }
   Group* hg = reinterpret_cast<Group*>(sl.h_groups.p);
-  fill_groups(gk, plans.data(), merged.data(), hg, sl.ranges);
+  std::vector<void*> arenas(n);
+  for (int i = 0; i < n; i++) arenas[i] = hi[i].arena;
+  fill_groups(gk, plans.data(), merged.data(), arenas, hg, sl.ranges);
   CU(cudaMemcpyAsync(sl.items.p, hi, sizeof(ItemDev<T>) * n, cudaMemcpyHostToDevice, s));
   if (svn) CU(cudaMemcpyAsync(sl.sv.p, hsv, svn, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(sl.rv.p, hr, sizeof(float) * n, cudaMemcpyHostToDevice, s));
@@ -2137,21 +2248,7 @@ static tb_status serve_launch(Server* S, Server::Slot& sl) {
   const float* drv = reinterpret_cast<const float*>(sl.rv.p);
   for (const auto& lr : sl.ranges) {
     if (lr.count > 0x7fffffffLL) return fail(TB_ERR_UNSUPPORTED, "level too large for one launch");
-    const Group* lg = dg + lr.g0;
-    const int lng = lr.g1 - lr.g0;
-    if (lr.kinds == 2) {
-      const int64_t grid = std::min<int64_t>(lr.count, c->gemm_ctas);
-      CU((launch_level<T, 2>((unsigned)grid, smem_bytes(2), s, di, lg, lng, lr.first, lr.first + lr.count,
-                             (lr.count + grid - 1) / grid, dout, drv, derr)));
-    } else if (c->stream_wide) {
-      const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas_wide);
-      CU((launch_level<T, 5>((unsigned)grid, smem_bytes(1), s, di, lg, lng, lr.first, lr.first + lr.count,
-                             (lr.count + grid - 1) / grid, dout, drv, derr)));
-    } else {
-      const int64_t grid = std::min<int64_t>(lr.count, c->stream_ctas);
-      CU((launch_level<T, 1>((unsigned)grid, smem_bytes(1), s, di, lg, lng, lr.first, lr.first + lr.count,
-                             (lr.count + grid - 1) / grid, dout, drv, derr)));
-    }
+    CU(launch_range<T>(c, lr, s, di, dg, dout, drv, derr));
     S->launches++;
   }
   // results and the error word back to the host, then the completion event

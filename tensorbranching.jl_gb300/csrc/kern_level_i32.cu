@@ -4,14 +4,14 @@
 
 namespace tb {
 
-template cudaError_t launch_level<int32_t, 1>(unsigned, int, cudaStream_t, const ItemDev<int32_t>*, const Group*, int, int64_t,
-                                             int64_t, int64_t, float*, const float*, int*);
+template cudaError_t launch_level<int32_t, 1>(unsigned, int, cudaStream_t, const ItemDev<int32_t>*, const Group*, int,
+                                             const LevelSpan&, float*, const float*, int*);
 template cudaError_t occupancy_level<int32_t, 1>(int*, int);
-template cudaError_t launch_level<int32_t, 2>(unsigned, int, cudaStream_t, const ItemDev<int32_t>*, const Group*, int, int64_t,
-                                             int64_t, int64_t, float*, const float*, int*);
+template cudaError_t launch_level<int32_t, 2>(unsigned, int, cudaStream_t, const ItemDev<int32_t>*, const Group*, int,
+                                             const LevelSpan&, float*, const float*, int*);
 template cudaError_t occupancy_level<int32_t, 2>(int*, int);
-template cudaError_t launch_level<int32_t, 5>(unsigned, int, cudaStream_t, const ItemDev<int32_t>*, const Group*, int, int64_t,
-                                             int64_t, int64_t, float*, const float*, int*);
+template cudaError_t launch_level<int32_t, 5>(unsigned, int, cudaStream_t, const ItemDev<int32_t>*, const Group*, int,
+                                             const LevelSpan&, float*, const float*, int*);
 template cudaError_t occupancy_level<int32_t, 5>(int*, int);
 
 }  // namespace tb

@@ -688,63 +688,61 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
 
 // A tiny stream step (Group::tiny) by one warp, straight from global memory
 // (its operands are a few hundred bytes, so staging would cost more than the
-// reads): lane l computes outputs l, l + 32, ...; an output's operand offsets
-// are sums of one power of two per set bit of its index (distinct tensor
-// positions), and the reduced terms are visited in Gray-code order, one XOR
-// per term.
+// reads).  Lane l takes reduced term r = l mod 2^n_tr of output l >> n_tr of
+// each pass (32 >> n_tr outputs a pass); the loads of four passes are in
+// flight at once, then the terms of each output meet in a shuffle max and
+// lane r = 0 stores it.  An offset is the sum of one power of two per set
+// bit of the output and term indices (distinct tensor positions).
+constexpr int kTinyPassesAtOnce = 4;
+
 template <typename T>
-__device__ __noinline__ void tiny_node(const TileDesc* __restrict__ d, T* __restrict__ arena) {
+__device__ __noinline__ void tiny_node(const TinyDesc* __restrict__ dp, T* __restrict__ arena) {
   const int lane = threadIdx.x & 31;
-  const int n_tc = d->n_tc, n_tr = d->n_tr;
-  const bool hasB = d->b_off >= 0;
-  const T* A = arena + d->a_off;
-  const T* B = arena + (hasB ? d->b_off : 0);
-  T* C = arena + d->c_off;
-  int sa[kTinyOut], sb[kTinyOut], sc[kTinyOut], ra[kTinyRed], rb[kTinyRed];
+  const TinyDesc d = *dp;
+  const int n_tc = d.n_tc, n_tr = d.n_tr;
+  const bool hasB = d.b_off >= 0;
+  const T* A = arena + d.a_off;
+  const T* B = arena + (hasB ? d.b_off : 0);
+  T* C = arena + d.c_off;
+  const int r = lane & ((1 << n_tr) - 1);
+  int ra = 0, rb = 0;
 #pragma unroll
-  for (int b = 0; b < kTinyOut; b++) {
-    sa[b] = sb[b] = sc[b] = 0;
-    if (b < n_tc) {
-      const int xa = d->tc_a[b], xb = d->tc_b[b];
-      if (xa >= 0) sa[b] = 1 << d->ta_pos[xa];
-      if (xb >= 0) sb[b] = 1 << d->tb_pos[xb];
-      sc[b] = 1 << d->tc_pos[b];
+  for (int b = 0; b < kTinyRed; b++)
+    if (b < n_tr && ((r >> b) & 1)) {
+      if (d.ra[b] >= 0) ra += 1 << d.ra[b];
+      if (d.rb[b] >= 0) rb += 1 << d.rb[b];
     }
-  }
+  const int n_out = 1 << n_tc, per = 32 >> n_tr;
+  const int passes = (n_out + per - 1) / per;
+  for (int p0 = 0; p0 < passes; p0 += kTinyPassesAtOnce) {  // the same trip count on every lane
+    T v[kTinyPassesAtOnce];
+    int oc[kTinyPassesAtOnce];
 #pragma unroll
-  for (int b = 0; b < kTinyRed; b++) {
-    ra[b] = rb[b] = 0;
-    if (b < n_tr) {
-      const int xa = d->tr_a[b], xb = d->tr_b[b];
-      if (xa >= 0) ra[b] = 1 << d->ta_pos[xa];
-      if (xb >= 0) rb[b] = 1 << d->tb_pos[xb];
-    }
-  }
-  const int nred = 1 << n_tr;
-  for (int c = lane; c < (1 << n_tc); c += 32) {
-    int oa = 0, ob = 0, oc = 0;
+    for (int k = 0; k < kTinyPassesAtOnce; k++) {
+      const int c = (p0 + k) * per + (lane >> n_tr);
+      v[k] = Trop<T>::neg();
+      oc[k] = 0;
+      if (p0 + k < passes && c < n_out) {
+        int oa = ra, ob = rb;
 #pragma unroll
-    for (int b = 0; b < kTinyOut; b++)
-      if ((c >> b) & 1) {
-        oa |= sa[b];
-        ob |= sb[b];
-        oc |= sc[b];
+        for (int b = 0; b < kTinyOut; b++)
+          if (b < n_tc && ((c >> b) & 1)) {
+            if (d.oa[b] >= 0) oa += 1 << d.oa[b];
+            if (d.ob[b] >= 0) ob += 1 << d.ob[b];
+            oc[k] += 1 << d.oc[b];
+          }
+        v[k] = hasB ? Trop<T>::mac(v[k], __ldcg(A + oa), __ldcg(B + ob)) : __ldcg(A + oa);
       }
-    T acc = Trop<T>::neg();
-    for (int r = 0; r < nred; r++) {
-      acc = hasB ? Trop<T>::mac(acc, __ldcg(A + oa), __ldcg(B + ob)) : Trop<T>::mx(acc, __ldcg(A + oa));
-      const int k = __ffs(r + 1) - 1;  // Gray code: the next term flips reduced bit k
-      int xa = 0, xb = 0;
-#pragma unroll
-      for (int b = 0; b < kTinyRed; b++)
-        if (b == k) {
-          xa = ra[b];
-          xb = rb[b];
-        }
-      oa ^= xa;
-      ob ^= xb;
     }
-    C[oc] = acc;
+#pragma unroll
+    for (int k = 0; k < kTinyPassesAtOnce; k++) {
+      if (p0 + k < passes) {  // warp-uniform
+        T x = v[k];
+        for (int s = 1; s < (1 << n_tr); s <<= 1) x = Trop<T>::mx(x, __shfl_xor_sync(0xffffffffu, x, s));
+        const int c = (p0 + k) * per + (lane >> n_tr);
+        if (r == 0 && c < n_out) C[oc[k]] = x;
+      }
+    }
   }
 }
 

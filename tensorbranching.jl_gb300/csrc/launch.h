@@ -31,8 +31,7 @@ cudaError_t launch_k1_any(const T* A, const T* B, T* C, int64_t M, int64_t N, in
                           cudaStream_t s);
 template <typename T, int KINDS>
 cudaError_t launch_level(unsigned grid, int smem, cudaStream_t s, const ItemDev<T>* items, const Group* groups,
-                         int n_groups, int64_t first, int64_t last, int64_t chunk, float* out_item, const float* r,
-                         int* err);
+                         int n_groups, const LevelSpan& span, float* out_item, const float* r, int* err);
 template <typename T, int KINDS>
 cudaError_t occupancy_level(int* per_sm, int smem);
 template <typename T>

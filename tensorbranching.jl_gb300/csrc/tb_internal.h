@@ -154,19 +154,42 @@ struct ItemDev {
 
 // A group = all tiles of one (item, step); groups are listed in dependency
 // order and tickets index tiles within the concatenation of groups.
-struct Group {
-  int32_t item, step;
-  int64_t first;          // first ticket of this group
-  int32_t tiny;           // 1: a one-tile stream step small enough for one warp (tiny_node)
-  int32_t pad_;
-  const TileDesc* tile;   // its descriptor (device), when tiny
-};
-
 // Stream steps one warp runs straight from global memory (tiny_node): one
 // tile, no reduction loop, at most 2^kTinyOut outputs and 2^kTinyRed reduced
 // terms.
 constexpr int kTinyOut = 8;
 constexpr int kTinyRed = 5;
+
+// A tiny stream step as tiny_node reads it: the operand and output offsets
+// and, per output bit and reduced bit, the tensor position the bit moves in
+// A, B and C (-1: not in that tensor).  Built on the host from the step's
+// TileDesc, so a lane forms its offsets from one 64-byte load.
+struct TinyDesc {
+  int64_t a_off, b_off, c_off;  // b_off < 0: unary
+  int8_t n_tc, n_tr;
+  int8_t oa[kTinyOut], ob[kTinyOut], oc[kTinyOut];
+  int8_t ra[kTinyRed], rb[kTinyRed];
+  int8_t pad_[4];
+};
+static_assert(sizeof(TinyDesc) == 64, "one 64-byte load");
+
+struct Group {
+  int32_t item, step;
+  int64_t first;          // first ticket of this group
+  int32_t tiny;           // 1: a one-tile stream step small enough for one warp (tiny_node)
+  int32_t run;            // tiny: groups from this one to the end of its level's tiny run
+  const TinyDesc* tile;   // its descriptor (device), when tiny
+  void* arena;            // the item's arena (device), when tiny
+};
+
+// The tickets of one per-level launch (k_level): CTAs b < split_cta take
+// runs of `chunk` tickets from `first` up to `mid` (the launch's tiny steps,
+// listed first), CTAs b >= split_cta runs of `chunk2` from `mid` up to
+// `last`.
+struct LevelSpan {
+  int64_t first, mid, last, chunk, chunk2;
+  int32_t split_cta, pad_;
+};
 
 // A unit of work of the persistent executor: tiles [t0, t1) of one group.
 // Chunks are listed in dependency order.

@@ -36,6 +36,15 @@ class TileDesc(ctypes.Structure):
                 ("tr_a", c_int8 * KMAXTILE), ("tr_b", c_int8 * KMAXTILE)]
 
 
+KTINYOUT, KTINYRED = 8, 5
+
+
+class TinyDesc(ctypes.Structure):
+    _fields_ = [("a_off", c_int64), ("b_off", c_int64), ("c_off", c_int64), ("n_tc", c_int8), ("n_tr", c_int8),
+                ("oa", c_int8 * KTINYOUT), ("ob", c_int8 * KTINYOUT), ("oc", c_int8 * KTINYOUT),
+                ("ra", c_int8 * KTINYRED), ("rb", c_int8 * KTINYRED), ("pad_", c_int8 * 4)]
+
+
 class Step(ctypes.Structure):
     _fields_ = [("kind", c_int32), ("desc", c_int32), ("dep0", c_int32), ("dep1", c_int32),
                 ("n_tiles", c_int32), ("level", c_int32)]
@@ -70,8 +79,8 @@ def check_layout(lib):
     out = (c_int32 * 6)()
     lib.tbi_sizes(out, 6)
     want = [ctypes.sizeof(TileDesc), ctypes.sizeof(Step), ctypes.sizeof(LeafDesc), ctypes.sizeof(FinalDesc),
-            ctypes.sizeof(GemmDesc)]
-    assert list(out)[:5] == want, (list(out), want)
+            ctypes.sizeof(GemmDesc), ctypes.sizeof(TinyDesc)]
+    assert list(out) == want, (list(out), want)
 
 
 def describe(lib, code, sliced=(), use_node_iy=False, gemm_min=4, tile_bits=9):
@@ -449,11 +458,53 @@ def to_reported(v, flab, lab):
     return v[x]
 
 
-def run_fused(desc, weights, slice_vals=(), kpart_atomic=False, by_deps=False):
+def tiny_desc(lib, d):
+    """(is tiny, TinyDesc) of a stream-tile descriptor, from the engine."""
+    lib.tbi_tiny_desc.restype = c_int32
+    lib.tbi_tiny_desc.argtypes = [c_void_p, c_void_p]
+    t = TinyDesc()
+    rc = lib.tbi_tiny_desc(ctypes.byref(d), ctypes.byref(t))
+    assert rc in (0, 1)
+    return bool(rc), t
+
+
+def emu_tiny_node(t, arena, written):
+    """tiny_node: lane l of a pass takes term l mod 2^n_tr of output
+    c0 + (l >> n_tr); offsets are sums of 2^position over the set bits of
+    the output and term indices; the terms meet in a max."""
+    n_tc, n_tr = t.n_tc, t.n_tr
+    assert 0 <= n_tc <= KTINYOUT and 0 <= n_tr <= KTINYRED and n_tc + n_tr <= 10
+    hasB = t.b_off >= 0
+
+    def offs(nbits, pos, idx):
+        o = np.zeros(idx.shape, np.int64)
+        for b in range(nbits):
+            if pos[b] >= 0:
+                o += ((idx >> b) & 1) << pos[b]
+        return o
+
+    c = np.arange(1 << n_tc)[:, None]
+    r = np.arange(1 << n_tr)[None, :]
+    oa = offs(n_tc, t.oa, c) + offs(n_tr, t.ra, r)
+    oc = offs(n_tc, t.oc, c)[:, 0]
+    assert len(set(oc.tolist())) == len(oc), "outputs collide"
+    va = arena[t.a_off + oa]
+    assert np.all(written[t.a_off + oa] == 1)
+    if hasB:
+        ob = offs(n_tc, t.ob, c) + offs(n_tr, t.rb, r)
+        assert np.all(written[t.b_off + ob] == 1)
+        va = va + arena[t.b_off + ob]
+    arena[t.c_off + oc] = va.max(axis=1)
+    written[t.c_off + oc] += 1
+
+
+def run_fused(desc, weights, slice_vals=(), kpart_atomic=False, by_deps=False, lib=None):
     """Replay the fused program; returns (root tensor, arena, node views).
     kpart_atomic: split-K parts combine by atomic max of the value bits into
     the output after STEP_FILL (the form for values >= 0 or -inf), instead of
-    partials and STEP_KRED.  by_deps: run the steps in dep_order."""
+    partials and STEP_KRED.  by_deps: run the steps in dep_order.  lib: run
+    the steps the per-level launches take as tiny steps through their
+    TinyDesc (emu_tiny_node), as those launches do."""
     arena = np.full(desc["arena"], np.nan, np.float32)
     written = np.zeros(desc["arena"], np.int32)
     leaves = desc["leaves"]
@@ -489,7 +540,11 @@ def run_fused(desc, weights, slice_vals=(), kpart_atomic=False, by_deps=False):
                 # node j's operands are its children; ranks known from the blob
                 node_of_step[si] = j
                 j += 1
-            emu_stream_tile(d, arena, written)
+            tiny, t = tiny_desc(lib, d) if lib is not None and st.kind == STEP_TILE else (False, None)
+            if tiny:
+                emu_tiny_node(t, arena, written)
+            else:
+                emu_stream_tile(d, arena, written)
         elif st.kind == STEP_GEMM:
             emu_gemm_step(desc["gemms"][st.desc], arena, written, kpart_atomic)
     fin = desc["fin"]

@@ -14,13 +14,37 @@ def lib(native):
 
 
 def _check(lib, orc, code, w, sliced=(), sv=()):
-    root, nodes = emulate.run_fused(emulate.describe(lib, code, sliced), w, sv)
+    """The fused program with every stream step as a stream tile (the
+    persistent executor) and with the small ones as tiny steps (the per-level
+    launches), and the plain program, against the oracle."""
+    d = emulate.describe(lib, code, sliced)
+    root, nodes = emulate.run_fused(d, w, sv)
+    roott, nodest = emulate.run_fused(d, w, sv, lib=lib)
     rootp, nodesp = emulate.run_plain(emulate.describe(lib, code, sliced), w, sv)
     ref, dumps = orc.execute(code, w, sliced=sliced, slice_vals=sv, dump=True)
-    assert np.array_equal(root, ref) and np.array_equal(rootp, ref)
-    for a, b, c in zip(nodes, nodesp, dumps or []):
-        assert np.array_equal(a, c) and np.array_equal(b, c)
+    assert np.array_equal(root, ref) and np.array_equal(roott, ref) and np.array_equal(rootp, ref)
+    for a, t, b, c in zip(nodes, nodest, nodesp, dumps or []):
+        assert np.array_equal(a, c) and np.array_equal(t, c) and np.array_equal(b, c)
     return float(np.max(ref))
+
+
+@pytest.mark.parametrize("case", ["ksg", (2, 2, 3, 0), (1, 1, 5, 0), (3, 2, 4, 1)])
+def test_tiny_steps(tb, orc, lib, case):
+    """Tiny steps (one warp each, straight from global memory): the small
+    nodes of a King's subgraph network, and middle nodes reducing 2^3 to 2^5
+    terms (lanes over outputs and terms, a shuffle max per output); their
+    TinyDesc offsets give the oracle's intermediates."""
+    from cases import gemm_case
+
+    g, w, code = ksg_case(tb, 6, 3) if case == "ksg" else gemm_case(tb, *case)
+    d = emulate.describe(lib, code)
+    tiny = [emulate.tiny_desc(lib, d["tiles"][s.desc]) for s in d["steps"] if s.kind == emulate.STEP_TILE]
+    tiny = [t for ok, t in tiny if ok]
+    if case == "ksg":
+        assert len(tiny) > 10
+    else:
+        assert max(t.n_tr for t in tiny) == case[2]
+    _check(lib, orc, code, w)
 
 
 @pytest.mark.parametrize("seed", range(4))
@@ -229,3 +253,34 @@ def test_small_form_branch_batch(tb, orc, lib):
         if b.code is None or b.p.g.n == 0:
             continue
         _check_small(lib, orc, b.code, b.p.weight_array(), r=b.r)
+
+
+def test_level_spans(lib):
+    """Every ticket of a per-level launch goes to exactly one CTA, and the
+    CTAs given to the tiny steps (listed first) take no other tile: k_level's
+    split of its grid (LevelSpan) over random ranges."""
+    import ctypes
+
+    lib.tbi_level_span.restype = ctypes.c_int32
+    lib.tbi_level_span.argtypes = [ctypes.c_int64] * 4 + [ctypes.c_void_p]
+    rng = np.random.default_rng(0)
+    cases = [(1, 0, 304), (1, 1, 304), (5, 5, 1), (13290, 11735, 304), (2000, 3, 304), (300, 297, 304)]
+    cases += [(int(c), int(rng.integers(0, c + 1)), int(rng.integers(1, 700)))
+              for c in rng.integers(1, 20000, 40)]
+    for count, tiny, ctas in cases:
+        out = np.zeros(7, np.int64)
+        assert lib.tbi_level_span(100, count, tiny, ctas, out.ctypes.data) == 0
+        grid, first, mid, last, chunk, chunk2, split = (int(x) for x in out)
+        assert 1 <= grid <= ctas and first == 100 and last == 100 + count and 0 <= split <= grid
+        if 0 < tiny < count and ctas >= 2:
+            assert mid == 100 + tiny and 0 < split < grid  # the tiny CTAs end at the last tiny step
+        hits = np.zeros(count, np.int64)
+        for b in range(grid):
+            if b < split:
+                t0, t1 = first + b * chunk, min(first + (b + 1) * chunk, mid)
+            else:
+                t0 = mid + (b - split) * chunk2
+                t1 = min(t0 + chunk2, last)
+            if t0 < t1:
+                hits[t0 - 100:t1 - 100] += 1
+        assert np.all(hits == 1), (count, tiny, ctas)
