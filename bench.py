@@ -401,15 +401,21 @@ def measure(tb, eng, wl, name, args, steps, warmup, plain_steps, flush, dev, ws,
     if len(uplans) > 1:
         w_offs[1:] = np.cumsum([len(w) for w in host_w[:-1]])
     w_flat = np.ascontiguousarray(np.concatenate(host_w), np.float32)  # the caller's host buffer
+    # at least 0.2 s of end-to-end steps (short steps: a few steps would
+    # weigh one host hiccup too much)
+    e2e_steps = max(steps, min(1000, int(0.2 / max(t_dev / steps, 1e-6))))
     if ws > 1:
+        t_es = torch.tensor([e2e_steps], dtype=torch.int64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t_es, op=torch.distributed.ReduceOp.MAX)
+        e2e_steps = int(t_es[0])
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    for _ in range(steps):
+    for _ in range(e2e_steps):
         eng.bind_batch(uplans, w_flat, w_offs)
         o, m = step()
         if not np.array_equal(o, out0):
             raise AssertionError(f"{name}: an end-to-end step's item values changed")
-    t_e2e = time.perf_counter() - t0
+    t_e2e = (time.perf_counter() - t0) * steps / e2e_steps  # per `steps` steps, as t_dev
     if ws > 1:
         tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=f"cuda:{dev}")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -424,7 +430,7 @@ def measure(tb, eng, wl, name, args, steps, warmup, plain_steps, flush, dev, ws,
            "tropical_gops": ops / t_step / 1e9, "gpu_launches": launches,
            "items_per_s": ws * steps * len(plans) / t_dev,
            "e2e": {"value": ws * steps * units / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                   "d2h_bytes_per_step": d2h},
+                   "d2h_bytes_per_step": d2h, "steps": e2e_steps},
            "clocks": clk.summary()}
     # the step as a whole against the node-weighted roofline
     step_roof = {"attainable_frac": t_bound / t_step, "algorithmic_ops": r_ops, "algorithmic_bytes": r_bytes}
