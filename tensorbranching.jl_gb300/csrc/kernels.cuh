@@ -1042,6 +1042,9 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -1061,7 +1064,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 template <int BM, int BN, int S = kGemmStages, int BK = kGemmBK, bool I16 = false>
 struct GemmSmem {
   static constexpr int KP = BK / 2;
-  static constexpr int BAR_BYTES = 128;  // full[S] mbarriers (room for 16)
+  static constexpr int BAR_BYTES = 256;  // full[S] then empty[S] mbarriers (room for 16 stages)
   static constexpr int A_STAGE = KP * BM * 2;  // elements
   static constexpr int B_STAGE = KP * BN * 2;
   static constexpr int SCAT_OFF = BAR_BYTES + S * (A_STAGE + B_STAGE) * 4;  // epilogue tables
@@ -1131,11 +1134,22 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   const int nkp_log2 = d.k_log2 - BK_LOG2 - d.ks_log2;  // chunks of one unit
   const int n_units = (int)(u1 - u0);
   const int total_q = n_units << nkp_log2;
+  // K = 16 (one chunk a unit, deep rings) with tiles of 64 x 64 or more: no
+  // block barrier per chunk; each warp arrives on the stage's empty barrier
+  // when done with it, and thread 0 refills the stage of the previous chunk
+  // once all eight have (by then they usually have).  Measured on rr300w's
+  // K = 16 levels: 128 x 128 tiles 1.88 -> 1.56 ms, but the skinny 256 x 16
+  // tiles (shared-load bound) 2.98 -> 3.18 ms, so those keep the barrier.
+  constexpr bool DEFER = BK == 16 && !I16 && BM >= 64 && BN >= 64;
+  uint64_t* empty = full + 16;
 
   __syncthreads();  // the previous user of this shared memory is done
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (t == 0)
-    for (int i = 0; i < S; i++) mbar_init(&full[i], 1);
+    for (int i = 0; i < S; i++) {
+      mbar_init(&full[i], 1);
+      if (DEFER) mbar_init(&empty[i], kThreads / 32);
+    }
   // C offsets of the tile's rows / columns from their low bits: the scatter
   // is linear over disjoint bits, so a unit adds only its (m0, n0, b) base
   for (int i = t; i < BM; i += kThreads) {
@@ -1206,14 +1220,30 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
         // while this one's adds and maxes run
 #pragma unroll 2
         for (int kp = 0; kp < KP; kp++) mp_step<T, TM, TN, BM, BN>(as, bs, kp, wm, wn, lm, ln, acc);
-        // every warp is done with this stage: thread 0 refills it at once (a
-        // block barrier per chunk measured faster than per-warp arrivals on
-        // an empty barrier that thread 0 waits on)
-        __syncthreads();
-        if (t == 0 && q + S < total_q && ok) {
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // reads above, then async writes
-          gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
-          issued = q + S + 1;
+        if constexpr (DEFER) {
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&empty[slot]);
+          // chunk q - 1's stage takes chunk q - 1 + S
+          const int pq = q - 1;
+          if (t == 0 && pq >= 0 && pq + S < total_q && ok) {
+            const int ps = slot == 0 ? S - 1 : slot - 1;
+            ok = mbar_wait(&empty[ps], (uint32_t)((pq / S) & 1));
+            if (ok) {
+              asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // reads above, then async writes
+              gemm_issue<T, BM, BN, S, BK>(d, u0, pq + S, ps, arena, smem);
+              issued = pq + S + 1;
+            }
+          }
+        } else {
+          // every warp is done with this stage: thread 0 refills it at once (a
+          // block barrier per chunk measured faster than per-warp arrivals on
+          // an empty barrier that thread 0 waits on, with 32-wide chunks)
+          __syncthreads();
+          if (t == 0 && q + S < total_q && ok) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // reads above, then async writes
+            gemm_issue<T, BM, BN, S, BK>(d, u0, q + S, slot, arena, smem);
+            issued = q + S + 1;
+          }
         }
       }
       if (++slot == S) {
@@ -1283,8 +1313,12 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
     __syncthreads();
     return false;
   }
+  // (the barrier of __syncthreads_or above: every warp's arrivals are in)
   if (t == 0)
-    for (int i = 0; i < S; i++) mbar_inval(&full[i]);
+    for (int i = 0; i < S; i++) {
+      mbar_inval(&full[i]);
+      if (DEFER) mbar_inval(&empty[i]);
+    }
   return true;
 }
 
@@ -1354,6 +1388,6 @@ static_assert(GemmSmem<128, 128, 6, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<256, 16, 5, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<16, 256, 5, 16>::BYTES <= gemm_smem_bytes_max(),
               "K=16 GEMM stages exceed the shared memory of the 128 x 128 form");
-static_assert(16 * 8 <= 128, "full mbarriers of 16 stages");
+static_assert(2 * 16 * 8 <= GemmSmem<16, 16>::BAR_BYTES, "full and empty mbarriers of 16 stages");
 
 }  // namespace tb
