@@ -78,10 +78,16 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
       tk = span.mid + (int64_t)(b - span.split_cta) * span.chunk2;
       end = tk + span.chunk2 < span.last ? tk + span.chunk2 : span.last;
     }
+    // launched with programmatic stream serialization (launch_level): the
+    // next level may launch once every CTA of this one has started, and
+    // waits for this grid's completion before its first access to the arena
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (tk >= end) return;
     // the first group by binary search, then the following ones in order
-    // (the index lives in shared memory, not across the tile code's registers)
+    // (the index lives in shared memory, not across the tile code's registers);
+    // groups and descriptors come from the host, the arena from earlier levels
     if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     __syncthreads();
     while (tk < end) {
       const int gi = s_g;
@@ -353,7 +359,21 @@ cudaError_t launch_level(unsigned grid, int smem, cudaStream_t s, const ItemDev<
                          int n_groups, const LevelSpan& span, float* out_item, const float* r, int* err) {
   cudaError_t e = level_attr<T, KINDS>(smem);
   if (e != cudaSuccess) return e;
-  k_level<T, KINDS><<<grid, kThreads, smem, s>>>(items, groups, n_groups, span, out_item, r, err);
+  // programmatic dependent launch: this level's CTAs may start (and find
+  // their first group) while the previous level drains; k_level waits on
+  // the previous grid before it touches the arena
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, k_level<T, KINDS>, items, groups, n_groups, span, out_item, r, err);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
