@@ -79,15 +79,15 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
       end = tk + span.chunk2 < span.last ? tk + span.chunk2 : span.last;
     }
     // launched with programmatic stream serialization (launch_level): the
-    // next level may launch once every CTA of this one has started, and
-    // waits for this grid's completion before its first access to the arena
+    // next level may launch once every CTA of this one has started; each
+    // path below waits for the previous grid's completion (dep_wait) before
+    // its first access to the arena or the outputs, after the setup that
+    // reads only host-written groups and descriptors
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (tk >= end) return;
     // the first group by binary search, then the following ones in order
-    // (the index lives in shared memory, not across the tile code's registers);
-    // groups and descriptors come from the host, the arena from earlier levels
+    // (the index lives in shared memory, not across the tile code's registers)
     if (threadIdx.x == 0) s_g = find_group(groups, n_groups, tk);
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     __syncthreads();
     while (tk < end) {
       const int gi = s_g;
@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
         // in their level) up to the CTA's last ticket or the level's last
         // tiny step: warp w takes the run's steps w, w + 8, ...
         const int n = (int)(g.run < end - tk ? g.run : end - tk);
+        dep_wait();
         for (int q = threadIdx.x >> 5; q < n; q += kThreads / 32) {
           const Group& gq = groups[gi + q];
           tiny_node<T>(gq.tile, reinterpret_cast<T*>(gq.arena));
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(kThreads, KINDS == 1 ? 3 : 2) k_level(const It
                                  (it.flags & 1) != 0, (it.flags & 2) != 0))
             return;
         } else {
+          dep_wait();
           for (int64_t x = tk; x < g_end; x++) run_small_step<T>(it, st, x - g_first, out_item, r, g.item);
         }
         tk = g_end;

@@ -88,6 +88,12 @@ struct Vec2<float> { using type = float2; };
 template <>
 struct Vec2<int32_t> { using type = int2; };
 
+// Wait for the grid this one depends on programmatically (the previous
+// per-level launch) to complete and its memory to be visible; returns at
+// once after the first call, and in launches without that dependency.
+// Every read or write of the arena in a per-level launch comes after it.
+__device__ __forceinline__ void dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ uint64_t globaltimer() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -650,7 +656,9 @@ __device__ void stream_tiles(const TileDesc& dg, int64_t t0, int64_t t1, T* __re
       }
     }
   }
-  // prologue: items 0 .. S-2, one commit group each (empty past the end)
+  // prologue: items 0 .. S-2, one commit group each (empty past the end);
+  // the arena's first access (the tables above read only the descriptor)
+  dep_wait();
   for (int k = 0; k < R.S - 1; k++) R.refill();
   if (fixed) {
     switch (shape) {
@@ -1166,6 +1174,7 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   }
   __syncthreads();
   int issued = 0;
+  dep_wait();  // the arena's first access (the tables above read only the descriptor)
   if (t == 0)
     for (; issued < S && issued < total_q; issued++) gemm_issue<T, BM, BN, S, BK>(d, u0, issued, issued, arena, smem);
 
