@@ -806,10 +806,29 @@ struct K1Cfg {
 // Rows of a thread: two halves of H rows; within a half, pairs of rows sit at
 // lm * 2 so the 8 m-lanes of a warp read 8 consecutive 16-byte chunks (one
 // conflict-free wavefront per 128-bit shared load).
+// The skinny tiles (256 x 16, 16 x 256) instead give each thread a 4 x 4
+// block of consecutive rows and columns: 64 groups along the long side (warp
+// w, lanes >> 2) by 4 along the short one (lanes & 3), so every shared pair
+// a thread loads serves four accumulators.
+template <int BM, int BN>
+struct GemmShape {
+  static constexpr bool SKINNY_M = BM == 256 && BN == 16, SKINNY_N = BM == 16 && BN == 256;
+  static constexpr int TM = SKINNY_M || SKINNY_N ? 4 : BM / 16;
+  static constexpr int TN = SKINNY_M || SKINNY_N ? 4 : BN / 16;
+  // (wm, wn, lm, ln) of gm_row / gm_col for thread lane of warp
+  __host__ __device__ static constexpr int wm(int warp) { return SKINNY_M ? warp : SKINNY_N ? 0 : warp & 1; }
+  __host__ __device__ static constexpr int wn(int warp) { return SKINNY_M ? 0 : SKINNY_N ? warp : warp >> 1; }
+  __host__ __device__ static constexpr int lm(int lane) { return SKINNY_M ? lane >> 2 : SKINNY_N ? lane & 3 : lane & 7; }
+  __host__ __device__ static constexpr int ln(int lane) { return SKINNY_M ? lane & 3 : SKINNY_N ? lane >> 2 : lane >> 3; }
+};
 template <int TM, int BM>
-__device__ __forceinline__ int gm_row(int wm, int lm, int i) {
+__host__ __device__ constexpr int gm_row(int wm, int lm, int i) {
   constexpr int H = TM >= 2 ? TM / 2 : 1;
-  if constexpr (H >= 2) {
+  if constexpr (BM == 256 && TM == 4) {
+    return (wm * 8 + lm) * 4 + i;  // skinny 256 x 16
+  } else if constexpr (BM == 16 && TM == 4) {
+    return lm * 4 + i;  // skinny 16 x 256
+  } else if constexpr (H >= 2) {
     const int q = i % H;
     return wm * (BM / 2) + (i / H) * (BM / 4) + (q / 2) * 16 + lm * 2 + (q % 2);
   } else {
@@ -817,9 +836,35 @@ __device__ __forceinline__ int gm_row(int wm, int lm, int i) {
   }
 }
 template <int TN, int BN>
-__device__ __forceinline__ int gm_col(int wn, int ln, int j) {
+__host__ __device__ constexpr int gm_col(int wn, int ln, int j) {
   constexpr int H = TN >= 2 ? TN / 2 : 1;
-  return wn * (BN / 4) + (j / H) * (BN / 8) + ln * H + (j % H);
+  if constexpr (BN == 16 && TN == 4) {
+    return ln * 4 + j;  // skinny 256 x 16
+  } else if constexpr (BN == 256 && TN == 4) {
+    return (wn * 8 + ln) * 4 + j;  // skinny 16 x 256
+  } else {
+    return wn * (BN / 4) + (j / H) * (BN / 8) + ln * H + (j % H);
+  }
+}
+// Every (row, column) of a BM x BN tile is one thread's accumulator exactly
+// once, and a thread's rows i, i + 1 (i even) are adjacent when TM >= 4 (the
+// paired stores of the epilogue rely on it).
+template <int BM, int BN>
+__host__ __device__ constexpr bool gm_covers() {
+  using G = GemmShape<BM, BN>;
+  constexpr int TM = G::TM, TN = G::TN;
+  if (TM * TN * 256 != BM * BN) return false;
+  bool seen[BM * BN] = {};
+  for (int t = 0; t < 256; t++)
+    for (int i = 0; i < TM; i++)
+      for (int j = 0; j < TN; j++) {
+        const int r = gm_row<TM, BM>(G::wm(t >> 5), G::lm(t & 31), i);
+        const int c = gm_col<TN, BN>(G::wn(t >> 5), G::ln(t & 31), j);
+        if (r < 0 || r >= BM || c < 0 || c >= BN || seen[r * BN + c]) return false;
+        seen[r * BN + c] = true;
+        if (TM >= 4 && i % 2 == 0 && gm_row<TM, BM>(G::wm(t >> 5), G::lm(t & 31), i + 1) != r + 1) return false;
+      }
+  return true;
 }
 
 // One k-pair step of the register tile: shared tiles hold [kp][x][2].  The
@@ -1127,8 +1172,9 @@ template <typename T, int BM, int BN, int S = kGemmStages, int BK = kGemmBK, boo
 __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restrict__ arena, int* __restrict__ smem,
                            int* err, bool kpart_atomic = false) {
   using SM = GemmSmem<BM, BN, S, BK, I16>;
+  using G = GemmShape<BM, BN>;
   constexpr int KP = SM::KP;
-  constexpr int TM = BM / 16, TN = BN / 16;
+  constexpr int TM = G::TM, TN = G::TN;
   static_assert(!I16 || std::is_same<T, float>::value, "packed int16 tiles stand in for f32 values");
   using Acc = typename std::conditional<I16, uint32_t, T>::type;
   constexpr int BK_LOG2 = BK == 32 ? 5 : 4;
@@ -1187,7 +1233,7 @@ __device__ bool gemm_tiles(const GemmDesc& d, int64_t u0, int64_t u1, T* __restr
   int q = 0;
   for (int ui = 0; ui < n_units; ui++) {
     const int warp = t >> 5, lane = t & 31;
-    const int wm = warp & 1, wn = warp >> 1, lm = lane & 7, ln = lane >> 3;
+    const int wm = G::wm(warp), wn = G::wn(warp), lm = G::lm(lane), ln = G::ln(lane);
     Acc acc[TM][TN];
 #pragma unroll
     for (int i = 0; i < TM; i++)
@@ -1398,5 +1444,8 @@ static_assert(GemmSmem<128, 128, 6, 16>::BYTES <= gemm_smem_bytes_max() &&
                   GemmSmem<16, 256, 5, 16>::BYTES <= gemm_smem_bytes_max(),
               "K=16 GEMM stages exceed the shared memory of the 128 x 128 form");
 static_assert(2 * 16 * 8 <= GemmSmem<16, 16>::BAR_BYTES, "full and empty mbarriers of 16 stages");
+static_assert(gm_covers<128, 128>() && gm_covers<128, 64>() && gm_covers<64, 128>() && gm_covers<64, 64>() &&
+                  gm_covers<32, 32>() && gm_covers<16, 16>() && gm_covers<256, 16>() && gm_covers<16, 256>(),
+              "GEMM tile thread layouts");
 
 }  // namespace tb
