@@ -320,14 +320,17 @@ def workload_config(wl, name):
             "sliced_labels": len(wl["sliced"]), "l2": "flushed between steps (256 MiB write)"}
 
 
-def level_roofline(prof, simt, hbm, simt_i16=None):
+def level_roofline(prof, simt, hbm, simt_i16=None, stream_wide=True):
     """Per-kernel roofline from a per-launch profile: the GEMM-tile launches
     (k_level<float, 2>) against the SIMT max-plus peak of their form, the
-    stream-tile launches (k_level<float, 1>) against HBM; the dominant kernel
-    is the one with the larger share of device time."""
+    stream-tile launches (k_level<float, 5>, the 128-register form, or
+    k_level<float, 1>) against HBM; the dominant kernel is the one with the
+    larger share of device time."""
     tot = sum(p["ms"] for p in prof) or 1e-9
     out = {}
-    for kind, name in (("gemm", "k_level<float,2> (GEMM tiles)"), ("stream", "k_level<float,1> (stream tiles)")):
+    stream_name = ("k_level<float,5> (stream tiles, 128-register form)" if stream_wide else
+                   "k_level<float,1> (stream tiles, 80-register form)")
+    for kind, name in (("gemm", "k_level<float,2> (GEMM tiles)"), ("stream", stream_name)):
         ps = [p for p in prof if p["kind"] == kind]
         if not ps:
             continue
@@ -450,7 +453,7 @@ def measure(tb, eng, wl, name, args, steps, warmup, plain_steps, flush, dev, ws,
             torch.cuda.synchronize()
             runs.append(eng.profile_levels(plans, slice_vals=svs, r=rs))
         prof = [dict(p, ms=float(np.mean([r[k]["ms"] for r in runs]))) for k, p in enumerate(runs[0])]
-        res["kernels"] = level_roofline(prof, simt, hbm, simt_i16 if i16 else None)
+        res["kernels"] = level_roofline(prof, simt, hbm, simt_i16 if i16 else None, eng.stream_wide())
     if plain_steps > 0:
         # the drop-in path on the same items: one item at a time, per-node
         # launches (permute + K1 GEMM + permute), a result read-back per item.

@@ -1810,6 +1810,14 @@ extern "C" int32_t tbi_ctx_set_stream_wide(tb_ctx* c, int32_t wide) {
   return TB_OK;
 }
 
+// The stream form the per-level launches use now: 1 for the 128-register
+// k_level<T, 5>, 0 for the 80-register k_level<T, 1>, negative on error.
+extern "C" int32_t tbi_ctx_stream_wide(tb_ctx* c) {
+  if (!c) return TB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  return c->stream_wide ? 1 : 0;
+}
+
 // Split-K parts by atomic max into the output where every value is >= 0 or
 // -inf (1), or through partials and a max step (0), as the autotuner may
 // choose; for tests that pin one.

@@ -184,6 +184,18 @@ class Engine:
         f.argtypes = [c_void_p, c_int32]
         _native.check(f(self.ctx, 1 if wide else 0), self.ctx)
 
+    def stream_wide(self) -> bool:
+        """Whether the per-level launches run the 128-register stream form
+        (k_level<T, 5>) rather than the 80-register one (k_level<T, 1>)
+        (tbi_ctx_stream_wide, an internal engine symbol)."""
+        f = self.lib.tbi_ctx_stream_wide
+        f.restype = c_int32
+        f.argtypes = [c_void_p]
+        v = f(self.ctx)
+        if v < 0:
+            _native.check(v, self.ctx)
+        return bool(v)
+
     def set_kpart_atomic(self, atomic: bool) -> None:
         """Split-K GEMM parts by atomic max into the output where every value
         is >= 0 or -inf (True) or through partials and a max step (False), as
