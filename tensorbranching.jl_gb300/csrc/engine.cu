@@ -409,14 +409,16 @@ static std::vector<char> merge_choice(const tb_ctx* c, int n, tb_plan* const* pl
 
 // Estimated CTA time (us) of per-level launch work, for level_span's split
 // of a grid between tiny steps and the rest (measured on KSG levels: a warp
-// runs a one-pass tiny step in ~2 us, eight warps at a time, and each further
-// four passes add about as much; a stream step builds its tables in ~3 us
-// and runs each tile of a run in < 1 us).
+// runs a one-pass tiny step in ~2 us and each further four passes add about
+// as much, with eight warps a CTA; a stream step builds its tables in ~3 us
+// and runs each tile of a run in < 1 us).  The tiny share is counted as if
+// six warps shared the tiny steps: the split measured best that way on the
+// King's-subgraph batches (ksg32_b20 22.0 -> 21.5 ms against eight).
 constexpr double kGroupCostUs = 3.0;
 constexpr double kTileCostUs = 0.8;
 static double tiny_cost_us(int n_tc, int n_tr) {
   const int passes = std::max(1, 1 << std::max(0, n_tc + n_tr - 5));
-  return (2.0 + 1.5 * (double)((passes - 1) / 4)) / 8.0;
+  return (2.0 + 1.5 * (double)((passes - 1) / 4)) / 6.0;
 }
 
 // The batch's steps in launch order: by tree level, then kind (stream-like
