@@ -284,3 +284,29 @@ def test_level_spans(lib):
             if t0 < t1:
                 hits[t0 - 100:t1 - 100] += 1
         assert np.all(hits == 1), (count, tiny, ctas)
+
+
+@pytest.mark.parametrize("name", ["rr220", "rr220w_s22", "rr300w_s22"])
+def test_merged_form_of_workload_plans(tb, lib, name):
+    """The merged split-K form of the benchmark workloads' plans (the form a
+    batch that fills the GPU runs): no step with tiles waits on a step
+    without tiles (the persistent executor counts those as done at once, so
+    such a wait would be no wait), each merged GEMM covers the whole K into
+    its node's output and waits on the step that wrote its A operand."""
+    from tensorbranching_gb300 import workloads
+
+    wl = workloads.load(name)
+    it = workloads.step_items(wl, 1)[0]
+    d = emulate.describe(lib, it["code"], it["fixed"], tile_bits=10)
+    steps, merged = d["steps"], d["steps_merged"]
+    split = [k for k, s in enumerate(steps) if s.kind == emulate.STEP_GEMM and d["gemms"][s.desc].ks_log2 > 0]
+    assert split  # each of these plans splits K at one GEMM node for one item alone
+    for k, s in enumerate(merged):
+        if s.n_tiles > 0:
+            for dep in (s.dep0, s.dep1):
+                assert dep < 0 or merged[dep].n_tiles > 0, (name, k, dep)
+    for k in split:
+        g0, g1 = d["gemms"][steps[k].desc], d["gemms_merged"][steps[k].desc]
+        assert g1.ks_log2 == 0 and g1.c_off == g0.c_fin and merged[k].n_tiles == g0.n_tiles >> g0.ks_log2
+        fill = steps[steps[k].dep0]
+        assert fill.kind == emulate.STEP_FILL and merged[k].dep0 == fill.dep0
